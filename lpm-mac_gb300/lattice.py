@@ -1,0 +1,154 @@
+"""Lattice geometry, unit cells and bond lists (host-side set-up).
+
+The unit-cell table restates unit_cell.h:27-127; the point generators follow
+the row/column rules of utilities.h (createPlateHEX2D :118-168,
+createCuboidSC3D :170-211), anchored at the origin; the bond rule is
+Assembly::createBonds (assembly.h:212-234): a directed bond i -> j for every
+j != i with |x_i - x_j| < 1.01 * cutoff[1], layer 0 when it is also below
+1.01 * cutoff[0].  Bonds come out ordered by (i, j), which is the order
+createBonds pushes them into Particle::bond_layers.
+"""
+import math
+
+import numpy as np
+
+SQUARE2D, HEXAGON2D, SIMPLECUBIC3D, FCC3D, BCC3D = "Square2D", "Hexagon2D", "SimpleCubic3D", "FCC3D", "BCC3D"
+
+
+class UnitCell:
+    """Per-lattice constants of unit_cell.h (same names as the reference)."""
+
+    # el_mapping data as written in unit_cell.h, row by row
+    _TABLE = {
+        SQUARE2D: dict(data=[1 / 2, -1 / 2, 0, 0, 0, 1 / 2, 0, 1 / 12, -1 / 12], dim=2, nneighbors=8,
+                       nneighbors1=4, nneighbors2=4, cut=(2.0, 2.0 * math.sqrt(2.0)), afem=(16, 12, 12),
+                       vol=lambda r: 4 * r ** 2),
+        HEXAGON2D: dict(data=[math.sqrt(3.0) / 12.0, -math.sqrt(3.0) / 12.0, 0, -math.sqrt(3.0) / 144.0,
+                              math.sqrt(3.0) / 48.0, 0, 0, 0, 1.0], dim=2, nneighbors=12, nneighbors1=6,
+                        nneighbors2=6, cut=(2.0, 2.0 * math.sqrt(3.0)), afem=(30, 18, 18),
+                        vol=lambda r: 2 * math.sqrt(3) * r ** 2),
+        SIMPLECUBIC3D: dict(data=[1, -1, -1.0, 0, 0, 1.0, 0, 1 / 18.0, -1 / 18.0], dim=3, nneighbors=18,
+                            nneighbors1=6, nneighbors2=12, cut=(2.0, 2.0 * math.sqrt(2.0)), afem=(60, 24, 54),
+                            vol=lambda r: (2 * r) ** 3),
+        FCC3D: dict(data=[0, 0, math.sqrt(2.0), math.sqrt(2.0) / 4, -math.sqrt(2.0) / 4, -math.sqrt(2.0) / 4, 0,
+                          math.sqrt(2.0) / 24, -math.sqrt(2.0) / 24], dim=3, nneighbors=18, nneighbors1=12,
+                    nneighbors2=6, cut=(2.0, 2.0 * math.sqrt(2.0)), afem=(60, 54, 24),
+                    vol=lambda r: 4.0 * math.sqrt(2.0) * r ** 3),
+        BCC3D: dict(data=[0, 0, math.sqrt(3.0), 1 / math.sqrt(3.0), -1 / math.sqrt(3.0), 0, 0, math.sqrt(3.0) / 14,
+                          math.sqrt(3.0) / 14], dim=3, nneighbors=14, nneighbors1=8, nneighbors2=6,
+                    cut=(2.0, 4.0 / math.sqrt(3.0)), afem=(40, 34, 24),
+                    vol=lambda r: 32.0 * math.sqrt(3.0) / 9.0 * r ** 3),
+    }
+
+    def __init__(self, lattice, radius):
+        t = self._TABLE[lattice]
+        self.lattice = lattice
+        self.radius = float(radius)
+        self.dim = t["dim"]
+        self.nneighbors = t["nneighbors"]
+        self.nneighbors1 = t["nneighbors1"]
+        self.nneighbors2 = t["nneighbors2"]
+        self.nneighbors_AFEM, self.nneighbors_AFEM1, self.nneighbors_AFEM2 = t["afem"]
+        self.neighbor_cutoff = [t["cut"][0] * radius, t["cut"][1] * radius]
+        self.particle_volume = t["vol"](radius)
+        self._data = np.array(t["data"], dtype=np.float64)
+
+    def el_mapping(self, layout="reference"):
+        """3x3 mapping from (C11, C12, C44) to (Kn, Tv) terms.
+
+        ``reference``: the matrix the reference builds, Eigen::Map over the
+        written data, which reads it column by column (unit_cell.h:49 etc.).
+        ``row``: the written rows applied as rows, which gives the physical
+        constants (Kn = r*C44, Tv = r*(C12-C44)/18 for the simple cubic cell).
+        """
+        m = self._data.reshape(3, 3)
+        return m.T.copy() if layout == "reference" else m.copy()
+
+    def elastic_constants(self, E=None, nu=None, plane_stress=False, C=None, layout="reference"):
+        """(Kn, Tv) per layer as ParticleElastic::setParticleProperty computes
+        them (particle_elastic.h:70-143): returns (Kn_layer0, Kn_layer1, Tv)."""
+        if C is None:
+            if not plane_stress:
+                C11 = E * (1.0 - nu) / (1.0 + nu) / (1.0 - 2.0 * nu)
+                C12 = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu)
+                C44 = E / 2.0 / (1.0 + nu)
+            else:
+                C11 = E / (1.0 - nu) / (1.0 + nu)
+                C12 = E * nu / (1.0 + nu) / (1.0 - nu)
+                C44 = E / 2.0 / (1.0 + nu)
+            C = (C11, C12, C44)
+        M = self.el_mapping(layout)
+        Ce = np.asarray(C, dtype=np.float64)
+        k = np.array([M[i, 0] * Ce[0] + M[i, 1] * Ce[1] + M[i, 2] * Ce[2] for i in range(3)])
+        if self.dim == 3:
+            k = self.radius * k
+        if self.lattice == HEXAGON2D:
+            return float(k[0]), float(k[0]), float(k[1])
+        return float(k[0]), float(k[1]), float(k[2])
+
+
+def hex_plate(ncol, nrow, a):
+    """Hexagonal plate: even rows hold ncol points, odd rows ncol-1 points
+    shifted by a/2 (the createPlateHEX2D row rule); row pitch a*sqrt(3)/2."""
+    hy = a * math.sqrt(3.0) / 2.0
+    pts = []
+    for j in range(nrow):
+        if j % 2 == 0:
+            xs = a * np.arange(ncol, dtype=np.float64)
+        else:
+            xs = a * (2 * np.arange(ncol - 1, dtype=np.float64) + 1) / 2.0
+        pts.append(np.stack([xs, np.full_like(xs, hy * j), np.zeros_like(xs)], axis=1))
+    return np.concatenate(pts, axis=0)
+
+
+def sc_cuboid(nx, ny, nz, a):
+    """Simple cubic grid of nx*ny*nz points, x fastest (createCuboidSC3D order)."""
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    return np.stack([a * i.ravel(), a * j.ravel(), a * k.ravel()], axis=1).astype(np.float64)
+
+
+def bcc_cuboid(nx, ny, nz, a):
+    """BCC grid: corner points of an nx*ny*nz cell block plus body centres,
+    ordered by z, then y, then x (corners and centres interleaved by layer)."""
+    pts = []
+    for kz in range(nz + 1):
+        k, j, i = np.meshgrid([kz], np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+        pts.append(np.stack([a * i.ravel(), a * j.ravel(), a * k.ravel()], axis=1))
+        if kz < nz:
+            k, j, i = np.meshgrid([kz], np.arange(ny), np.arange(nx), indexing="ij")
+            pts.append(np.stack([a * (i.ravel() + 0.5), a * (j.ravel() + 0.5), a * (k.ravel() + 0.5)], axis=1))
+    return np.concatenate(pts, axis=0).astype(np.float64)
+
+
+def find_bonds(xyz, cell):
+    """Directed bonds (p1, p2, layer) with the createBonds rule and order.
+
+    Candidate pairs come from a k-d tree; each is then accepted with the
+    reference's own arithmetic (sqrt of the summed squared differences,
+    compared with 1.01 * cutoff), so the result matches the O(N^2) search.
+    """
+    from scipy.spatial import cKDTree
+
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    c0 = 1.01 * cell.neighbor_cutoff[0]
+    c1 = 1.01 * cell.neighbor_cutoff[1]
+    tree = cKDTree(xyz)
+    pairs = tree.query_pairs(c1 * (1 + 1e-9) + 1e-12, output_type="ndarray")
+    i = np.concatenate([pairs[:, 0], pairs[:, 1]])
+    j = np.concatenate([pairs[:, 1], pairs[:, 0]])
+    d = xyz[i] - xyz[j]
+    dist = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+    keep = (dist < c1) & (i != j)
+    i, j, dist = i[keep], j[keep], dist[keep]
+    order = np.lexsort((j, i))
+    i, j, dist = i[order], j[order], dist[order]
+    layer = np.where(dist < c0, 0, 1).astype(np.int32)
+    return i.astype(np.int32), j.astype(np.int32), layer
+
+
+def bond_constants(cell, layer, KnTv):
+    """Per-bond Kn, Tv from (Kn0, Kn1, Tv) (particle_elastic.h:112-124)."""
+    kn0, kn1, tv = KnTv
+    Kn = np.where(layer == 0, kn0, kn1).astype(np.float64)
+    Tv = np.full(layer.shape, tv, dtype=np.float64)
+    return Kn, Tv
