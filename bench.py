@@ -1,0 +1,447 @@
+#!/usr/bin/env python
+"""Load steps/s of the LPM quasi-static Newton load step on one GB300.
+
+Workload: the 3-D simple-cubic lattice of 101^3 = 1,030,301 particles
+(18,240,600 directed bonds, 60,969,107 3x3 tangent blocks), lattice
+constant 0.2 mm, E = 200 GPa, nu = 0.3, bottom face clamped, top face pulled
+in z by 0.002 mm per load step.  A load step = apply the step's boundary
+conditions, assemble the tangent (symmetric variant, BC elimination), and
+Newton iterations (tol 1e-5) each with a Jacobi-CG solve to 1e-10.
+
+Reported (one JSON line on rank 0):
+  value        load steps/s of the mixed form (FP32 CG in FP64 refinement),
+               device-timed with CUDA events on the library's stream
+  fp64         the same with the plain FP64 CG
+  e2e          steps driven through the C ABI with host buffers: each step
+               passes its BC descriptors from pinned host memory and reads
+               positions and internal forces back into pinned host memory
+  roofline     the CG sparse product (dominant kernel): algorithmic bytes
+               per launch / average launch time, against the measured HBM
+               copy bandwidth
+  cpu_baseline the CPU oracle (a restatement of the reference algorithm) on
+               the host cores, bounded sample extrapolated to a full step
+
+--impl reference times the CPU oracle alone on the same workload.
+Multi-GPU runs are independent replicas (the path has no exchange step).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "load steps/s, 1M-particle SC lattice (quasi-static Newton load step)"
+UNIT = "load steps/s"
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=101, help="particles per cube edge")
+    p.add_argument("--du", type=float, default=0.002, help="top-face displacement per step (mm)")
+    p.add_argument("--cg-tol", type=float, default=1e-10)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--cpu-sample-iters", type=int, default=20)
+    return p.parse_args(argv)
+
+
+# ------------------------------------------------------------------ set-up
+def workload(n, a=0.2, E=200e3, nu=0.3):
+    import __graft_entry__ as ge
+    lat = ge.load_package().lattice
+    cell = lat.UnitCell(lat.SIMPLECUBIC3D, a / 2)
+    xyz = lat.sc_cuboid(n, n, n, a)
+    p1, p2, layer = lat.find_bonds(xyz, cell)
+    Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(E, nu, layout="row"))
+    z = xyz[:, 2]
+    bottom = np.where(z < z.min() + 1e-9)[0]
+    top = np.where(z > z.max() - 1e-9)[0]
+    return dict(cell=cell, xyz=xyz, p1=p1, p2=p2, layer=layer, Kn=Kn, Tv=Tv, bottom=bottom, top=top)
+
+
+def describe(w):
+    return "SC %d^3 lattice (%d particles, %d bonds), a=0.2 mm, E=200 GPa, nu=0.3, clamped base, top +%g mm/step" % (
+        round(len(w["xyz"]) ** (1 / 3)), len(w["xyz"]), len(w["p1"]), ARGS.du)
+
+
+# ------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for k, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(k)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ distributed
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(x, world):
+    """Max of a float over ranks (identity on one process)."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def aggregate(elapsed_s, steps, world):
+    """Whole-job throughput: every rank ran `steps`; the job took the slowest rank's time."""
+    t = max_over_ranks(elapsed_s, world)
+    return world * steps / t, t
+
+
+# --------------------------------------------------------------- GPU arm
+def gpu_run(w, args, precision, world, local):
+    import torch
+    import __graft_entry__ as ge
+    capi = ge.load_package().capi
+    g = capi.Lattice(3, w["xyz"], w["p1"], w["p2"], w["layer"], w["Kn"], w["Tv"], w["cell"].particle_volume,
+                     w["cell"].nneighbors)
+    gb, gt = g.add_group(w["bottom"]), g.add_group(w["top"])
+    bcs = [("disp", gb, 0, 0.0), ("disp", gb, 1, 0.0), ("disp", gb, 2, 0.0), ("disp", gt, 2, args.du)]
+    opts = dict(tangent=capi.TANGENT_SYMMETRIC, precision=precision, max_iter=30, tol=1e-5, cg_tol=args.cg_tol)
+    g.update()
+    for _ in range(args.warmup):
+        r = g.load_step(bcs, **opts)
+        if r["status"] != 0:
+            raise RuntimeError("warm-up step did not converge: %s" % r)
+    stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    g.set_kernel_timing(True)
+    g.reset_stats()
+    newton, cg = [], []
+    barrier(world)
+    torch.cuda.synchronize()
+    g.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        r = g.load_step(bcs, **opts)
+        if r["status"] != 0:
+            raise RuntimeError("timed step did not converge: %s" % r)
+        newton.append(r["newton_iters"])
+        cg.append(r["cg_iters"])
+    e1.record(stream)
+    e1.synchronize()
+    g.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    st = g.stats()
+    g.set_kernel_timing(False)
+    out = dict(ms=ms, stats=st, newton=newton, cg=cg, handle=g, bcs=bcs, opts=opts)
+    return out
+
+
+def e2e_run(g, bcs, opts, steps, world):
+    """Steps through the C ABI with host buffers: BC descriptors from pinned
+    host memory, positions and internal forces read back into pinned memory."""
+    import torch
+    capi = sys.modules["lpm_mac_gb300"].capi
+    n = g.n
+    xyz_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    pin_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    import ctypes
+    dp = ctypes.POINTER(ctypes.c_double)
+    L = g._L
+    barrier(world)
+    g.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r = g.load_step(bcs, **opts)
+        if r["status"] != 0:
+            raise RuntimeError("e2e step did not converge: %s" % r)
+        g._check(L.lpm_download(g.h, capi.F_XYZ, xyz_h.ctypes.data_as(dp)))
+        g._check(L.lpm_download(g.h, capi.F_PIN, pin_h.ctypes.data_as(dp)))
+    t1 = time.perf_counter()
+    barrier(world)
+    h2d = len(bcs) * ctypes.sizeof(capi.BC)
+    d2h = 2 * n * 3 * 8
+    return t1 - t0, h2d, d2h
+
+
+def spmv_bytes(nblk, n, dim, value_bytes):
+    """Algorithmic bytes of one CG sparse-product launch: every block's
+    dim*dim values and column index, the row pointers, the search direction
+    read once and the product written once."""
+    return nblk * (dim * dim * value_bytes + 4) + (n + 1) * 8 + 2 * n * dim * value_bytes
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel_key):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "cg_spmv_sc101.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch") and kernel_key in line:
+                return float(line.split("=")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+# --------------------------------------------------------------- CPU arm
+def cpu_oracle_system(w, threads):
+    import __graft_entry__ as ge
+    oracle = ge.load_oracle()
+    oracle.lib().lo_set_threads(threads)
+    o = oracle.OracleSystem(3, w["xyz"], w["p1"], w["p2"], w["layer"], w["Kn"], w["Tv"], w["cell"].particle_volume,
+                            w["cell"].nneighbors)
+    return oracle, o
+
+
+def cpu_sample(oracle, o, w, du, cg_iters):
+    """One bounded sample of a load step on the CPU oracle: BC move, force
+    pass, tangent assembly and `cg_iters` FP64 CG iterations."""
+    n = len(w["xyz"])
+    apply = np.zeros((n, 3), np.int32)
+    d = np.zeros((n, 3))
+    apply[w["bottom"], :] = 1
+    apply[w["top"], 2] = 1
+    d[w["top"], 2] = du
+    x = o.get(oracle.XYZ)
+    x[w["top"], 2] += du
+    o.set(oracle.XYZ, x)
+    m = np.zeros((n, 3), np.int32)
+    m[apply == 1] = 1
+    o.set_mask(m)
+    t0 = time.perf_counter()
+    o.update()
+    t1 = time.perf_counter()
+    o.assemble(sym=1, bc=1)
+    t2 = time.perf_counter()
+    r, _, _ = o.residual()
+    t3 = time.perf_counter()
+    o.cg(r, 1e-30, maxit=cg_iters)
+    t4 = time.perf_counter()
+    return dict(force=t1 - t0, assemble=t2 - t1, cg_iter=(t4 - t3) / cg_iters)
+
+
+def cpu_step_time(s, newton, cg_iters):
+    return s["assemble"] + (newton + 1) * s["force"] + cg_iters * s["cg_iter"]
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    w = workload(args.n)
+    oracle, o = cpu_oracle_system(w, threads)
+    o.update()
+    # iteration counts of a full step: one complete FP64 load step on the CPU
+    n = len(w["xyz"])
+    apply = np.zeros((n, 3), np.int32)
+    apply[w["bottom"], :] = 1
+    apply[w["top"], 2] = 1
+    dd = np.zeros((n, 3))
+    dd[w["top"], 2] = args.du
+    o.clear_log()
+    t0 = time.perf_counter()
+    o.load_step(apply, dd, sym=1, bc_elim=1, cg_tol=args.cg_tol)
+    full = time.perf_counter() - t0
+    log = o.log()
+    newton, cg_iters = len(log), int(log[:, 0].sum())
+    times = []
+    for k in range(args.warmup + args.steps):
+        s = cpu_sample(oracle, o, w, args.du, args.cpu_sample_iters)
+        if k >= args.warmup:
+            times.append(cpu_step_time(s, newton, cg_iters))
+    value = 1.0 / statistics.mean(times)
+    sample = ("each step: 1 force pass + 1 tangent assembly + %d FP64 CG iterations on the full lattice, "
+              "extrapolated with the %d Newton / %d CG iterations of one complete CPU load step (%.1f s)" %
+              (args.cpu_sample_iters, newton, cg_iters, full))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": describe(w), "solver": "CPU oracle (reference algorithm restated), FP64 Jacobi CG",
+                       "cg_tol": args.cg_tol, "newton_tol": 1e-5, "threads": threads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    capi = pkg.capi
+    capi.set_device(local)
+    w = workload(args.n)
+    clocks = ClockSampler(local)
+    results = {}
+    order = ([] if args.no_fp64 else [capi.PREC_FP64]) + [capi.PREC_MIXED]
+    for prec in order:
+        if prec == capi.PREC_MIXED:
+            clocks.start()
+        results[prec] = gpu_run(w, args, prec, world, local)
+        if prec == capi.PREC_MIXED:
+            clk = clocks.stop()
+    mixed = results[capi.PREC_MIXED]
+    value, t_mixed = aggregate(mixed["ms"] / 1e3, args.steps, world)
+    g = mixed["handle"]
+    # e2e through the C ABI with host buffers
+    e2e_s, h2d, d2h = e2e_run(g, mixed["bcs"], mixed["opts"], args.steps, world)
+    e2e_value, _ = aggregate(e2e_s, args.steps, world)
+    st = mixed["stats"]
+    n, nb, nblk = g.n, g.nb, g.nblk
+    launches = st["spmv32_launches"]
+    avg_ms = st["spmv32_ms"] / max(launches, 1)
+    byts = spmv_bytes(nblk, n, 3, 4)
+    peak, peak_kind = measured_peaks()
+    achieved = byts / (avg_ms * 1e-3) / 1e9
+    traffic = profiled_traffic("float")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_mixed * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 CG + f64 refinement/forces", "data": "synthetic",
+            "config": {"workload": describe(w), "precision": "FP32 CG inside FP64 iterative refinement",
+                       "tangent": "symmetric K_ii[1][0]", "bc": "eliminated (updateStiffnessDispBC)",
+                       "cg_tol": args.cg_tol, "newton_tol": 1e-5, "l2": "inputs larger than L2 (FP32 operator %.2f GB)"
+                       % (nblk * 40 / 1e9), "parallelism": "replicas x%d" % world},
+            "newton_iters_per_step": statistics.mean(mixed["newton"]),
+            "cg_iters_per_step": statistics.mean(mixed["cg"]),
+            "cg_iters_per_s": sum(mixed["cg"]) / (mixed["ms"] / 1e3),
+            "gpu_launches": int(st["kernel_launches"]),
+            "roofline": {"kernel": "k_cg_spmv<float,3>", "bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": byts, "avg_launch_ms": avg_ms, "launches": launches,
+                         "peak_kind": peak_kind + " (hbm_gbs copy bandwidth)"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
+    if clk:
+        line["clocks"] = clk
+    if capi.PREC_FP64 in results:
+        f = results[capi.PREC_FP64]
+        fv, tf = aggregate(f["ms"] / 1e3, args.steps, world)
+        sf = f["stats"]
+        avg64 = sf["spmv_ms"] / max(sf["spmv_launches"], 1)
+        b64 = spmv_bytes(nblk, n, 3, 8)
+        line["fp64"] = {"value": fv, "ms_per_step": tf * 1e3 / args.steps,
+                        "newton_iters_per_step": statistics.mean(f["newton"]),
+                        "cg_iters_per_step": statistics.mean(f["cg"]),
+                        "spmv_avg_launch_ms": avg64, "spmv_achieved_gbs": b64 / (avg64 * 1e-3) / 1e9,
+                        "spmv_fp64_gflops": 2 * nblk * 9 / (avg64 * 1e-3) / 1e9,
+                        "mixed_speedup": value / fv}
+        f["handle"].close()
+    line["bonds_per_s_force"] = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        oracle, o = cpu_oracle_system(w, threads)
+        o.update()
+        newton = line["newton_iters_per_step"]
+        cgi = line.get("fp64", line)["cg_iters_per_step"]
+        s = cpu_sample(oracle, o, w, args.du, args.cpu_sample_iters)
+        t = cpu_step_time(s, newton, cgi)
+        line["cpu_baseline"] = {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "1 force pass + 1 tangent assembly + %d FP64 CG iterations on the full "
+                                          "lattice (%.2f s force, %.2f s assembly, %.3f s/CG iteration), "
+                                          "extrapolated with %.1f Newton / %.0f CG iterations per step" %
+                                          (args.cpu_sample_iters, s["force"], s["assemble"], s["cg_iter"], newton,
+                                           cgi)}
+        del o
+    g.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+ARGS = None
+
+
+def main(argv=None):
+    global ARGS
+    ARGS = parse_args(argv)
+    if ARGS.impl == "reference":
+        return run_reference(ARGS)
+    return run_gb300(ARGS)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,234 @@
+/* liblpmgpu: C ABI of the GB300 (sm_103a) LPM quasi-static Newton load step.
+ *
+ * The LPM-MAC reference has no FFI: its interface is the header-only class
+ * set (Assembly, Particle*, Stiffness, Solver, SolverStatic, SolverFatigue,
+ * LoadStep/DispBC/ForceBC).  Each entry point below replaces the body of one
+ * of those methods; the class it stands in for is cited next to it
+ * (paths relative to the LPM-MAC project root).  The C++ mirror of the class
+ * API (lpm-mac_gb300/cpp/) and the Python mirror call these functions.
+ *
+ * Conventions: plain pointers and sizes; host buffers unless stated; an
+ * opaque handle per lattice; every call returns an int status
+ * (0 ok, >0 not converged, <0 error, see LPM_* below) and never throws or
+ * exits.  All device work runs on the handle's own CUDA stream on the
+ * current device; calls are synchronous with respect to the host unless
+ * stated.  Indices are 0-based particle ids; a particle's DOF k lives at
+ * dim*id + k (solver.h:102,117).
+ */
+#ifndef LPM_GPU_H
+#define LPM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lpm_handle lpm_handle;
+
+/* status codes */
+#define LPM_OK 0
+#define LPM_NOT_CONVERGED 1    /* Newton or CG hit its iteration cap       */
+#define LPM_ERR_ARG (-1)       /* bad argument, size or id                  */
+#define LPM_ERR_TOPOLOGY (-2)  /* a bond has no opposite bond               */
+#define LPM_ERR_CUDA (-3)      /* CUDA runtime error (see lpm_last_error)   */
+#define LPM_ERR_NOMEM (-4)     /* device allocation failed                  */
+#define LPM_ERR_STATE (-5)     /* call out of order (e.g. solve before K)   */
+#define LPM_ERR_NONFINITE (-6) /* NaN/Inf met in a solve                    */
+
+/* particle fields for lpm_upload / lpm_download (double unless noted) */
+#define LPM_F_XYZ 0        /* N*3 current positions (Particle::xyz)          */
+#define LPM_F_XYZ0 1       /* N*3 initial positions (xyz_initial)            */
+#define LPM_F_PIN 2        /* N*3 internal force (Pin)                        */
+#define LPM_F_PEX 3        /* N*3 external force (Pex)                        */
+#define LPM_F_STRESS 4     /* N*6 xx yy zz yz xz xy (stress)                  */
+#define LPM_F_DVIS 5       /* N   damage_visual                               */
+#define LPM_F_DLE_TOT 6    /* N*2 per-layer sum of dLe (dLe_total)            */
+#define LPM_F_TDLE_TOT 7   /* N*2 per-layer sum of Tv*dLe (TdLe_total)        */
+#define LPM_F_CS_SUM 8     /* N*2*3 per-layer direction-cosine sums           */
+#define LPM_F_DAMAGE 9     /* N   particle damage                             */
+#define LPM_F_XYZ_LAST 10  /* N*3 last converged positions (xyz_last)         */
+#define LPM_F_DISP 11      /* N*dim last Newton increment (Solver::disp)     */
+#define LPM_F_RESIDUAL 12  /* N*dim residual (Stiffness::residual)           */
+/* bond fields, stored order (by p1, layer, input order) */
+#define LPM_B_BFORCE 100
+#define LPM_B_BDAMAGE 101
+#define LPM_B_DLE 102
+#define LPM_B_DIS 103
+#define LPM_B_BSTRAIN 104
+#define LPM_B_CS 105 /* Nb*3 */
+#define LPM_B_KN 106
+#define LPM_B_TV 107
+#define LPM_B_DIS0 108
+#define LPM_B_DLP 109
+
+/* tangent variants for lpm_assemble */
+#define LPM_TANGENT_AS_WRITTEN 0 /* derivative.h as written: K_ii[1][0] stays 0 (derivative.h:38) */
+#define LPM_TANGENT_SYMMETRIC 1  /* K_ii[1][0] = K_ii[0][1]                                    */
+/* boundary treatment of the tangent */
+#define LPM_BC_NONE 0      /* SolverStatic: K unchanged (solver_static.h:113 leaves it out)  */
+#define LPM_BC_ELIMINATE 1 /* Stiffness::updateStiffnessDispBC (stiffness.h:265-294)          */
+/* linear-solver precision */
+#define LPM_PREC_FP64 0  /* Jacobi CG in FP64, the Eigen algorithm (solver.h:192-217)       */
+#define LPM_PREC_MIXED 1 /* FP32 Jacobi CG inside FP64 iterative refinement                 */
+
+/* Creates the device lattice.  Replaces Assembly's constructors
+ * (assembly.h:83-106), Assembly::createBonds / readBond (bond lists are given
+ * here, assembly.h:212-234, 390-424), Assembly::updateConnections
+ * (assembly.h:236-266, computed on the device) and the Kn/Tv assignment of
+ * setParticleProperty (particle_elastic.h:70-143: per-bond constants given).
+ * xyz N*3; p1/p2/layer/Kn/Tv per directed bond; particle_volume and
+ * nneighbors from the UnitCell (unit_cell.h).  Every bond must have an
+ * opposite bond in the same layer (LPM_ERR_TOPOLOGY otherwise). */
+/* Selects the CUDA device for the calling host thread's later lpm_create
+ * calls (the library links its own CUDA runtime, so a device chosen through
+ * another runtime instance does not carry over).  Library-level addition:
+ * the reference runs on the host only. */
+int lpm_set_device(int device);
+
+int lpm_create(int dim, int n, int64_t nb, const double* xyz, const int* p1, const int* p2, const int* layer,
+               const double* Kn, const double* Tv, double particle_volume, int nneighbors, lpm_handle** out);
+int lpm_destroy(lpm_handle* h);
+/* Human-readable text of the last error on this handle (or global). */
+const char* lpm_last_error(const lpm_handle* h);
+
+int lpm_num_bonds(const lpm_handle* h, int64_t* nb);
+int lpm_num_blocks(const lpm_handle* h, int64_t* nblocks);
+/* The conns pattern (Particle::conns, assembly.h:236-266) as CSR:
+ * cptr[N+1], cidx[nblocks]; and the stored bond order: bptr[N+1], bp2[Nb],
+ * blayer[Nb], opp[Nb] (the opposite bond found by particle.h:207-209). */
+int lpm_get_pattern(const lpm_handle* h, int64_t* cptr, int* cidx);
+int lpm_get_bonds(const lpm_handle* h, int64_t* bptr, int* bp2, int* blayer, int64_t* opp);
+
+/* Field transfer (host <-> device), sizes as listed with the field ids. */
+int lpm_upload(lpm_handle* h, int field, const double* src);
+int lpm_download(lpm_handle* h, int field, double* dst);
+/* Particle::disp_constraint for all particles: N*3 ints (0/1). */
+int lpm_set_mask(lpm_handle* h, const int* mask);
+int lpm_get_mask(const lpm_handle* h, int* mask);
+
+/* Material law of all particles.  law 0 = ParticleElastic, params[0] =
+ * critical_bstrain (particle_elastic.h:14-68). */
+#define LPM_LAW_ELASTIC 0
+int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams);
+
+/* Static damage update of SolverStatic (solver_static.h:31-62) for the
+ * elastic law: breaks bonds whose strain reached the critical bond strain
+ * (particle_elastic.h:52-68); *any_new = 1 when a bond broke. */
+int lpm_update_damage(lpm_handle* h, int* any_new);
+
+/* Boundary groups: index lists registered once, used by the BC calls below
+ * (DispBC / ForceBC groups, boundary.h:10-44). */
+int lpm_add_group(lpm_handle* h, const int* ids, int count, int* group_id);
+/* DispBC applied by Solver::updateDisplacementBC (solver.h:130-166):
+ * axis 0/1/2 ('x','y','z'), mode 0 Relative (moveBy) / 1 Absolute (moveTo
+ * of that axis' value, other axes set to 0 as the reference's moveTo(dxyz)
+ * does), sets disp_constraint[axis] = 1. */
+int lpm_apply_disp_bc(lpm_handle* h, int group, int axis, int mode, double value);
+/* ForceBC applied by Solver::updateForceBC (solver.h:168-190): the total
+ * force is split evenly over the group; mode 0 Relative (+=) / 1 Absolute. */
+int lpm_apply_force_bc(lpm_handle* h, int group, int mode, double fx, double fy, double fz);
+
+/* Assembly::updateGeometry + Assembly::updateForceState
+ * (assembly.h:132-138, 178-191; bond.h:30-39; particle.h:151-240;
+ * particle_elastic.h:38-50). */
+int lpm_update_geometry_force(lpm_handle* h);
+/* Solver::updateRR + the norms of NewtonIteration (solver.h:108-128, 62-64). */
+int lpm_residual(lpm_handle* h, double* norm_residual, double* norm_reaction);
+
+/* Stiffness::reset + calcStiffness (stiffness.h:43-48, 228-263, derivative.h)
+ * and, with LPM_BC_ELIMINATE, updateStiffnessDispBC (stiffness.h:265-294).
+ * Builds the FP64 tangent and, when mixed precision is requested later, its
+ * FP32 copy. */
+int lpm_assemble(lpm_handle* h, int tangent, int bc);
+/* BSR values of K (not transposed) in pattern order, dim*dim row-major. */
+int lpm_get_K(const lpm_handle* h, double* vals);
+
+/* Solver::LPM_CG (solver.h:192-217): solves with the residual as right-hand
+ * side into Solver::disp.  FP64: Eigen's ConjugateGradient with its Jacobi
+ * preconditioner, applied through the transposed view of the column-major
+ * matrix as Eigen does for Lower|Upper; stops when |r|^2 < tol^2 |b|^2, at
+ * most maxit iterations (maxit < 0: 2*n_dof).  MIXED: FP32 CG steps on an
+ * FP32 copy of the same operator inside FP64 refinement, stopped on the FP64
+ * residual |b - A x| <= tol |b|.  iters/relres may be NULL. */
+int lpm_solve(lpm_handle* h, int precision, double tol, int64_t maxit, int64_t* iters, double* relres);
+/* Solver::solveLinearSystem's position update (solver.h:97-105). */
+int lpm_move_by_disp(lpm_handle* h);
+
+/* Solver::NewtonIteration (solver.h:53-89).  *n_iter gets the iteration
+ * count, max_iter on failure (status LPM_NOT_CONVERGED). */
+int lpm_newton(lpm_handle* h, int max_iter, double tol, int precision, double cg_tol, int64_t cg_maxit,
+               int* n_iter);
+
+/* One boundary condition of a LoadStep (load_step.h:12-29, boundary.h). */
+#define LPM_BC_DISP 0
+#define LPM_BC_FORCE 1
+typedef struct {
+  int kind;          /* LPM_BC_DISP or LPM_BC_FORCE                       */
+  int group;         /* id from lpm_add_group                             */
+  int mode;          /* 0 Relative, 1 Absolute (LoadMode, lpm.h:57-61)     */
+  int axis;          /* DispBC flag: 0 'x', 1 'y', 2 'z'                  */
+  double value;      /* DispBC step                                        */
+  double fx, fy, fz; /* ForceBC total force                                */
+} lpm_bc;
+
+/* Load-step driver. */
+#define LPM_SOLVER_STATIC 0 /* SolverStatic::solveProblemStep (solver_static.h:97-149) */
+#define LPM_SOLVER_FATIGUE_STATIC 1 /* SolverFatigue::solveProblemStep + the storing of
+                                       solveProblemStatic (solver_fatigue.h:243-298) */
+typedef struct {
+  int solver;        /* LPM_SOLVER_*                                       */
+  int tangent;       /* LPM_TANGENT_*                                      */
+  int precision;     /* LPM_PREC_*                                         */
+  int max_iter;      /* Solver::max_NR_iter                                */
+  double tol;        /* Solver::tol_NR_iter                                */
+  double cg_tol;     /* CG tolerance (the reference uses machine epsilon)  */
+  int64_t cg_maxit;  /* < 0: 2 * n_dof                                     */
+  int max_cuts;      /* cut-backs allowed before giving up                 */
+} lpm_step_opts;
+typedef struct {
+  int newton_iters;  /* Newton iterations of the last accepted sub-step    */
+  int cuts;          /* load cut-backs taken                               */
+  int damage_rounds; /* damage sub-iterations (SolverStatic)               */
+  int pad;
+  int64_t cg_iters;  /* CG iterations of the whole step                    */
+} lpm_step_result;
+/* Applies one LoadStep (force BCs, then displacement BCs, in the order
+ * given, as updateForceBC / updateDisplacementBC do) and solves it, halving
+ * the step and retrying on Newton failure as SolverStatic::solveProblem and
+ * SolverFatigue::solveProblemStatic do (solver_static.h:79-87).  Returns
+ * LPM_NOT_CONVERGED after max_cuts cut-backs. */
+int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts* opts, lpm_step_result* res);
+
+/* Assembly::storeStateVar / resetStateVar (assembly.h:140-159). */
+int lpm_store_state(lpm_handle* h);
+int lpm_reset_state(lpm_handle* h, int reset_xyz);
+
+/* Counters since the last lpm_reset_stats: total CG iterations, refinement
+ * sweeps, kernel launches, and, when kernel timing is on, the summed device
+ * time and launch count of the CG sparse product (the dominant kernel) in
+ * FP64 and in FP32. */
+typedef struct {
+  int64_t cg_iters_total;
+  int64_t refine_sweeps;
+  int64_t spmv_launches;
+  double spmv_ms;
+  int64_t spmv32_launches;
+  double spmv32_ms;
+  int64_t kernel_launches;
+} lpm_stats;
+int lpm_get_stats(const lpm_handle* h, lpm_stats* st);
+int lpm_reset_stats(lpm_handle* h);
+/* Records CUDA events around every CG sparse-product launch (on the
+ * handle's stream) so that lpm_get_stats reports its device time. */
+int lpm_set_kernel_timing(lpm_handle* h, int on);
+/* The handle's CUDA stream (cudaStream_t), for callers that time or order
+ * work around the library. */
+int lpm_get_stream(const lpm_handle* h, void** stream);
+/* Blocks until the handle's stream is idle. */
+int lpm_synchronize(lpm_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,13 @@
+"""GB300-native LPM quasi-static Newton load step.
+
+Host-side Python mirror over liblpmgpu (hand-written CUDA for sm_103a behind
+the C ABI in include/lpm_gpu.h):
+
+  lattice   unit cells, lattice generators and the createBonds bond rule
+  capi      ctypes binding of the C ABI (Lattice = one device lattice)
+  build     nvcc build of liblpmgpu.so
+
+The directory name is not a Python identifier; load it with
+``__graft_entry__.load_package()``, which registers it as ``lpm_mac_gb300``.
+"""
+from . import build, capi, lattice  # noqa: F401

@@ -1,0 +1,603 @@
+// C ABI of liblpmgpu (declared in include/lpm_gpu.h): handle life cycle,
+// host <-> device transfers and the Newton driver.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "lpm_internal.cuh"
+
+namespace lpm {
+
+static thread_local std::string g_err;
+
+int cuda_fail(lpm_handle* h, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (h) h->err = m;
+  g_err = m;
+  return e == cudaErrorMemoryAllocation ? LPM_ERR_NOMEM : LPM_ERR_CUDA;
+}
+
+void* dev_alloc(lpm_handle* h, size_t bytes) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 16));
+  if (e != cudaSuccess) {
+    cuda_fail(h, e, "cudaMalloc");
+    return nullptr;
+  }
+  h->allocations.push_back(p);
+  return p;
+}
+
+}  // namespace lpm
+
+using namespace lpm;
+
+namespace {
+
+int arg_error(lpm_handle* h, const char* msg) {
+  if (h) h->err = msg;
+  g_err = msg;
+  return LPM_ERR_ARG;
+}
+
+template <typename T>
+T* upload_new(lpm_handle* h, const T* src, size_t count) {
+  T* p = (T*)dev_alloc(h, sizeof(T) * count);
+  if (!p) return nullptr;
+  if (count && cudaMemcpy(p, src, sizeof(T) * count, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+  return p;
+}
+
+template <typename T>
+T* zeros_new(lpm_handle* h, size_t count) {
+  T* p = (T*)dev_alloc(h, sizeof(T) * count);
+  if (!p) return nullptr;
+  if (cudaMemset(p, 0, sizeof(T) * std::max<size_t>(count, 1)) != cudaSuccess) return nullptr;
+  return p;
+}
+
+struct FieldRef {
+  double* ptr;
+  size_t count;
+};
+
+FieldRef field_ref(lpm_handle* h, int f) {
+  const size_t N = (size_t)h->n, B = (size_t)h->nb, D = (size_t)h->dim;
+  Dev& d = h->d;
+  switch (f) {
+    case LPM_F_XYZ: return {d.x, 3 * N};
+    case LPM_F_XYZ0: return {d.x0, 3 * N};
+    case LPM_F_PIN: return {d.pin, 3 * N};
+    case LPM_F_PEX: return {d.pex, 3 * N};
+    case LPM_F_STRESS: return {d.stress, 6 * N};
+    case LPM_F_DVIS: return {d.dvis, N};
+    case LPM_F_DLE_TOT: return {d.dle_tot, NL * N};
+    case LPM_F_TDLE_TOT: return {d.tdle_tot, NL * N};
+    case LPM_F_CS_SUM: return {d.cs_sum, NL * 3 * N};
+    case LPM_F_DAMAGE: return {d.damage, N};
+    case LPM_F_XYZ_LAST: return {d.xlast, 3 * N};
+    case LPM_F_DISP: return {d.disp, D * N};
+    case LPM_F_RESIDUAL: return {d.rhs, D * N};
+    case LPM_B_BFORCE: return {d.bforce, B};
+    case LPM_B_BDAMAGE: return {d.bdamage, B};
+    case LPM_B_DLE: return {d.dLe, B};
+    case LPM_B_DIS: return {d.dis, B};
+    case LPM_B_BSTRAIN: return {d.bstrain, B};
+    case LPM_B_CS: return {d.cs, 3 * B};
+    case LPM_B_KN: return {d.Kn, B};
+    case LPM_B_TV: return {d.Tv, B};
+    case LPM_B_DIS0: return {d.dis0, B};
+    case LPM_B_DLP: return {d.dLp, B};
+  }
+  return {nullptr, 0};
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lpm_last_error(const lpm_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int lpm_set_device(int device) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  return LPM_OK;
+}
+
+int lpm_create(int dim, int n, int64_t nb, const double* xyz, const int* p1, const int* p2, const int* layer,
+               const double* Kn, const double* Tv, double particle_volume, int nneighbors, lpm_handle** out) {
+  if (!out) return arg_error(nullptr, "out is NULL");
+  *out = nullptr;
+  if ((dim != 2 && dim != 3) || n <= 0 || nb < 0 || nneighbors <= 0 || !xyz || (nb > 0 && (!p1 || !p2 || !layer ||
+                                                                                            !Kn || !Tv)))
+    return arg_error(nullptr, "bad sizes or NULL arrays");
+  if (nb >= ((int64_t)1 << 31) || (int64_t)n * 3 >= ((int64_t)1 << 31))
+    return arg_error(nullptr, "lattice too large for 32-bit bond/particle indices");
+  for (int64_t b = 0; b < nb; ++b)
+    if (p1[b] < 0 || p1[b] >= n || p2[b] < 0 || p2[b] >= n || layer[b] < 0 || layer[b] >= NL)
+      return arg_error(nullptr, "bond with particle id or layer out of range");
+  const size_t N = (size_t)n, B = (size_t)nb;
+  // bond CSR by (p1, layer), stable (bond_layers order)
+  std::vector<int64_t> cnt(N * NL + 1, 0);
+  for (int64_t b = 0; b < nb; ++b) cnt[(size_t)p1[b] * NL + layer[b] + 1]++;
+  for (size_t k = 1; k < cnt.size(); ++k) cnt[k] += cnt[k - 1];
+  std::vector<int64_t> src(B);
+  {
+    std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+    for (int64_t b = 0; b < nb; ++b) src[(size_t)pos[(size_t)p1[b] * NL + layer[b]]++] = b;
+  }
+  std::vector<int64_t> bptr(N + 1), lptr(N);
+  for (size_t i = 0; i <= N; ++i) bptr[i] = cnt[i * NL];
+  for (size_t i = 0; i < N; ++i) lptr[i] = cnt[i * NL + 1];
+  std::vector<int> bp2(B), bl(B), nbonds(N), opp(B, -1);
+  std::vector<double> kn(B), tv(B), dis0(B);
+  for (size_t b = 0; b < B; ++b) {
+    bp2[b] = p2[src[b]];
+    bl[b] = layer[src[b]];
+    kn[b] = Kn[src[b]];
+    tv[b] = Tv[src[b]];
+  }
+  for (size_t i = 0; i < N; ++i) {
+    nbonds[i] = (int)(bptr[i + 1] - bptr[i]);
+    for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+      const double* xi = xyz + 3 * i;
+      const double* xj = xyz + 3 * (size_t)bp2[(size_t)b];
+      const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+      dis0[(size_t)b] = std::sqrt(dx * dx + dy * dy + dz * dz);
+      // opposite bond: the first bond of p2 in the same layer pointing back
+      // (particle.h:207-209)
+      const int j = bp2[(size_t)b], l = bl[(size_t)b];
+      const int64_t jb = l == 0 ? bptr[(size_t)j] : lptr[(size_t)j];
+      const int64_t je = l == 0 ? lptr[(size_t)j] : bptr[(size_t)j + 1];
+      for (int64_t c = jb; c < je; ++c)
+        if (bp2[(size_t)c] == (int)i) {
+          opp[(size_t)b] = (int)c;
+          break;
+        }
+      if (opp[(size_t)b] < 0) {
+        g_err = "bond without an opposite bond in the same layer";
+        return LPM_ERR_TOPOLOGY;
+      }
+    }
+  }
+  lpm_handle* h = new lpm_handle();
+  h->dim = dim;
+  h->n = n;
+  h->nb = nb;
+  h->particle_volume = particle_volume;
+  h->nneighbors = nneighbors;
+  cudaGetDevice(&h->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    int st = cuda_fail(h, e, "cudaStreamCreate");
+    delete h;
+    return st;
+  }
+  auto fail = [&](int st) {
+    g_err = h->err;
+    lpm_destroy(h);
+    return st;
+  };
+  Dev& d = h->d;
+  bool ok = true;
+  ok = ok && (d.x = upload_new(h, xyz, 3 * N)) && (d.x0 = upload_new(h, xyz, 3 * N)) &&
+       (d.xlast = upload_new(h, xyz, 3 * N));
+  ok = ok && (d.pin = zeros_new<double>(h, 3 * N)) && (d.pex = zeros_new<double>(h, 3 * N)) &&
+       (d.stress = zeros_new<double>(h, 6 * N)) && (d.dvis = zeros_new<double>(h, N)) &&
+       (d.dle_tot = zeros_new<double>(h, NL * N)) && (d.tdle_tot = zeros_new<double>(h, NL * N)) &&
+       (d.cs_sum = zeros_new<double>(h, NL * 3 * N)) && (d.damage = zeros_new<double>(h, N)) &&
+       (d.damage_last = zeros_new<double>(h, N)) && (d.mask = zeros_new<int>(h, 3 * N)) &&
+       (d.nbonds = upload_new(h, nbonds.data(), N)) && (d.fixed = zeros_new<unsigned char>(h, 3 * N));
+  ok = ok && (d.bptr = upload_new(h, bptr.data(), N + 1)) && (d.lptr = upload_new(h, lptr.data(), N)) &&
+       (d.bp2 = upload_new(h, bp2.data(), B)) && (d.blayer = upload_new(h, bl.data(), B)) &&
+       (d.opp = upload_new(h, opp.data(), B)) && (d.Kn = upload_new(h, kn.data(), B)) &&
+       (d.Tv = upload_new(h, tv.data(), B)) && (d.dis0 = upload_new(h, dis0.data(), B)) &&
+       (d.dis = upload_new(h, dis0.data(), B)) && (d.dis_last = upload_new(h, dis0.data(), B));
+  ok = ok && (d.dLe = zeros_new<double>(h, B)) && (d.dLp = zeros_new<double>(h, B)) &&
+       (d.dLp_last = zeros_new<double>(h, B)) && (d.bstrain = zeros_new<double>(h, B)) &&
+       (d.cs = zeros_new<double>(h, 3 * B)) && (d.bforce = zeros_new<double>(h, B)) &&
+       (d.bforce_last = zeros_new<double>(h, B)) && (d.bdamage = zeros_new<double>(h, B)) &&
+       (d.bdamage_last = zeros_new<double>(h, B));
+  const size_t ndof = (size_t)dim * N;
+  ok = ok && (d.rhs = zeros_new<double>(h, ndof)) && (d.disp = zeros_new<double>(h, ndof)) &&
+       (d.x64 = zeros_new<double>(h, ndof)) && (d.r64 = zeros_new<double>(h, ndof)) &&
+       (d.p64 = zeros_new<double>(h, ndof)) && (d.q64 = zeros_new<double>(h, ndof)) &&
+       (d.invd64 = zeros_new<double>(h, ndof));
+  ok = ok && (d.red.partials = zeros_new<double>(h, (size_t)kMaxRedBlocks * 4)) &&
+       (d.red.ticket = zeros_new<unsigned int>(h, 16)) && (d.cg = zeros_new<CgScalars>(h, 1)) &&
+       (d.norms = zeros_new<double>(h, 8));
+  std::vector<double> crit(N, 1.0);
+  ok = ok && (d.crit = upload_new(h, crit.data(), N));
+  if (!ok) return fail(h->err.empty() ? LPM_ERR_CUDA : LPM_ERR_NOMEM);
+  if (cudaMallocHost((void**)&h->h_cg, sizeof(CgScalars)) != cudaSuccess ||
+      cudaMallocHost((void**)&h->h_norms, 8 * sizeof(double)) != cudaSuccess) {
+    h->err = "cudaMallocHost failed";
+    return fail(LPM_ERR_NOMEM);
+  }
+  int st = build_pattern(h);
+  if (st) return fail(st);
+  *out = h;
+  return LPM_OK;
+}
+
+int lpm_destroy(lpm_handle* h) {
+  if (!h) return LPM_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (void* p : h->allocations) cudaFree(p);
+  for (auto& g : h->groups) cudaFree(g.ids);
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  if (h->h_cg) cudaFreeHost(h->h_cg);
+  if (h->h_norms) cudaFreeHost(h->h_norms);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return LPM_OK;
+}
+
+int lpm_num_bonds(const lpm_handle* h, int64_t* nb) {
+  if (!h || !nb) return LPM_ERR_ARG;
+  *nb = h->nb;
+  return LPM_OK;
+}
+
+int lpm_num_blocks(const lpm_handle* h, int64_t* nblocks) {
+  if (!h || !nblocks) return LPM_ERR_ARG;
+  *nblocks = h->nblk;
+  return LPM_OK;
+}
+
+int lpm_get_pattern(const lpm_handle* h, int64_t* cptr, int* cidx) {
+  if (!h) return LPM_ERR_ARG;
+  lpm_handle* hh = const_cast<lpm_handle*>(h);
+  if (cptr) LPM_CUDA(hh, cudaMemcpy(cptr, h->d.cptr, sizeof(int64_t) * (h->n + 1), cudaMemcpyDeviceToHost));
+  if (cidx) LPM_CUDA(hh, cudaMemcpy(cidx, h->d.cidx, sizeof(int) * h->nblk, cudaMemcpyDeviceToHost));
+  return LPM_OK;
+}
+
+int lpm_get_bonds(const lpm_handle* h, int64_t* bptr, int* bp2, int* blayer, int64_t* opp) {
+  if (!h) return LPM_ERR_ARG;
+  lpm_handle* hh = const_cast<lpm_handle*>(h);
+  if (bptr) LPM_CUDA(hh, cudaMemcpy(bptr, h->d.bptr, sizeof(int64_t) * (h->n + 1), cudaMemcpyDeviceToHost));
+  if (bp2) LPM_CUDA(hh, cudaMemcpy(bp2, h->d.bp2, sizeof(int) * h->nb, cudaMemcpyDeviceToHost));
+  if (blayer) LPM_CUDA(hh, cudaMemcpy(blayer, h->d.blayer, sizeof(int) * h->nb, cudaMemcpyDeviceToHost));
+  if (opp) {
+    std::vector<int> o((size_t)h->nb);
+    LPM_CUDA(hh, cudaMemcpy(o.data(), h->d.opp, sizeof(int) * h->nb, cudaMemcpyDeviceToHost));
+    for (int64_t b = 0; b < h->nb; ++b) opp[b] = o[(size_t)b];
+  }
+  return LPM_OK;
+}
+
+int lpm_upload(lpm_handle* h, int field, const double* src) {
+  if (!h || !src) return arg_error(h, "NULL handle or buffer");
+  FieldRef f = field_ref(h, field);
+  if (!f.ptr) return arg_error(h, "unknown field");
+  LPM_CUDA(h, cudaMemcpyAsync(f.ptr, src, sizeof(double) * f.count, cudaMemcpyHostToDevice, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_download(lpm_handle* h, int field, double* dst) {
+  if (!h || !dst) return arg_error(h, "NULL handle or buffer");
+  FieldRef f = field_ref(h, field);
+  if (!f.ptr) return arg_error(h, "unknown field");
+  LPM_CUDA(h, cudaMemcpyAsync(dst, f.ptr, sizeof(double) * f.count, cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_set_mask(lpm_handle* h, const int* mask) {
+  if (!h || !mask) return arg_error(h, "NULL handle or buffer");
+  LPM_CUDA(h, cudaMemcpyAsync(h->d.mask, mask, sizeof(int) * 3 * h->n, cudaMemcpyHostToDevice, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_get_mask(const lpm_handle* h, int* mask) {
+  if (!h || !mask) return LPM_ERR_ARG;
+  lpm_handle* hh = const_cast<lpm_handle*>(h);
+  LPM_CUDA(hh, cudaMemcpyAsync(mask, h->d.mask, sizeof(int) * 3 * h->n, cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(hh, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_update_damage(lpm_handle* h, int* any_new) {
+  if (!h) return LPM_ERR_ARG;
+  int flag = 0;
+  int st = launch_static_damage(h, &flag);
+  if (any_new) *any_new = flag;
+  return st;
+}
+
+int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams) {
+  if (!h) return LPM_ERR_ARG;
+  if (law != LPM_LAW_ELASTIC) return arg_error(h, "unknown material law");
+  h->law = law;
+  if (nparams >= 1 && params) {
+    std::vector<double> c((size_t)h->n, params[0]);
+    LPM_CUDA(h, cudaMemcpy(h->d.crit, c.data(), sizeof(double) * h->n, cudaMemcpyHostToDevice));
+  }
+  return LPM_OK;
+}
+
+int lpm_add_group(lpm_handle* h, const int* ids, int count, int* group_id) {
+  if (!h || !group_id || count < 0 || (count > 0 && !ids)) return arg_error(h, "bad group");
+  for (int t = 0; t < count; ++t)
+    if (ids[t] < 0 || ids[t] >= h->n) return arg_error(h, "group id out of range");
+  Group g{nullptr, count};
+  LPM_CUDA(h, cudaMalloc((void**)&g.ids, sizeof(int) * std::max(count, 1)));
+  if (count) LPM_CUDA(h, cudaMemcpy(g.ids, ids, sizeof(int) * count, cudaMemcpyHostToDevice));
+  h->groups.push_back(g);
+  *group_id = (int)h->groups.size() - 1;
+  return LPM_OK;
+}
+
+int lpm_apply_disp_bc(lpm_handle* h, int group, int axis, int mode, double value) {
+  if (!h || group < 0 || group >= (int)h->groups.size() || axis < 0 || axis > 2 || (mode != 0 && mode != 1))
+    return arg_error(h, "bad displacement BC");
+  return launch_disp_bc(h, h->groups[(size_t)group], axis, mode, value);
+}
+
+int lpm_apply_force_bc(lpm_handle* h, int group, int mode, double fx, double fy, double fz) {
+  if (!h || group < 0 || group >= (int)h->groups.size() || (mode != 0 && mode != 1))
+    return arg_error(h, "bad force BC");
+  return launch_force_bc(h, h->groups[(size_t)group], mode, fx, fy, fz);
+}
+
+int lpm_update_geometry_force(lpm_handle* h) {
+  if (!h) return LPM_ERR_ARG;
+  int st = launch_geometry_force(h);
+  if (st) return st;
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_residual(lpm_handle* h, double* norm_residual, double* norm_reaction) {
+  if (!h) return LPM_ERR_ARG;
+  return launch_residual(h, norm_residual, norm_reaction);
+}
+
+int lpm_assemble(lpm_handle* h, int tangent, int bc) {
+  if (!h || (tangent != LPM_TANGENT_AS_WRITTEN && tangent != LPM_TANGENT_SYMMETRIC) ||
+      (bc != LPM_BC_NONE && bc != LPM_BC_ELIMINATE))
+    return arg_error(h, "bad tangent or BC mode");
+  int st = launch_assemble(h, tangent, bc);
+  if (st) return st;
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_get_K(const lpm_handle* h, double* vals) {
+  if (!h || !vals) return LPM_ERR_ARG;
+  lpm_handle* hh = const_cast<lpm_handle*>(h);
+  if (!h->have_K) {
+    hh->err = "no tangent assembled";
+    return LPM_ERR_STATE;
+  }
+  const int dim = h->dim, e2 = dim * dim;
+  const size_t nb = (size_t)h->nblk;
+  std::vector<double> A(nb * e2);
+  std::vector<int64_t> cptr((size_t)h->n + 1);
+  std::vector<int> cidx(nb);
+  LPM_CUDA(hh, cudaMemcpy(A.data(), h->d.A64, sizeof(double) * A.size(), cudaMemcpyDeviceToHost));
+  LPM_CUDA(hh, cudaMemcpy(cptr.data(), h->d.cptr, sizeof(int64_t) * cptr.size(), cudaMemcpyDeviceToHost));
+  LPM_CUDA(hh, cudaMemcpy(cidx.data(), h->d.cidx, sizeof(int) * nb, cudaMemcpyDeviceToHost));
+  // block (i, j) of K is block (j, i) of A transposed
+  for (int i = 0; i < h->n; ++i)
+    for (int64_t q = cptr[(size_t)i]; q < cptr[(size_t)i + 1]; ++q) {
+      const int j = cidx[(size_t)q];
+      const int* b = &cidx[(size_t)cptr[(size_t)j]];
+      const int* e = &cidx[(size_t)cptr[(size_t)j + 1]];
+      const int* f = std::lower_bound(b, e, i);
+      if (f == e || *f != i) {
+        hh->err = "pattern is not structurally symmetric";
+        return LPM_ERR_STATE;
+      }
+      const size_t t = (size_t)(cptr[(size_t)j] + (f - b));
+      for (int r = 0; r < dim; ++r)
+        for (int s = 0; s < dim; ++s) vals[(size_t)q * e2 + r * dim + s] = A[(size_t)(s * dim + r) * nb + t];
+    }
+  return LPM_OK;
+}
+
+int lpm_solve(lpm_handle* h, int precision, double tol, int64_t maxit, int64_t* iters, double* relres) {
+  if (!h) return LPM_ERR_ARG;
+  if (!h->have_K) {
+    h->err = "lpm_solve before lpm_assemble";
+    return LPM_ERR_STATE;
+  }
+  long long it = 0;
+  double rr = 0;
+  int st;
+  if (precision == LPM_PREC_FP64)
+    st = solve_fp64(h, tol, maxit, &it, &rr);
+  else if (precision == LPM_PREC_MIXED)
+    st = solve_mixed(h, tol, maxit, &it, &rr);
+  else
+    return arg_error(h, "bad precision");
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
+  return st;
+}
+
+int lpm_move_by_disp(lpm_handle* h) {
+  if (!h) return LPM_ERR_ARG;
+  int st = launch_move_by_disp(h);
+  if (st) return st;
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_newton(lpm_handle* h, int max_iter, double tol, int precision, double cg_tol, int64_t cg_maxit,
+               int* n_iter) {
+  if (!h) return LPM_ERR_ARG;
+  int st = launch_geometry_force(h);
+  if (st) return st;
+  double nr = 0, nR = 0;
+  st = launch_residual(h, &nr, &nR);
+  if (st) return st;
+  const double mult = std::max(nr, nR);
+  int ni = 0;
+  while (nr > tol * mult) {
+    if (++ni > max_iter) {
+      if (n_iter) *n_iter = max_iter;
+      return LPM_NOT_CONVERGED;
+    }
+    st = lpm_solve(h, precision, cg_tol, cg_maxit, nullptr, nullptr);
+    if (st < 0 && st != LPM_ERR_NONFINITE) return st;
+    st = launch_move_by_disp(h);
+    if (st) return st;
+    st = launch_geometry_force(h);
+    if (st) return st;
+    st = launch_residual(h, &nr, &nR);
+    if (st) return st;
+  }
+  if (n_iter) *n_iter = ni;
+  if (!std::isfinite(nr)) {
+    h->err = "non-finite residual in the Newton iteration";
+    return LPM_ERR_NONFINITE;
+  }
+  return LPM_OK;
+}
+
+int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts* o, lpm_step_result* res) {
+  if (!h || !o || nbc < 0 || (nbc > 0 && !bcs)) return arg_error(h, "bad load step");
+  if (o->solver != LPM_SOLVER_STATIC && o->solver != LPM_SOLVER_FATIGUE_STATIC)
+    return arg_error(h, "bad solver kind");
+  for (int k = 0; k < nbc; ++k)
+    if (bcs[k].group < 0 || bcs[k].group >= (int)h->groups.size() || (bcs[k].kind != LPM_BC_DISP &&
+                                                                     bcs[k].kind != LPM_BC_FORCE))
+      return arg_error(h, "bad boundary condition");
+  lpm_step_result r{};
+  const int64_t it0 = h->stats.cg_iters_total;
+  std::vector<double> pending{1.0};
+  int st = LPM_OK;
+  while (!pending.empty()) {
+    const double s = pending.front();
+    for (int k = 0; k < nbc; ++k)
+      if (bcs[k].kind == LPM_BC_FORCE) {
+        st = lpm_apply_force_bc(h, bcs[k].group, bcs[k].mode, bcs[k].fx * s, bcs[k].fy * s, bcs[k].fz * s);
+        if (st) return st;
+      }
+    for (int k = 0; k < nbc; ++k)
+      if (bcs[k].kind == LPM_BC_DISP) {
+        st = lpm_apply_disp_bc(h, bcs[k].group, bcs[k].axis, bcs[k].mode, bcs[k].value * s);
+        if (st) return st;
+      }
+    int ni = 0;
+    bool failed = false;
+    if (o->solver == LPM_SOLVER_FATIGUE_STATIC) {
+      st = lpm_assemble(h, o->tangent, LPM_BC_ELIMINATE);
+      if (st) return st;
+      st = lpm_newton(h, o->max_iter, o->tol, o->precision, o->cg_tol, o->cg_maxit, &ni);
+      if (st < 0) return st;
+      failed = ni >= o->max_iter;
+      if (!failed) {
+        st = lpm_store_state(h);
+        if (st) return st;
+      }
+    } else {
+      int damaged = 0;
+      do {
+        st = lpm_assemble(h, o->tangent, LPM_BC_NONE);
+        if (st) return st;
+        st = lpm_newton(h, o->max_iter, o->tol, o->precision, o->cg_tol, o->cg_maxit, &ni);
+        if (st < 0) return st;
+        if (ni >= o->max_iter) {
+          failed = true;
+          break;
+        }
+        st = launch_static_damage(h, &damaged);
+        if (st) return st;
+        st = lpm_store_state(h);
+        if (st) return st;
+        if (damaged) {
+          ++r.damage_rounds;
+          st = lpm_update_geometry_force(h);
+          if (st) return st;
+        }
+      } while (damaged);
+    }
+    if (failed) {
+      if (++r.cuts > o->max_cuts) {
+        r.cg_iters = h->stats.cg_iters_total - it0;
+        if (res) *res = r;
+        h->err = "load step did not converge after the allowed cut-backs";
+        return LPM_NOT_CONVERGED;
+      }
+      st = lpm_reset_state(h, 1);
+      if (st) return st;
+      pending.front() = 0.5 * s;
+      pending.insert(pending.begin(), 0.5 * s);
+      continue;
+    }
+    r.newton_iters = ni;
+    pending.erase(pending.begin());
+  }
+  r.cg_iters = h->stats.cg_iters_total - it0;
+  if (res) *res = r;
+  return LPM_OK;
+}
+
+int lpm_store_state(lpm_handle* h) {
+  if (!h) return LPM_ERR_ARG;
+  Dev& d = h->d;
+  const size_t N = (size_t)h->n, B = (size_t)h->nb;
+  const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+  LPM_CUDA(h, cudaMemcpyAsync(d.xlast, d.x, sizeof(double) * 3 * N, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.damage_last, d.damage, sizeof(double) * N, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.dis_last, d.dis, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.bdamage_last, d.bdamage, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.bforce_last, d.bforce, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.dLp_last, d.dLp, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_reset_state(lpm_handle* h, int reset_xyz) {
+  if (!h) return LPM_ERR_ARG;
+  Dev& d = h->d;
+  const size_t N = (size_t)h->n, B = (size_t)h->nb;
+  const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+  if (reset_xyz) LPM_CUDA(h, cudaMemcpyAsync(d.x, d.xlast, sizeof(double) * 3 * N, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.damage, d.damage_last, sizeof(double) * N, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.dis, d.dis_last, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.bdamage, d.bdamage_last, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.bforce, d.bforce_last, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.dLp, d.dLp_last, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_get_stats(const lpm_handle* h, lpm_stats* st) {
+  if (!h || !st) return LPM_ERR_ARG;
+  *st = h->stats;
+  return LPM_OK;
+}
+
+int lpm_reset_stats(lpm_handle* h) {
+  if (!h) return LPM_ERR_ARG;
+  h->stats = lpm_stats{};
+  return LPM_OK;
+}
+
+int lpm_set_kernel_timing(lpm_handle* h, int on) {
+  if (!h) return LPM_ERR_ARG;
+  h->timing = on != 0;
+  return LPM_OK;
+}
+
+int lpm_get_stream(const lpm_handle* h, void** stream) {
+  if (!h || !stream) return LPM_ERR_ARG;
+  *stream = (void*)h->stream;
+  return LPM_OK;
+}
+
+int lpm_synchronize(lpm_handle* h) {
+  if (!h) return LPM_ERR_ARG;
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+}  // extern "C"

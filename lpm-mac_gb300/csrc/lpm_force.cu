@@ -1,0 +1,252 @@
+// Force path: bond geometry and nonlocal dilatation sums, bond forces,
+// particle forces / stress / damage_visual, residual and boundary conditions.
+//
+// One thread owns one particle and walks its bonds in stored order, so every
+// per-particle sum adds its terms in the order Particle::bond_layers lists
+// them (particle.h:163-181, 197-240).
+#include "lpm_device.cuh"
+
+namespace lpm {
+namespace {
+
+// Bond geometry + per-layer sums (bond.h:30-39, particle.h:163-181), then
+// the elastic bond force (particle_elastic.h:38-50), which needs the owner's
+// complete dLe_total: bforce = (2 Kn dLe + 2 Tv dLe_total[layer]) (1 - bdamage).
+__global__ void k_geometry_force(int n, const double* __restrict__ x, const int64_t* __restrict__ bptr,
+                                 const int* __restrict__ bp2, const int* __restrict__ blayer,
+                                 const double* __restrict__ dis0, const double* __restrict__ dLp,
+                                 const double* __restrict__ bdamage, const double* __restrict__ Kn,
+                                 const double* __restrict__ Tv, double* __restrict__ dis, double* __restrict__ bstrain,
+                                 double* __restrict__ dLe, double* __restrict__ cs, double* __restrict__ bforce,
+                                 double* __restrict__ dle_tot, double* __restrict__ tdle_tot,
+                                 double* __restrict__ cs_sum) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double xi0 = x[3 * i], xi1 = x[3 * i + 1], xi2 = x[3 * i + 2];
+  double dlt[NL] = {0.0, 0.0}, tdlt[NL] = {0.0, 0.0};
+  double css[NL][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+  const int64_t b0 = bptr[i], b1 = bptr[i + 1];
+  for (int64_t b = b0; b < b1; ++b) {
+    const int j = bp2[b];
+    const double dx = xi0 - x[3 * j], dy = xi1 - x[3 * j + 1], dz = xi2 - x[3 * j + 2];
+    const double d = sqrt(dx * dx + dy * dy + dz * dz);
+    const bool br = is_broken(bdamage[b]);
+    const double d0 = dis0[b];
+    const double dl = br ? 0.0 : (d - d0);
+    const double e = br ? 0.0 : (d - d0 - dLp[b]);
+    const double c0 = br ? 0.0 : dx / d, c1 = br ? 0.0 : dy / d, c2 = br ? 0.0 : dz / d;
+    dis[b] = d;
+    bstrain[b] = br ? 0.0 : dl / d;
+    dLe[b] = e;
+    cs[3 * b] = c0;
+    cs[3 * b + 1] = c1;
+    cs[3 * b + 2] = c2;
+    const int l = blayer[b];
+    dlt[l] += e;
+    tdlt[l] += Tv[b] * e;
+    css[l][0] += c0;
+    css[l][1] += c1;
+    css[l][2] += c2;
+  }
+#pragma unroll
+  for (int l = 0; l < NL; ++l) {
+    dle_tot[NL * i + l] = dlt[l];
+    tdle_tot[NL * i + l] = tdlt[l];
+    cs_sum[(NL * i + l) * 3 + 0] = css[l][0];
+    cs_sum[(NL * i + l) * 3 + 1] = css[l][1];
+    cs_sum[(NL * i + l) * 3 + 2] = css[l][2];
+  }
+  for (int64_t b = b0; b < b1; ++b) {
+    const int l = blayer[b];
+    double f = 2. * Kn[b] * dLe[b] + 2. * Tv[b] * dlt[l];
+    f *= (1.0 - bdamage[b]);
+    bforce[b] = f;
+  }
+}
+
+// Pin = sum cs * (f + f_opposite)/2 (particle.h:197-215); stress from the
+// averaged bond force (particle.h:217-240); damage_visual (particle.h:151-161).
+__global__ void k_particle_force(int n, const int64_t* __restrict__ bptr, const int* __restrict__ opp,
+                                 const double* __restrict__ bforce, const double* __restrict__ cs,
+                                 const double* __restrict__ dis, const double* __restrict__ bdamage,
+                                 const int* __restrict__ nbonds, double pvol, int nneighbors, double* __restrict__ pin,
+                                 double* __restrict__ stress, double* __restrict__ dvis) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double P0 = 0, P1 = 0, P2 = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, dv = 0;
+  const double Vm = pvol * nbonds[i] / nneighbors;
+  const double hv = 0.5 / Vm;
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    const double f = 0.5 * (bforce[b] + bforce[opp[b]]);
+    const double c0 = cs[3 * b], c1 = cs[3 * b + 1], c2 = cs[3 * b + 2];
+    P0 += c0 * f;
+    P1 += c1 * f;
+    P2 += c2 * f;
+    const double sf = hv * dis[b] * f;
+    s0 += sf * c0 * c0;
+    s1 += sf * c1 * c1;
+    s2 += sf * c2 * c2;
+    s3 += sf * c1 * c2;
+    s4 += sf * c0 * c2;
+    s5 += sf * c0 * c1;
+    dv += bdamage[b];
+  }
+  pin[3 * i] = P0;
+  pin[3 * i + 1] = P1;
+  pin[3 * i + 2] = P2;
+  stress[6 * i + 0] = s0;
+  stress[6 * i + 1] = s1;
+  stress[6 * i + 2] = s2;
+  stress[6 * i + 3] = s3;
+  stress[6 * i + 4] = s4;
+  stress[6 * i + 5] = s5;
+  dvis[i] = dv / (double)nbonds[i];
+}
+
+// r = (1 - mask) (Pex - Pin) on the dim DOFs of each particle, |r|^2 and
+// |reaction|^2 (solver.h:108-128, 62-63).
+__global__ void k_residual(int n, int dim, const int* __restrict__ mask, const double* __restrict__ pex,
+                           const double* __restrict__ pin, double* __restrict__ r, double* partials,
+                           unsigned int* ticket, double* norms) {
+  double v[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int k = 0; k < dim; ++k) {
+      const int m = mask[3 * i + k];
+      const double p = pin[3 * i + k];
+      const double ri = (1 - m) * (pex[3 * i + k] - p);
+      r[dim * i + k] = ri;
+      v[0] += ri * ri;
+      if (m == 1) v[1] += p * p;
+    }
+  }
+  double tot[2];
+  if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
+    norms[0] = sqrt(tot[0]);
+    norms[1] = sqrt(tot[1]);
+  }
+}
+
+// Particle::moveBy with Solver::disp (solver.h:97-105): all particles move.
+__global__ void k_move_by(int n, int dim, const double* __restrict__ d, double* __restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = 0; k < dim; ++k) x[3 * i + k] += d[dim * i + k];
+}
+
+// DispBC (solver.h:130-166).
+__global__ void k_disp_bc(const int* __restrict__ ids, int count, int axis, int mode, double value, double* x,
+                          int* mask) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = ids[t];
+  if (mode == 0) {
+    x[3 * i + axis] += value;
+  } else {
+    x[3 * i + 0] = axis == 0 ? value : 0.0;
+    x[3 * i + 1] = axis == 1 ? value : 0.0;
+    x[3 * i + 2] = axis == 2 ? value : 0.0;
+  }
+  mask[3 * i + axis] = 1;
+}
+
+// ForceBC (solver.h:168-190).
+__global__ void k_force_bc(const int* __restrict__ ids, int count, int mode, double fx, double fy, double fz,
+                           double* pex) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = ids[t];
+  const double a = fx / count, b = fy / count, c = fz / count;
+  if (mode == 0) {
+    pex[3 * i] += a;
+    pex[3 * i + 1] += b;
+    pex[3 * i + 2] += c;
+  } else {
+    pex[3 * i] = a;
+    pex[3 * i + 1] = b;
+    pex[3 * i + 2] = c;
+  }
+}
+
+// Brittle bond breaking of the elastic law (particle_elastic.h:52-68):
+// bstrain >= critical_bstrain of the owner breaks an unbroken bond.
+__global__ void k_elastic_break(int n, const int64_t* __restrict__ bptr, const double* __restrict__ bstrain,
+                                const double* __restrict__ crit, double* __restrict__ bdamage, int* any) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double c = crit[i];
+  bool hit = false;
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b)
+    if (bstrain[b] >= c && fabs(bdamage[b] - 1.0) > EPS) {
+      bdamage[b] = 1.0;
+      hit = true;
+    }
+  if (hit) atomicOr(any, 1);
+}
+
+}  // namespace
+
+int launch_static_damage(lpm_handle* h, int* any_new) {
+  const Dev& d = h->d;
+  int* flag = (int*)d.red.ticket + 15;
+  LPM_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+  const int T = 128;
+  k_elastic_break<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.bptr, d.bstrain, d.crit, d.bdamage, flag);
+  LPM_LAUNCHED(h, "k_elastic_break");
+  int v = 0;
+  LPM_CUDA(h, cudaMemcpyAsync(&v, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  *any_new = v;
+  return LPM_OK;
+}
+
+int launch_geometry_force(lpm_handle* h) {
+  const Dev& d = h->d;
+  const int T = 128;
+  k_geometry_force<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.x, d.bptr, d.bp2, d.blayer, d.dis0, d.dLp,
+                                                           d.bdamage, d.Kn, d.Tv, d.dis, d.bstrain, d.dLe, d.cs,
+                                                           d.bforce, d.dle_tot, d.tdle_tot, d.cs_sum);
+  LPM_LAUNCHED(h, "k_geometry_force");
+  k_particle_force<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.bptr, d.opp, d.bforce, d.cs, d.dis, d.bdamage,
+                                                           d.nbonds, h->particle_volume, h->nneighbors, d.pin,
+                                                           d.stress, d.dvis);
+  LPM_LAUNCHED(h, "k_particle_force");
+  return LPM_OK;
+}
+
+int launch_residual(lpm_handle* h, double* norm_r, double* norm_R) {
+  const Dev& d = h->d;
+  const int G = grid_for(h->n, kRedThreads, kMaxRedBlocks);
+  k_residual<<<G, kRedThreads, 0, h->stream>>>(h->n, h->dim, d.mask, d.pex, d.pin, d.rhs, d.red.partials,
+                                               d.red.ticket + 0, d.norms);
+  LPM_LAUNCHED(h, "k_residual");
+  LPM_CUDA(h, cudaMemcpyAsync(h->h_norms, d.norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (norm_r) *norm_r = h->h_norms[0];
+  if (norm_R) *norm_R = h->h_norms[1];
+  return LPM_OK;
+}
+
+int launch_move_by_disp(lpm_handle* h) {
+  const int T = 256;
+  k_move_by<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, h->dim, h->d.disp, h->d.x);
+  LPM_LAUNCHED(h, "k_move_by");
+  return LPM_OK;
+}
+
+int launch_disp_bc(lpm_handle* h, const Group& g, int axis, int mode, double value) {
+  if (g.count == 0) return LPM_OK;
+  const int T = 256;
+  k_disp_bc<<<grid_for(g.count, T), T, 0, h->stream>>>(g.ids, g.count, axis, mode, value, h->d.x, h->d.mask);
+  LPM_LAUNCHED(h, "k_disp_bc");
+  return LPM_OK;
+}
+
+int launch_force_bc(lpm_handle* h, const Group& g, int mode, double fx, double fy, double fz) {
+  if (g.count == 0) return LPM_OK;
+  const int T = 256;
+  k_force_bc<<<grid_for(g.count, T), T, 0, h->stream>>>(g.ids, g.count, mode, fx, fy, fz, h->d.pex);
+  LPM_LAUNCHED(h, "k_force_bc");
+  return LPM_OK;
+}
+
+}  // namespace lpm

@@ -1,0 +1,152 @@
+// Internal declarations shared by the liblpmgpu translation units.
+//
+// Device layout (all arrays live in HBM for the life of the handle):
+//   particles  SoA, positions interleaved xyz (3 doubles per particle even in
+//              2-D, z = 0), per-layer sums [i][layer], stress [i][6]
+//   bonds      CSR by owner particle (bptr), layer 0 then layer 1 inside a
+//              particle (lptr = first layer-1 bond), each group in input
+//              order, as Particle::bond_layers holds them; SoA per field
+//   pattern    conns CSR (cptr, cidx), ascending ids, self included
+//   operator   A = K^T in block-CSR over the same pattern: block (j, i) of A
+//              is K_ij transposed; values stored one array per block element
+//              ("element-major"): A[e * nblk + q], e = r*dim + s, so that a
+//              warp reading consecutive blocks of a row reads consecutive
+//              addresses
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "lpm_gpu.h"
+
+namespace lpm {
+
+constexpr int NL = 2;            // neighbour layers
+constexpr double EPS = 1e-6;     // lpm.h:37
+constexpr int kRedThreads = 256; // threads per block of the reduction kernels
+
+// Scalars of one CG run, resident on the device.
+struct CgScalars {
+  double rhs_norm2;   // |b|^2
+  double threshold;   // max(tol^2 |b|^2, DBL_MIN)
+  double abs_new;     // r . z
+  double alpha, beta;
+  double rr;          // |r|^2 of the last update
+  long long it;       // completed iterations (Eigen's count)
+  long long maxit;
+  int done;           // 0 running, 1 converged, 2 iteration cap, 3 non-finite
+  int pad;
+};
+
+// Deterministic grid reductions: each block writes a partial, the last block
+// to finish (atomic ticket) folds the partials in index order.
+struct RedBuf {
+  double* partials;       // [kMaxRedBlocks * 4]
+  unsigned int* ticket;   // one counter per reduction slot
+};
+constexpr int kMaxRedBlocks = 2048;
+
+struct Group {
+  int* ids;
+  int count;
+};
+
+struct Dev {
+  // particles
+  double *x, *x0, *xlast, *pin, *pex, *stress, *dvis, *dle_tot, *tdle_tot, *cs_sum, *damage, *damage_last;
+  int *mask, *nbonds;
+  // bonds
+  int64_t *bptr, *lptr;
+  int *bp2, *blayer, *opp;
+  double *Kn, *Tv, *dis0, *dis, *dis_last, *dLe, *dLp, *dLp_last, *bstrain, *cs, *bforce, *bforce_last, *bdamage,
+      *bdamage_last;
+  // pattern
+  int64_t* cptr;
+  int *cidx, *diag_slot;
+  // operator values
+  double* A64;
+  float* A32;
+  // solver vectors (n_dof each)
+  double *rhs, *disp, *x64, *r64, *p64, *q64, *invd64;
+  float *b32, *x32, *r32, *p32, *q32, *invd32;
+  // reductions
+  RedBuf red;
+  CgScalars* cg;   // device scalars
+  double* norms;   // device results of small reductions [8]
+  // per-particle flags for the BC elimination
+  unsigned char* fixed;
+  // critical bond strain per particle (elastic law)
+  double* crit;
+};
+
+}  // namespace lpm
+
+struct lpm_handle {
+  int dim = 3, n = 0;
+  int64_t nb = 0, nblk = 0;
+  double particle_volume = 0;
+  int nneighbors = 1;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  lpm::Dev d{};
+  std::vector<lpm::Group> groups;
+  int law = 0;
+  bool have_K = false;
+  bool a32_valid = false;  // FP32 copy of the operator matches A64
+  int tangent = LPM_TANGENT_AS_WRITTEN;
+  // host mirrors
+  lpm::CgScalars* h_cg = nullptr;  // pinned
+  double* h_norms = nullptr;       // pinned [8]
+  lpm_stats stats{};
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<void*> allocations;
+};
+
+namespace lpm {
+
+// ---- kernels launched by the C ABI layer (definitions in the .cu files) ----
+// geometry / force / residual (lpm_force.cu)
+int launch_geometry_force(lpm_handle* h);
+int launch_residual(lpm_handle* h, double* norm_r, double* norm_R);
+int launch_move_by_disp(lpm_handle* h);
+int launch_disp_bc(lpm_handle* h, const Group& g, int axis, int mode, double value);
+int launch_force_bc(lpm_handle* h, const Group& g, int mode, double fx, double fy, double fz);
+int launch_static_damage(lpm_handle* h, int* any_new);
+// pattern / tangent (lpm_tangent.cu)
+int build_pattern(lpm_handle* h);
+int launch_assemble(lpm_handle* h, int tangent, int bc);
+int convert_A32(lpm_handle* h);
+// solvers (lpm_cg.cu)
+int solve_fp64(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);
+int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);
+
+// helpers (lpm_capi.cu)
+int cuda_fail(lpm_handle* h, cudaError_t e, const char* what);
+void* dev_alloc(lpm_handle* h, size_t bytes);
+inline int grid_for(long long work, int threads, int cap = 1 << 20) {
+  long long g = (work + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+}  // namespace lpm
+
+#define LPM_CUDA(h, call)                                  \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return lpm::cuda_fail(h, e_, #call); \
+  } while (0)
+
+#define LPM_LAUNCHED(h, what)                             \
+  do {                                                    \
+    cudaError_t e_ = cudaGetLastError();                  \
+    if (e_ != cudaSuccess) return lpm::cuda_fail(h, e_, what); \
+    (h)->stats.kernel_launches++;                         \
+  } while (0)

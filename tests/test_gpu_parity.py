@@ -1,0 +1,239 @@
+"""GPU path (through the C ABI) against the reference goldens and the oracle.
+
+Bars: integer work (bond order, opposite bonds, pattern) bit-exact; FP64
+force state and tangent within 1e-12 relative to the largest entry; FP64
+solves and load steps within the tolerances written at each assert.
+"""
+import numpy as np
+import pytest
+
+from lpm_cases import (cube, dense_from_bsr, dense_from_csc, golden, golden_meta, gpu_bcs, inputs_from_golden,
+                       make_gpu, make_oracle, mask3, oracle, pkg, plate, rel, tension_bcs)
+
+capi = pkg.capi
+pytestmark = pytest.mark.gpu
+
+KERNEL_CASES = ["kernels_hex", "kernels_sc", "kernels_hex_refmap", "kernels_sc_undamaged"]
+FP_TOL = 1e-12  # force state and tangent (FP64, different summation/FMA order)
+
+
+def _gpu_at_golden_state(d):
+    dim, xyz0, p1, p2, layer, Kn, Tv, cell = inputs_from_golden(d)
+    g = make_gpu(dim, xyz0, p1, p2, layer, Kn, Tv, cell)
+    g.upload(capi.F_XYZ, d["s_xyz"])
+    g.upload(capi.B_BDAMAGE, d["s_bdamage"])
+    g.set_mask(mask3(d, len(xyz0), dim))
+    g.update()
+    return g, dim, len(xyz0)
+
+
+@pytest.mark.parametrize("name", KERNEL_CASES)
+def test_topology_pattern_bit_exact(name):
+    d = golden(name)
+    dim, xyz0, p1, p2, layer, Kn, Tv, cell = inputs_from_golden(d)
+    g = make_gpu(dim, xyz0, p1, p2, layer, Kn, Tv, cell)
+    o = make_oracle(dim, xyz0, p1, p2, layer, Kn, Tv, cell)
+    b = g.bonds()
+    t = o.topology()
+    assert np.array_equal(b["bptr"], t["bptr"])
+    assert np.array_equal(b["bp2"], d["bond_p2"])
+    assert np.array_equal(b["blayer"], d["bond_layer"])
+    assert np.array_equal(b["opp"], t["opp"])
+    cptr, cidx = g.pattern()
+    assert np.array_equal(cptr, d["conn_ptr"])
+    assert np.array_equal(cidx, d["conn_idx"])
+    g.close()
+
+
+@pytest.mark.parametrize("name", KERNEL_CASES)
+def test_force_state(name):
+    d = golden(name)
+    g, dim, n = _gpu_at_golden_state(d)
+    for key, fld in [("dLe_total", capi.F_DLE_TOT), ("TdLe_total", capi.F_TDLE_TOT), ("cs_sum", capi.F_CS_SUM),
+                     ("Pin", capi.F_PIN), ("stress", capi.F_STRESS), ("damage_visual", capi.F_DVIS)]:
+        assert rel(g.download(fld).ravel(), d["s_" + key]) <= FP_TOL, key
+    for key, fld in [("bforce", capi.B_BFORCE), ("dLe", capi.B_DLE)]:
+        assert rel(g.download(fld), d["s_" + key]) <= FP_TOL, key
+    nr, nR = g.residual()
+    assert rel(g.download(capi.F_RESIDUAL), d["residual"]) <= FP_TOL
+    assert nR == pytest.approx(np.linalg.norm(d["reaction"]), rel=1e-12)
+    g.close()
+
+
+@pytest.mark.parametrize("name", KERNEL_CASES)
+def test_tangent_as_written_and_eliminated(name):
+    d = golden(name)
+    g, dim, n = _gpu_at_golden_state(d)
+    cptr, cidx = g.pattern()
+    nd = n * dim
+    g.assemble(capi.TANGENT_AS_WRITTEN, capi.BC_NONE)
+    K = dense_from_bsr(cptr, cidx, g.K_bsr(), n, dim)
+    assert rel(K, dense_from_csc(d["K_csc_outer"], d["K_csc_inner"], d["K_csc_values"], nd)) <= FP_TOL
+    g.assemble(capi.TANGENT_AS_WRITTEN, capi.BC_ELIMINATE)
+    K = dense_from_bsr(cptr, cidx, g.K_bsr(), n, dim)
+    assert rel(K, dense_from_csc(d["Kbc_csc_outer"], d["Kbc_csc_inner"], d["Kbc_csc_values"], nd)) <= FP_TOL
+    g.close()
+
+
+@pytest.mark.parametrize("name", ["kernels_sc_undamaged", "kernels_hex"])
+def test_symmetric_tangent_matches_oracle(name):
+    d = golden(name)
+    g, dim, n = _gpu_at_golden_state(d)
+    o = make_oracle(*inputs_from_golden(d))
+    o.set(oracle.XYZ, d["s_xyz"])
+    o.set_bond(oracle.BDAMAGE, d["s_bdamage"])
+    o.set_mask(mask3(d, n, dim))
+    o.update()
+    for bc in (0, 1):
+        g.assemble(capi.TANGENT_SYMMETRIC, bc)
+        o.assemble(sym=1, bc=bc)
+        assert rel(g.K_bsr(), o.K_bsr()) <= FP_TOL
+    g.close()
+
+
+def test_cg_fp64_matches_oracle():
+    """Symmetric, eliminated tangent of the undamaged cube: CG to 1e-10."""
+    d = golden("kernels_sc_undamaged")
+    g, dim, n = _gpu_at_golden_state(d)
+    o = make_oracle(*inputs_from_golden(d))
+    o.set(oracle.XYZ, d["s_xyz"])
+    o.set_mask(mask3(d, n, dim))
+    o.update()
+    g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_ELIMINATE)
+    o.assemble(sym=1, bc=1)
+    r, _, _ = o.residual()
+    g.residual()
+    it, rr, st = g.solve(capi.PREC_FP64, 1e-10)
+    x, it_o, err_o, st_o = o.cg(r, 1e-10)
+    assert st == 0 and st_o == 0
+    assert abs(it - it_o) <= 2
+    assert rr < 1e-10
+    assert rel(g.download(capi.F_DISP), x) <= 1e-8
+    g.close()
+
+
+def test_cg_zero_rhs_and_maxit():
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = cube(4)
+    g = make_gpu(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    g.update()
+    g.residual()  # zero: undeformed, no loads
+    g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_NONE)
+    it, rr, st = g.solve(capi.PREC_FP64, 1e-10)
+    assert it == 0 and st == 0 and not np.any(g.download(capi.F_DISP))
+    g.close()
+
+
+@pytest.mark.parametrize("name,rtol", [("steps_hex_fatigue", 1e-9), ("steps_sc_fatigue", 1e-6), ("config1_hex", 1e-9)])
+def test_load_steps_as_written_match_reference(name, rtol):
+    """SolverFatigue static steps (as-written tangent, BC elimination, FP64
+    CG at 1e-10) against the reference's positions and reactions.  The SC
+    case runs a CG that stalls (the as-written tangent is not symmetric), so
+    its trajectory is only reproducible to the stall level."""
+    d = golden(name)
+    meta = golden_meta(d)
+    dim, xyz0, p1, p2, layer, Kn, Tv, cell = inputs_from_golden(d)
+    g = make_gpu(dim, xyz0, p1, p2, layer, Kn, Tv, cell)
+    steps, du = int(meta["steps"]), float(meta["du"])
+    groups, _, _ = tension_bcs(xyz0, dim, du)
+    bcs = gpu_bcs(g, groups, dim, du)
+    g.update()
+    n = len(xyz0)
+    xs = d["xyz_steps"].reshape(-1, n, 3)
+    react = d["reaction_top_bottom"].reshape(-1, 2)
+    all_xyz = meta.get("all_xyz", "0") == "1"
+    ax = 1 if dim == 2 else 2
+    for s in range(steps):
+        res = g.load_step(bcs, solver=capi.SOLVER_FATIGUE_STATIC, tangent=capi.TANGENT_AS_WRITTEN,
+                          precision=capi.PREC_FP64, max_iter=30, tol=1e-5, cg_tol=1e-10)
+        assert res["status"] == 0
+        x = g.download(capi.F_XYZ)
+        if all_xyz or s == steps - 1:
+            ref = xs[s if all_xyz else 0]
+            assert rel(x - xyz0, ref - xyz0) <= rtol, "step %d" % s
+        pin = g.download(capi.F_PIN)
+        assert pin[groups["top"], ax].sum() == pytest.approx(react[s, 0], rel=max(rtol, 1e-9))
+    g.close()
+
+
+@pytest.mark.parametrize("maker,args,du", [(plate, (21, 21), 1e-3), (cube, (9,), 2e-3)])
+def test_symmetric_steps_fp64_and_mixed_match_oracle(maker, args, du):
+    """Benchmark semantics (symmetric tangent, BC elimination): FP64 GPU vs
+    oracle within 1e-9, mixed precision vs FP64 GPU within 1e-8."""
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = maker(*args)
+    groups, apply, dd = tension_bcs(xyz, dim, du)
+    o = make_oracle(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    o.update()
+    outs = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        g = make_gpu(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+        bcs = gpu_bcs(g, groups, dim, du)
+        g.update()
+        for s in range(2):
+            res = g.load_step(bcs, tangent=capi.TANGENT_SYMMETRIC, precision=prec, cg_tol=1e-10)
+            assert res["status"] == 0
+        outs[prec] = g.download(capi.F_XYZ) - xyz
+        g.close()
+    for s in range(2):
+        o.load_step(apply, dd, sym=1, bc_elim=1, cg_tol=1e-10)
+    uo = o.get(oracle.XYZ) - xyz
+    assert rel(outs[capi.PREC_FP64], uo) <= 1e-9
+    assert rel(outs[capi.PREC_MIXED], outs[capi.PREC_FP64]) <= 1e-8
+
+
+def test_broken_bonds_carry_no_force():
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = plate(9, 9)
+    g = make_gpu(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    rng = np.random.default_rng(3)
+    g.upload(capi.F_XYZ, xyz + 0.01 * rng.standard_normal(xyz.shape) * np.array([1, 1, 0]))
+    bd = np.zeros(g.nb)
+    bd[::5] = 1.0
+    g.upload(capi.B_BDAMAGE, bd)
+    g.update()
+    f = g.download(capi.B_BFORCE)
+    assert np.all(f[bd == 1.0] == 0.0)
+    assert np.all(g.download(capi.B_CS)[bd == 1.0] == 0.0)
+    g.close()
+
+
+def test_static_damage_breaks_bonds_like_oracle():
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = plate(9, 9)
+    g = make_gpu(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    o = make_oracle(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    x = xyz.copy()
+    x[:, 1] *= 1.002
+    for s in (g, o):
+        s.set_law(0, [1.2e-3])
+    g.upload(capi.F_XYZ, x)
+    o.set(oracle.XYZ, x)
+    g.update()
+    o.update()
+    assert g.update_damage()
+    # oracle: particle_elastic.h:52-68 through its own SolverStatic path
+    bstrain = o.get_bond(oracle.BSTRAIN)
+    expect = (bstrain >= 1.2e-3).astype(float)
+    assert np.array_equal(g.download(capi.B_BDAMAGE), expect)
+    g.close()
+
+
+def test_errors_are_reported():
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = plate(5, 5)
+    g = make_gpu(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    with pytest.raises(capi.LpmError) as e:
+        g.K_bsr()
+    assert e.value.code == capi.ERR_STATE
+    with pytest.raises(capi.LpmError):
+        g.add_group([0, 10 ** 6])
+    g.close()
+
+
+def test_isolated_particle():
+    """A particle with no bonds has an empty pattern row (conns is empty)."""
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = plate(5, 5)
+    xyz2 = np.vstack([xyz, [[100.0, 100.0, 0.0]]])
+    g = make_gpu(dim, xyz2, p1, p2, layer, Kn, Tv, cell)
+    o = make_oracle(dim, xyz2, p1, p2, layer, Kn, Tv, cell)
+    cptr, cidx = g.pattern()
+    t = o.topology()
+    assert np.array_equal(cptr, t["cptr"]) and np.array_equal(cidx, t["cidx"])
+    assert cptr[-1] == cptr[-2]
+    g.close()
