@@ -50,6 +50,10 @@ typedef struct lpm_handle lpm_handle;
 #define LPM_F_XYZ_LAST 10  /* N*3 last converged positions (xyz_last)         */
 #define LPM_F_DISP 11      /* N*dim last Newton increment (Solver::disp)     */
 #define LPM_F_RESIDUAL 12  /* N*dim residual (Stiffness::residual)           */
+#define LPM_F_STATE 13     /* N*nstate state variables (state_var)           */
+#define LPM_F_DDOT_LOCAL 14    /* N local damage rate (Ddot_local)           */
+#define LPM_F_DDOT_NONLOCAL 15 /* N nonlocal damage rate (Ddot_nonlocal)     */
+#define LPM_F_DAMAGE_LAST 16   /* N last converged damage (damage_last)      */
 /* bond fields, stored order (by p1, layer, input order) */
 #define LPM_B_BFORCE 100
 #define LPM_B_BDAMAGE 101
@@ -107,14 +111,43 @@ int lpm_download(lpm_handle* h, int field, double* dst);
 int lpm_set_mask(lpm_handle* h, const int* mask);
 int lpm_get_mask(const lpm_handle* h, int* mask);
 
-/* Material law of all particles.  law 0 = ParticleElastic, params[0] =
- * critical_bstrain (particle_elastic.h:14-68). */
+/* Material law of all particles (the particle class the reference
+ * Assembly was built with) and its parameters: params holds nparams values
+ * for every particle, or N*nparams values when per_particle is set.  Resets
+ * the state variables to the class constructors' values.
+ *   LPM_LAW_ELASTIC      ParticleElastic        {critical_bstrain}
+ *   LPM_LAW_DAMAGE       ParticleElasticDamage  {k0, k1, damage_threshold}
+ *   LPM_LAW_J2           ParticleJ2Plasticity   {E, mu, sigmay, xi, H, A, damage_threshold}
+ *   LPM_LAW_FATIGUE_HCF  ParticleFatigueHCF     {A, B, d, damage_threshold}
+ * (setParticleProperty of particle_elastic.h:70-143,
+ * particle_elastic_damage.h:175-254, particle_j2plasticity.h:154-201,
+ * particle_fatigue_hcf.h:162-209; ParticleJ2Plasticity never sets its
+ * damage_threshold, which stays 0 in the reference). */
 #define LPM_LAW_ELASTIC 0
-int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams);
+#define LPM_LAW_DAMAGE 1
+#define LPM_LAW_J2 2
+#define LPM_LAW_FATIGUE_HCF 3
+int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams, int per_particle);
+/* Particle::type of every particle and the solver's undamaged_pt_type
+ * (particles of that type skip the damage updates, solver_static.h:37,57). */
+int lpm_set_types(lpm_handle* h, const int* types, int undamaged_type);
+/* Assembly::searchNonlocalNeighbors (assembly.h:117-130) result as CSR
+ * (ptr[N+1], idx ascending per particle) and Particle::nonlocal_L. */
+int lpm_set_nonlocal(lpm_handle* h, const int64_t* ptr, const int* idx, const double* nonlocal_L);
+/* Assembly::updateStateVar (assembly.h:161-166): the J2 return map
+ * (particle_j2plasticity.h:78-140), strain-energy damage rate
+ * (particle_elastic_damage.h:150-161), fatigue energy range
+ * (particle_fatigue_hcf.h:127-145). */
+int lpm_update_state(lpm_handle* h);
+/* SolverFatigue::updateFatigueDamage (solver_fatigue.h:75-126): nonlocal
+ * damage rate and D += Ddot * dNdt; *any_new = 1 if damage moved by > 1e-3. */
+int lpm_fatigue_damage(lpm_handle* h, double dNdt, int* any_new);
 
-/* Static damage update of SolverStatic (solver_static.h:31-62) for the
- * elastic law: breaks bonds whose strain reached the critical bond strain
- * (particle_elastic.h:52-68); *any_new = 1 when a bond broke. */
+/* SolverStatic::updateStaticDamage (solver_static.h:31-62): the nonlocal
+ * damage rate (func_phi weights, lpm.h:45-49) and each law's
+ * updateParticleStaticDamage: brittle bond breaking for the elastic law
+ * (particle_elastic.h:52-68), D += Ddot_nonlocal with the threshold for the
+ * damage and J2 laws; *any_new = 1 when something changed noticeably. */
 int lpm_update_damage(lpm_handle* h, int* any_new);
 
 /* Boundary groups: index lists registered once, used by the BC calls below

@@ -15,7 +15,7 @@ OK, NOT_CONVERGED = 0, 1
 ERR_ARG, ERR_TOPOLOGY, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_NONFINITE = -1, -2, -3, -4, -5, -6
 # particle fields
 F_XYZ, F_XYZ0, F_PIN, F_PEX, F_STRESS, F_DVIS, F_DLE_TOT, F_TDLE_TOT, F_CS_SUM, F_DAMAGE, F_XYZ_LAST, F_DISP, \
-    F_RESIDUAL = range(13)
+    F_RESIDUAL, F_STATE, F_DDOT_LOCAL, F_DDOT_NONLOCAL, F_DAMAGE_LAST = range(17)
 # bond fields
 B_BFORCE, B_BDAMAGE, B_DLE, B_DIS, B_BSTRAIN, B_CS, B_KN, B_TV, B_DIS0, B_DLP = range(100, 110)
 TANGENT_AS_WRITTEN, TANGENT_SYMMETRIC = 0, 1
@@ -23,7 +23,8 @@ BC_NONE, BC_ELIMINATE = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 BC_DISP, BC_FORCE = 0, 1
 SOLVER_STATIC, SOLVER_FATIGUE_STATIC = 0, 1
-LAW_ELASTIC = 0
+LAW_ELASTIC, LAW_DAMAGE, LAW_J2, LAW_FATIGUE_HCF = 0, 1, 2, 3
+_NSTATE = {LAW_ELASTIC: 1, LAW_DAMAGE: 1, LAW_J2: 7, LAW_FATIGUE_HCF: 3}
 
 
 class LpmError(RuntimeError):
@@ -91,7 +92,11 @@ def load(build_if_needed=True):
         "lpm_download": [H, ctypes.c_int, dp],
         "lpm_set_mask": [H, ip],
         "lpm_get_mask": [H, ip],
-        "lpm_set_law": [H, ctypes.c_int, dp, ctypes.c_int],
+        "lpm_set_law": [H, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int],
+        "lpm_set_types": [H, ip, ctypes.c_int],
+        "lpm_set_nonlocal": [H, i64p, ip, dp],
+        "lpm_update_state": [H],
+        "lpm_fatigue_damage": [H, ctypes.c_double, ip],
         "lpm_update_damage": [H, ip],
         "lpm_add_group": [H, ip, ctypes.c_int, ip],
         "lpm_apply_disp_bc": [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double],
@@ -126,7 +131,8 @@ def exported_symbols():
     """Names of the C-ABI entry points this binding uses."""
     return ["lpm_set_device", "lpm_create", "lpm_destroy", "lpm_last_error", "lpm_num_bonds", "lpm_num_blocks", "lpm_get_pattern",
             "lpm_get_bonds", "lpm_upload", "lpm_download", "lpm_set_mask", "lpm_get_mask", "lpm_set_law",
-            "lpm_update_damage", "lpm_add_group", "lpm_apply_disp_bc", "lpm_apply_force_bc",
+            "lpm_update_damage", "lpm_set_types", "lpm_set_nonlocal", "lpm_update_state", "lpm_fatigue_damage",
+            "lpm_add_group", "lpm_apply_disp_bc", "lpm_apply_force_bc",
             "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
             "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize"]
@@ -153,7 +159,7 @@ def _l(a):
 
 
 _PWIDTH = {F_XYZ: 3, F_XYZ0: 3, F_PIN: 3, F_PEX: 3, F_STRESS: 6, F_DVIS: 1, F_DLE_TOT: 2, F_TDLE_TOT: 2,
-           F_CS_SUM: 6, F_DAMAGE: 1, F_XYZ_LAST: 3}
+           F_CS_SUM: 6, F_DAMAGE: 1, F_XYZ_LAST: 3, F_DDOT_LOCAL: 1, F_DDOT_NONLOCAL: 1, F_DAMAGE_LAST: 1}
 _BWIDTH = {B_BFORCE: 1, B_BDAMAGE: 1, B_DLE: 1, B_DIS: 1, B_BSTRAIN: 1, B_CS: 3, B_KN: 1, B_TV: 1, B_DIS0: 1,
            B_DLP: 1}
 
@@ -246,8 +252,35 @@ class Lattice:
 
     # -- physics -----------------------------------------------------------
     def set_law(self, law, params):
+        """params: one row for all particles, or an (N, P) array per particle."""
         p = np.ascontiguousarray(params, dtype=np.float64)
-        self._check(self._L.lpm_set_law(self.h, int(law), _d(p), len(p)))
+        per = p.ndim == 2
+        self._check(self._L.lpm_set_law(self.h, int(law), _d(p), p.shape[-1], int(per)))
+        self.law = int(law)
+
+    def set_types(self, types, undamaged):
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        self._check(self._L.lpm_set_types(self.h, _i(t), int(undamaged)))
+
+    def set_nonlocal(self, ptr, idx, L):
+        ptr = np.ascontiguousarray(ptr, dtype=np.int64)
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        L = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (self.n,)))
+        self._check(self._L.lpm_set_nonlocal(self.h, _l(ptr), _i(idx), _d(L)))
+
+    def update_state(self):
+        self._check(self._L.lpm_update_state(self.h))
+
+    def fatigue_damage(self, dNdt):
+        f = ctypes.c_int()
+        self._check(self._L.lpm_fatigue_damage(self.h, float(dNdt), ctypes.byref(f)))
+        return bool(f.value)
+
+    def state(self):
+        ns = _NSTATE[getattr(self, "law", LAW_ELASTIC)]
+        out = np.zeros(self.n * ns)
+        self._check(self._L.lpm_download(self.h, F_STATE, _d(out)))
+        return out.reshape(self.n, ns)
 
     def update(self):
         self._check(self._L.lpm_update_geometry_force(self.h))

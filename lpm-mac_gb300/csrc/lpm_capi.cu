@@ -1,6 +1,7 @@
 // C ABI of liblpmgpu (declared in include/lpm_gpu.h): handle life cycle,
 // host <-> device transfers and the Newton driver.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -80,6 +81,10 @@ FieldRef field_ref(lpm_handle* h, int f) {
     case LPM_F_XYZ_LAST: return {d.xlast, 3 * N};
     case LPM_F_DISP: return {d.disp, D * N};
     case LPM_F_RESIDUAL: return {d.rhs, D * N};
+    case LPM_F_STATE: return {d.state, (size_t)h->nstate * N};
+    case LPM_F_DDOT_LOCAL: return {d.ddot_local, N};
+    case LPM_F_DDOT_NONLOCAL: return {d.ddot_nl, N};
+    case LPM_F_DAMAGE_LAST: return {d.damage_last, N};
     case LPM_B_BFORCE: return {d.bforce, B};
     case LPM_B_BDAMAGE: return {d.bdamage, B};
     case LPM_B_DLE: return {d.dLe, B};
@@ -180,8 +185,21 @@ int lpm_create(int dim, int n, int64_t nb, const double* xyz, const int* p1, con
     lpm_destroy(h);
     return st;
   };
+  // partner-sorted view of each (particle, layer) bond segment, used by the
+  // tangent's common-neighbour merge
+  std::vector<int> sbond(B), sp2(B);
+  for (size_t i = 0; i < N; ++i)
+    for (int l = 0; l < NL; ++l) {
+      const int64_t b0 = l == 0 ? bptr[i] : lptr[i], b1 = l == 0 ? lptr[i] : bptr[i + 1];
+      for (int64_t b = b0; b < b1; ++b) sbond[(size_t)b] = (int)b;
+      std::stable_sort(sbond.begin() + b0, sbond.begin() + b1,
+                       [&](int a, int c) { return bp2[(size_t)a] < bp2[(size_t)c]; });
+      for (int64_t b = b0; b < b1; ++b) sp2[(size_t)b] = bp2[(size_t)sbond[(size_t)b]];
+    }
   Dev& d = h->d;
   bool ok = true;
+  ok = ok && (d.sbond = upload_new(h, sbond.data(), B)) && (d.sp2 = upload_new(h, sp2.data(), B)) &&
+       (d.tsum = zeros_new<double>(h, NL * 3 * N)) && (d.msum = zeros_new<double>(h, NL * 6 * N));
   ok = ok && (d.x = upload_new(h, xyz, 3 * N)) && (d.x0 = upload_new(h, xyz, 3 * N)) &&
        (d.xlast = upload_new(h, xyz, 3 * N));
   ok = ok && (d.pin = zeros_new<double>(h, 3 * N)) && (d.pex = zeros_new<double>(h, 3 * N)) &&
@@ -209,7 +227,10 @@ int lpm_create(int dim, int n, int64_t nb, const double* xyz, const int* p1, con
        (d.red.ticket = zeros_new<unsigned int>(h, 16)) && (d.cg = zeros_new<CgScalars>(h, 1)) &&
        (d.norms = zeros_new<double>(h, 8));
   std::vector<double> crit(N, 1.0);
-  ok = ok && (d.crit = upload_new(h, crit.data(), N));
+  ok = ok && (d.crit = upload_new(h, crit.data(), N)) && (d.pp = upload_new(h, crit.data(), N)) &&
+       (d.ptype = zeros_new<int>(h, N)) && (d.state = zeros_new<double>(h, N)) &&
+       (d.state_last = zeros_new<double>(h, N)) && (d.ddot_local = zeros_new<double>(h, N)) &&
+       (d.ddot_nl = zeros_new<double>(h, N)) && (d.nonlocal_L = zeros_new<double>(h, N));
   if (!ok) return fail(h->err.empty() ? LPM_ERR_CUDA : LPM_ERR_NOMEM);
   if (cudaMallocHost((void**)&h->h_cg, sizeof(CgScalars)) != cudaSuccess ||
       cudaMallocHost((void**)&h->h_norms, 8 * sizeof(double)) != cudaSuccess) {
@@ -310,14 +331,79 @@ int lpm_update_damage(lpm_handle* h, int* any_new) {
   return st;
 }
 
-int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams) {
+int lpm_fatigue_damage(lpm_handle* h, double dNdt, int* any_new) {
   if (!h) return LPM_ERR_ARG;
-  if (law != LPM_LAW_ELASTIC) return arg_error(h, "unknown material law");
-  h->law = law;
-  if (nparams >= 1 && params) {
-    std::vector<double> c((size_t)h->n, params[0]);
-    LPM_CUDA(h, cudaMemcpy(h->d.crit, c.data(), sizeof(double) * h->n, cudaMemcpyHostToDevice));
+  int flag = 0;
+  int st = launch_fatigue_damage(h, dNdt, &flag);
+  if (any_new) *any_new = flag;
+  return st;
+}
+
+int lpm_update_state(lpm_handle* h) {
+  if (!h) return LPM_ERR_ARG;
+  int st = launch_update_state(h);
+  if (st) return st;
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams, int per_particle) {
+  if (!h) return LPM_ERR_ARG;
+  static const int need[4] = {1, 3, 7, 4};
+  if (law < LPM_LAW_ELASTIC || law > LPM_LAW_FATIGUE_HCF) return arg_error(h, "unknown material law");
+  if (nparams < need[law] || !params) return arg_error(h, "too few material parameters for the law");
+  const size_t N = (size_t)h->n;
+  std::vector<double> pp(N * (size_t)nparams);
+  for (size_t i = 0; i < N; ++i)
+    for (int k = 0; k < nparams; ++k) pp[i * nparams + k] = per_particle ? params[i * nparams + k] : params[k];
+  const int ns = law == LPM_LAW_J2 ? 7 : (law == LPM_LAW_FATIGUE_HCF ? 3 : 1);
+  std::vector<double> st(N * (size_t)ns, 0.0);
+  if (law == LPM_LAW_FATIGUE_HCF)
+    for (size_t i = 0; i < N; ++i) st[i * 3 + 1] = (double)INT_MAX;  // particle_fatigue_hcf.h:27
+  Dev& d = h->d;
+  double* npp = upload_new(h, pp.data(), pp.size());
+  double* nst = upload_new(h, st.data(), st.size());
+  double* nsl = upload_new(h, st.data(), st.size());
+  if (!npp || !nst || !nsl) return h->err.empty() ? LPM_ERR_CUDA : LPM_ERR_NOMEM;
+  d.pp = npp;
+  d.state = nst;
+  d.state_last = nsl;
+  if (law == LPM_LAW_ELASTIC) {
+    std::vector<double> c(N);
+    for (size_t i = 0; i < N; ++i) c[i] = pp[i * nparams];
+    LPM_CUDA(h, cudaMemcpy(d.crit, c.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
   }
+  h->law = law;
+  h->law_np = nparams;
+  h->nstate = ns;
+  return LPM_OK;
+}
+
+int lpm_set_types(lpm_handle* h, const int* types, int undamaged_type) {
+  if (!h || !types) return arg_error(h, "NULL handle or types");
+  LPM_CUDA(h, cudaMemcpy(h->d.ptype, types, sizeof(int) * h->n, cudaMemcpyHostToDevice));
+  h->undamaged = undamaged_type;
+  return LPM_OK;
+}
+
+int lpm_set_nonlocal(lpm_handle* h, const int64_t* ptr, const int* idx, const double* L) {
+  if (!h || !ptr || !L) return arg_error(h, "NULL nonlocal arrays");
+  const size_t N = (size_t)h->n;
+  if (ptr[0] != 0) return arg_error(h, "nonlocal pointer must start at 0");
+  for (size_t i = 0; i < N; ++i)
+    if (ptr[i + 1] < ptr[i]) return arg_error(h, "nonlocal pointer not ascending");
+  const int64_t m = ptr[N];
+  if (m > 0 && !idx) return arg_error(h, "NULL nonlocal indices");
+  for (int64_t q = 0; q < m; ++q)
+    if (idx[q] < 0 || idx[q] >= h->n) return arg_error(h, "nonlocal neighbour id out of range");
+  Dev& d = h->d;
+  int64_t* np_ = upload_new(h, ptr, N + 1);
+  int* ni = (int*)dev_alloc(h, sizeof(int) * (size_t)std::max<int64_t>(m, 1));
+  if (!np_ || !ni) return LPM_ERR_NOMEM;
+  if (m) LPM_CUDA(h, cudaMemcpy(ni, idx, sizeof(int) * (size_t)m, cudaMemcpyHostToDevice));
+  LPM_CUDA(h, cudaMemcpy(d.nonlocal_L, L, sizeof(double) * N, cudaMemcpyHostToDevice));
+  d.nl_ptr = np_;
+  d.nl_idx = ni;
   return LPM_OK;
 }
 
@@ -376,14 +462,16 @@ int lpm_get_K(const lpm_handle* h, double* vals) {
     return LPM_ERR_STATE;
   }
   const int dim = h->dim, e2 = dim * dim;
-  const size_t nb = (size_t)h->nblk;
-  std::vector<double> A(nb * e2);
-  std::vector<int64_t> cptr((size_t)h->n + 1);
+  const size_t ns = (size_t)h->nslots, nb = (size_t)h->nblk;
+  std::vector<double> A(ns * e2);
+  std::vector<int64_t> cptr((size_t)h->n + 1), sp((size_t)h->nslice + 1);
   std::vector<int> cidx(nb);
   LPM_CUDA(hh, cudaMemcpy(A.data(), h->d.A64, sizeof(double) * A.size(), cudaMemcpyDeviceToHost));
   LPM_CUDA(hh, cudaMemcpy(cptr.data(), h->d.cptr, sizeof(int64_t) * cptr.size(), cudaMemcpyDeviceToHost));
   LPM_CUDA(hh, cudaMemcpy(cidx.data(), h->d.cidx, sizeof(int) * nb, cudaMemcpyDeviceToHost));
-  // block (i, j) of K is block (j, i) of A transposed
+  LPM_CUDA(hh, cudaMemcpy(sp.data(), h->d.sell_ptr, sizeof(int64_t) * sp.size(), cudaMemcpyDeviceToHost));
+  // block (i, j) of K is block (j, i) of A transposed; (j, i) is the k-th
+  // block of row j, in slot sell_ptr[j/32] + 32 k + j%32
   for (int i = 0; i < h->n; ++i)
     for (int64_t q = cptr[(size_t)i]; q < cptr[(size_t)i + 1]; ++q) {
       const int j = cidx[(size_t)q];
@@ -394,9 +482,9 @@ int lpm_get_K(const lpm_handle* h, double* vals) {
         hh->err = "pattern is not structurally symmetric";
         return LPM_ERR_STATE;
       }
-      const size_t t = (size_t)(cptr[(size_t)j] + (f - b));
+      const size_t slot = (size_t)(sp[(size_t)j / lpm::kSlice] + (f - b) * lpm::kSlice + j % lpm::kSlice);
       for (int r = 0; r < dim; ++r)
-        for (int s = 0; s < dim; ++s) vals[(size_t)q * e2 + r * dim + s] = A[(size_t)(s * dim + r) * nb + t];
+        for (int s = 0; s < dim; ++s) vals[(size_t)q * e2 + r * dim + s] = A[(size_t)(s * dim + r) * ns + slot];
     }
   return LPM_OK;
 }
@@ -493,7 +581,9 @@ int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts
       st = lpm_newton(h, o->max_iter, o->tol, o->precision, o->cg_tol, o->cg_maxit, &ni);
       if (st < 0) return st;
       failed = ni >= o->max_iter;
-      if (!failed) {
+      if (!failed) {  // solver_fatigue.h:266-267
+        st = launch_update_state(h);
+        if (st) return st;
         st = lpm_store_state(h);
         if (st) return st;
       }
@@ -508,6 +598,8 @@ int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts
           failed = true;
           break;
         }
+        st = launch_update_state(h);  // solver_static.h:122-123
+        if (st) return st;
         st = launch_static_damage(h, &damaged);
         if (st) return st;
         st = lpm_store_state(h);
@@ -551,6 +643,7 @@ int lpm_store_state(lpm_handle* h) {
   LPM_CUDA(h, cudaMemcpyAsync(d.bdamage_last, d.bdamage, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.bforce_last, d.bforce, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.dLp_last, d.dLp, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.state_last, d.state, sizeof(double) * N * h->nstate, k, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   return LPM_OK;
 }
@@ -566,6 +659,7 @@ int lpm_reset_state(lpm_handle* h, int reset_xyz) {
   LPM_CUDA(h, cudaMemcpyAsync(d.bdamage, d.bdamage_last, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.bforce, d.bforce_last, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.dLp, d.dLp_last, sizeof(double) * B, k, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.state, d.state_last, sizeof(double) * N * h->nstate, k, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   return LPM_OK;
 }

@@ -15,11 +15,12 @@ namespace {
 __global__ void k_geometry_force(int n, const double* __restrict__ x, const int64_t* __restrict__ bptr,
                                  const int* __restrict__ bp2, const int* __restrict__ blayer,
                                  const double* __restrict__ dis0, const double* __restrict__ dLp,
-                                 const double* __restrict__ bdamage, const double* __restrict__ Kn,
+                                 double* __restrict__ bdamage, const double* __restrict__ Kn,
                                  const double* __restrict__ Tv, double* __restrict__ dis, double* __restrict__ bstrain,
                                  double* __restrict__ dLe, double* __restrict__ cs, double* __restrict__ bforce,
                                  double* __restrict__ dle_tot, double* __restrict__ tdle_tot,
-                                 double* __restrict__ cs_sum) {
+                                 double* __restrict__ cs_sum, const double* __restrict__ damage, int damage_law,
+                                 double* __restrict__ tsum, double* __restrict__ msum) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double xi0 = x[3 * i], xi1 = x[3 * i + 1], xi2 = x[3 * i + 2];
@@ -41,12 +42,20 @@ __global__ void k_geometry_force(int n, const double* __restrict__ x, const int6
     cs[3 * b] = c0;
     cs[3 * b + 1] = c1;
     cs[3 * b + 2] = c2;
-    const int l = blayer[b];
-    dlt[l] += e;
-    tdlt[l] += Tv[b] * e;
-    css[l][0] += c0;
-    css[l][1] += c1;
-    css[l][2] += c2;
+    const double te = Tv[b] * e;
+    if (blayer[b] == 0) {
+      dlt[0] += e;
+      tdlt[0] += te;
+      css[0][0] += c0;
+      css[0][1] += c1;
+      css[0][2] += c2;
+    } else {
+      dlt[1] += e;
+      tdlt[1] += te;
+      css[1][0] += c0;
+      css[1][1] += c1;
+      css[1][2] += c2;
+    }
   }
 #pragma unroll
   for (int l = 0; l < NL; ++l) {
@@ -56,12 +65,44 @@ __global__ void k_geometry_force(int n, const double* __restrict__ x, const int6
     cs_sum[(NL * i + l) * 3 + 1] = css[l][1];
     cs_sum[(NL * i + l) * 3 + 2] = css[l][2];
   }
+  // the damage laws raise the bond damage to the larger particle damage
+  // first (particle_elastic_damage.h:83, particle_j2plasticity.h:72,
+  // particle_fatigue_hcf.h:74)
+  const double di = damage_law ? damage[i] : 0.0;
+  // the tangent's per-particle sums use the final bond damage (the tangent
+  // is assembled after this pass): T = sum w Tv n, M = sum w (2 Kn + Tv) n n^T
+  double T[2 * 3] = {0, 0, 0, 0, 0, 0}, M[2 * 6] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int64_t b = b0; b < b1; ++b) {
-    const int l = blayer[b];
-    double f = 2. * Kn[b] * dLe[b] + 2. * Tv[b] * dlt[l];
-    f *= (1.0 - bdamage[b]);
+    const bool l1 = blayer[b] != 0;
+    double f = 2. * Kn[b] * dLe[b] + 2. * Tv[b] * (l1 ? dlt[1] : dlt[0]);
+    double bd = bdamage[b];
+    if (damage_law) {
+      bd = fmax(bd, fmax(di, damage[bp2[b]]));
+      bdamage[b] = bd;
+    }
+    const double w = 1.0 - bd;
+    f *= w;
     bforce[b] = f;
+    const double c0 = cs[3 * b], c1 = cs[3 * b + 1], c2 = cs[3 * b + 2];
+    const double wt = w * Tv[b], wk = w * (2.0 * Kn[b] + Tv[b]);
+    const double t[3] = {wt * c0, wt * c1, wt * c2};
+    const double m[6] = {wk * c0 * c0, wk * c0 * c1, wk * c0 * c2, wk * c1 * c1, wk * c1 * c2, wk * c2 * c2};
+    if (l1) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) T[3 + k] += t[k];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) M[6 + k] += m[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) T[k] += t[k];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) M[k] += m[k];
+    }
   }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) tsum[NL * 3 * i + k] = T[k];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) msum[NL * 6 * i + k] = M[k];
 }
 
 // Pin = sum cs * (f + f_opposite)/2 (particle.h:197-215); stress from the
@@ -167,44 +208,15 @@ __global__ void k_force_bc(const int* __restrict__ ids, int count, int mode, dou
   }
 }
 
-// Brittle bond breaking of the elastic law (particle_elastic.h:52-68):
-// bstrain >= critical_bstrain of the owner breaks an unbroken bond.
-__global__ void k_elastic_break(int n, const int64_t* __restrict__ bptr, const double* __restrict__ bstrain,
-                                const double* __restrict__ crit, double* __restrict__ bdamage, int* any) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double c = crit[i];
-  bool hit = false;
-  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b)
-    if (bstrain[b] >= c && fabs(bdamage[b] - 1.0) > EPS) {
-      bdamage[b] = 1.0;
-      hit = true;
-    }
-  if (hit) atomicOr(any, 1);
-}
-
 }  // namespace
-
-int launch_static_damage(lpm_handle* h, int* any_new) {
-  const Dev& d = h->d;
-  int* flag = (int*)d.red.ticket + 15;
-  LPM_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
-  const int T = 128;
-  k_elastic_break<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.bptr, d.bstrain, d.crit, d.bdamage, flag);
-  LPM_LAUNCHED(h, "k_elastic_break");
-  int v = 0;
-  LPM_CUDA(h, cudaMemcpyAsync(&v, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
-  *any_new = v;
-  return LPM_OK;
-}
 
 int launch_geometry_force(lpm_handle* h) {
   const Dev& d = h->d;
   const int T = 128;
   k_geometry_force<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.x, d.bptr, d.bp2, d.blayer, d.dis0, d.dLp,
                                                            d.bdamage, d.Kn, d.Tv, d.dis, d.bstrain, d.dLe, d.cs,
-                                                           d.bforce, d.dle_tot, d.tdle_tot, d.cs_sum);
+                                                           d.bforce, d.dle_tot, d.tdle_tot, d.cs_sum, d.damage,
+                                                           h->law != 0 ? 1 : 0, d.tsum, d.msum);
   LPM_LAUNCHED(h, "k_geometry_force");
   k_particle_force<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.bptr, d.opp, d.bforce, d.cs, d.dis, d.bdamage,
                                                            d.nbonds, h->particle_volume, h->nneighbors, d.pin,

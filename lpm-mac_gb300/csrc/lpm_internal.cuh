@@ -7,11 +7,15 @@
 //              particle (lptr = first layer-1 bond), each group in input
 //              order, as Particle::bond_layers holds them; SoA per field
 //   pattern    conns CSR (cptr, cidx), ascending ids, self included
-//   operator   A = K^T in block-CSR over the same pattern: block (j, i) of A
-//              is K_ij transposed; values stored one array per block element
-//              ("element-major"): A[e * nblk + q], e = r*dim + s, so that a
-//              warp reading consecutive blocks of a row reads consecutive
-//              addresses
+//   operator   A = K^T over the same pattern: block (j, i) of A is K_ij
+//              transposed.  Sliced block-ELL storage: rows are grouped in
+//              slices of 32 consecutive rows; block k of row j sits in slot
+//              sell_ptr[j/32] + 32*k + j%32, so the 32 rows of a slice read
+//              their k-th blocks from 32 consecutive slots.  Values are
+//              stored one array per block element ("element-major"):
+//              A[e * nslots + slot], e = r*dim + s.  A thread owns a row;
+//              rows shorter than their slice leave padding slots (zeros,
+//              never read by the row loops)
 #pragma once
 
 #include <cuda_runtime.h>
@@ -38,7 +42,9 @@ struct CgScalars {
   long long it;       // completed iterations (Eigen's count)
   long long maxit;
   int done;           // 0 running, 1 converged, 2 iteration cap, 3 non-finite
-  int pad;
+  int ru;             // mixed solve: a reliable update is pending
+  double rmax;        // mixed solve: largest |r| since the last reliable update
+  long long ru_count; // mixed solve: reliable updates taken
 };
 
 // Deterministic grid reductions: each block writes a partial, the last block
@@ -48,6 +54,7 @@ struct RedBuf {
   unsigned int* ticket;   // one counter per reduction slot
 };
 constexpr int kMaxRedBlocks = 2048;
+constexpr int kSlice = 32;  // rows per slice of the sliced operator
 
 struct Group {
   int* ids;
@@ -58,14 +65,21 @@ struct Dev {
   // particles
   double *x, *x0, *xlast, *pin, *pex, *stress, *dvis, *dle_tot, *tdle_tot, *cs_sum, *damage, *damage_last;
   int *mask, *nbonds;
+  // per particle and layer, for the tangent: T = sum w Tv n, M = sum w (2Kn+Tv) n n^T
+  // (upper triangle xx xy xz yy yz zz)
+  double *tsum, *msum;
   // bonds
   int64_t *bptr, *lptr;
   int *bp2, *blayer, *opp;
+  int *sbond, *sp2;  // per (particle, layer) segment: bond ids and partners sorted by partner id
   double *Kn, *Tv, *dis0, *dis, *dis_last, *dLe, *dLp, *dLp_last, *bstrain, *cs, *bforce, *bforce_last, *bdamage,
       *bdamage_last;
-  // pattern
+  // pattern (CSR) and its sliced layout
   int64_t* cptr;
-  int *cidx, *diag_slot;
+  int *cidx, *diag_slot;  // diag_slot: slot of the diagonal block (sliced)
+  int64_t* sell_ptr;      // [nslice + 1] first slot of each slice
+  int* scol;              // [nslots] column (particle id) of each slot
+  int* rowlen;            // [n] blocks in each row
   // operator values
   double* A64;
   float* A32;
@@ -80,6 +94,11 @@ struct Dev {
   unsigned char* fixed;
   // critical bond strain per particle (elastic law)
   double* crit;
+  // material laws: type, parameters, state variables, damage rates
+  int* ptype;
+  double *pp, *state, *state_last, *ddot_local, *ddot_nl, *nonlocal_L;
+  int64_t* nl_ptr;  // nonlocal neighbours (CSR, ascending ids)
+  int* nl_idx;
 };
 
 }  // namespace lpm
@@ -87,6 +106,8 @@ struct Dev {
 struct lpm_handle {
   int dim = 3, n = 0;
   int64_t nb = 0, nblk = 0;
+  int64_t nslots = 0;  // sliced slots (nblk plus padding)
+  int nslice = 0;
   double particle_volume = 0;
   int nneighbors = 1;
   int device = 0;
@@ -95,6 +116,9 @@ struct lpm_handle {
   lpm::Dev d{};
   std::vector<lpm::Group> groups;
   int law = 0;
+  int law_np = 1;      // parameters per particle
+  int nstate = 1;      // state variables per particle
+  int undamaged = -1;  // particle type that skips damage updates
   bool have_K = false;
   bool a32_valid = false;  // FP32 copy of the operator matches A64
   int tangent = LPM_TANGENT_AS_WRITTEN;
@@ -117,7 +141,10 @@ int launch_residual(lpm_handle* h, double* norm_r, double* norm_R);
 int launch_move_by_disp(lpm_handle* h);
 int launch_disp_bc(lpm_handle* h, const Group& g, int axis, int mode, double value);
 int launch_force_bc(lpm_handle* h, const Group& g, int mode, double fx, double fy, double fz);
+// material laws (lpm_laws.cu)
+int launch_update_state(lpm_handle* h);
 int launch_static_damage(lpm_handle* h, int* any_new);
+int launch_fatigue_damage(lpm_handle* h, double dt, int* any_new);
 // pattern / tangent (lpm_tangent.cu)
 int build_pattern(lpm_handle* h);
 int launch_assemble(lpm_handle* h, int tangent, int bc);

@@ -1,0 +1,259 @@
+// Material laws: state-variable updates (Assembly::updateStateVar), the
+// nonlocal damage rate, and the static / fatigue damage updates.
+//
+// One thread per particle; each particle's sums walk its bonds and its
+// nonlocal neighbours in stored (ascending) order, the order the reference
+// loops use.
+//   law 1 ParticleElasticDamage  params {k0, k1, damage_threshold}
+//   law 2 ParticleJ2Plasticity   params {E, mu, sigmay, xi, H, A, damage_threshold}
+//   law 3 ParticleFatigueHCF     params {A, B, d, damage_threshold}
+#include <climits>
+
+#include "lpm_device.cuh"
+
+namespace lpm {
+namespace {
+
+struct LawView {
+  int n, law, np, ns, undamaged;
+  double pvol;
+  int nneighbors;
+  const int64_t *bptr, *lptr;
+  const int *bp2, *blayer, *nbonds, *ptype;
+  const double *Kn, *dLe, *dis, *cs, *dle_tot, *tdle_tot, *stress, *pp, *x, *nonlocal_L;
+  double *dLp, *state, *ddot_local, *ddot_nl, *damage, *bdamage;
+  const double *state_last, *damage_last, *bstrain, *crit;
+  const int64_t* nl_ptr;
+  const int* nl_idx;
+};
+
+// particle_elastic_damage.h:89-104 (the total of particle_fatigue_hcf.h:82-125
+// is the same sum)
+__device__ double strain_energy(const LawView& v, int i) {
+  const double Vm = v.pvol * v.nbonds[i] / v.nneighbors;
+  double e = 0.0;
+  for (int l = 0; l < NL; ++l) {
+    const int64_t b0 = l == 0 ? v.bptr[i] : v.lptr[i], b1 = l == 0 ? v.lptr[i] : v.bptr[i + 1];
+    for (int64_t b = b0; b < b1; ++b) e += 0.5 * (v.Kn[b] * v.dLe[b] * v.dLe[b]) / Vm;
+    e += 0.5 * v.tdle_tot[NL * i + l] * v.dle_tot[NL * i + l] / Vm;
+  }
+  return e;
+}
+
+__global__ void k_update_state(LawView v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n) return;
+  const double* P = v.pp + (int64_t)i * v.np;
+  double* sv = v.state + (int64_t)i * v.ns;
+  const double* svl = v.state_last + (int64_t)i * v.ns;
+  if (v.law == 1) {  // particle_elastic_damage.h:150-161
+    const double k0 = P[0], k1 = P[1];
+    sv[0] = strain_energy(v, i);
+    const double delta = sv[0] - svl[0];
+    const double f = sv[0] - k1 * v.damage[i] - k0;
+    v.ddot_local[i] = (f > 0 && delta > 0) ? (1 / k1) * delta : 0.0;
+  } else if (v.law == 2) {  // particle_j2plasticity.h:78-140 (radial return)
+    const double E = P[0], mu = P[1], sigmay = P[2], xi = P[3], H = P[4], A = P[5];
+    double st[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) st[j] = v.stress[6 * (int64_t)i + j];
+    const double sigma_m = 1.0 / 3.0 * (st[0] + st[1] + st[2]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) st[j] -= sigma_m;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) st[j] -= sv[j + 1];
+    double seq = 0.0;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) seq += (j < 3 ? 1.0 : 2.0) * st[j] * st[j];
+    seq = sqrt(3.0 / 2.0 * seq);
+    const double yf = seq - (sigmay + (1.0 - xi) * H * sv[0]);
+    const double G = E / 2 / (1 + mu);
+    const double dl = yf > 0.0 ? yf / (3 * G + H) : 0.0;
+    sv[0] += dl;
+    double dp[6] = {0, 0, 0, 0, 0, 0};
+    if (fabs(seq) > EPS) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        dp[j] = dl * 1.5 * st[j] / seq;
+        sv[j + 1] += 2. / 3. * xi * H * dp[j];
+      }
+    }
+    if (dl != 0.0)
+      for (int64_t b = v.bptr[i]; b < v.bptr[i + 1]; ++b) {
+        const double c0 = v.cs[3 * b], c1 = v.cs[3 * b + 1], c2 = v.cs[3 * b + 2];
+        v.dLp[b] += v.dis[b] * (dp[0] * c0 * c0 + dp[1] * c1 * c1 + dp[2] * c2 * c2 + 2 * dp[3] * c1 * c2 +
+                                2 * dp[4] * c0 * c2 + 2 * dp[5] * c0 * c1);
+      }
+    const double tri = seq > EPS ? sigma_m / seq : 0.0;
+    v.ddot_local[i] = dl * (1.0 + A * tri);
+  } else if (v.law == 3) {  // particle_fatigue_hcf.h:127-145
+    const double A = P[0], B = P[1], d = P[2];
+    const double u = strain_energy(v, i);
+    sv[1] = fmin(u, sv[1]);
+    sv[2] = fmax(u, sv[2]);
+    sv[0] = fmax(sv[2], sv[0]);
+    v.ddot_local[i] = (sv[2] - sv[1] > 0) ? A * pow(sv[0], B) * pow(sv[2] - sv[1], d) : 0.0;
+  }
+}
+
+// func_phi (lpm.h:45-49) and the nonlocal damage rate of
+// SolverStatic::updateStaticDamage / SolverFatigue::updateFatigueDamage
+// (solver_static.h:34-54, solver_fatigue.h:79-116).
+__device__ __forceinline__ double phi(double x, double L) {
+  const double t = x / L;
+  const double t2 = t * t, t4 = t2 * t2;
+  const double g = 1 / (1 + t4 * t4);
+  return g * g;
+}
+
+__global__ void k_nonlocal_rate(LawView v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n || v.ptype[i] == v.undamaged) return;
+  double A = 0.0, D = 0.0;
+  const double x0 = v.x[3 * i], x1 = v.x[3 * i + 1], x2 = v.x[3 * i + 2];
+  const double L = v.nonlocal_L[i];
+  for (int64_t q = v.nl_ptr[i]; q < v.nl_ptr[i + 1]; ++q) {
+    const int j = v.nl_idx[q];
+    if (v.ptype[j] == v.undamaged) continue;
+    const double dx = x0 - v.x[3 * j], dy = x1 - v.x[3 * j + 1], dz = x2 - v.x[3 * j + 2];
+    const double w = phi(sqrt(dx * dx + dy * dy + dz * dz), L) * (v.pvol * v.nbonds[j] / v.nneighbors);
+    D += v.ddot_local[j] * w;
+    A += w;
+  }
+  v.ddot_nl[i] = D / A;
+}
+
+// updateParticleStaticDamage of each law (particle_elastic.h:52-68,
+// particle_elastic_damage.h:163-173, particle_j2plasticity.h:142-152).
+__global__ void k_static_damage(LawView v, int* any) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n || v.ptype[i] == v.undamaged) return;
+  bool hit = false;
+  if (v.law == 0) {
+    const double c = v.crit[i];
+    for (int64_t b = v.bptr[i]; b < v.bptr[i + 1]; ++b)
+      if (v.bstrain[b] >= c && fabs(v.bdamage[b] - 1.0) > EPS) {
+        v.bdamage[b] = 1.0;
+        hit = true;
+      }
+  } else if (v.law == 1 || v.law == 2) {
+    const double thr = v.pp[(int64_t)i * v.np + (v.law == 1 ? 2 : 6)];
+    double d = v.damage[i] + v.ddot_nl[i];
+    if (d >= thr) d = 1.0;
+    v.damage[i] = d;
+    hit = fabs(d - v.damage_last[i]) > 1e-3;
+  }
+  if (hit) atomicOr(any, 1);
+}
+
+// ParticleFatigueHCF::updateParticleFatigueDamage (particle_fatigue_hcf.h:147-160).
+__global__ void k_fatigue_damage(LawView v, double dt, int* any) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n || v.ptype[i] == v.undamaged || v.law != 3) return;
+  const double thr = v.pp[(int64_t)i * v.np + 3];
+  double d = v.damage[i] + v.ddot_nl[i] * dt;
+  if (d >= thr) d = 1.0;
+  v.damage[i] = d;
+  v.state[(int64_t)i * v.ns + 1] = (double)INT_MAX;
+  v.state[(int64_t)i * v.ns + 2] = 0.0;
+  if (fabs(d - v.damage_last[i]) > 1e-3) atomicOr(any, 1);
+}
+
+LawView law_view(lpm_handle* h) {
+  Dev& d = h->d;
+  LawView v;
+  v.n = h->n;
+  v.law = h->law;
+  v.np = h->law_np;
+  v.ns = h->nstate;
+  v.undamaged = h->undamaged;
+  v.pvol = h->particle_volume;
+  v.nneighbors = h->nneighbors;
+  v.bptr = d.bptr;
+  v.lptr = d.lptr;
+  v.bp2 = d.bp2;
+  v.blayer = d.blayer;
+  v.nbonds = d.nbonds;
+  v.ptype = d.ptype;
+  v.Kn = d.Kn;
+  v.dLe = d.dLe;
+  v.dis = d.dis;
+  v.cs = d.cs;
+  v.dle_tot = d.dle_tot;
+  v.tdle_tot = d.tdle_tot;
+  v.stress = d.stress;
+  v.pp = d.pp;
+  v.x = d.x;
+  v.nonlocal_L = d.nonlocal_L;
+  v.dLp = d.dLp;
+  v.state = d.state;
+  v.ddot_local = d.ddot_local;
+  v.ddot_nl = d.ddot_nl;
+  v.damage = d.damage;
+  v.bdamage = d.bdamage;
+  v.state_last = d.state_last;
+  v.damage_last = d.damage_last;
+  v.bstrain = d.bstrain;
+  v.crit = d.crit;
+  v.nl_ptr = d.nl_ptr;
+  v.nl_idx = d.nl_idx;
+  return v;
+}
+
+int read_flag(lpm_handle* h, int* flag, int* out) {
+  int v = 0;
+  LPM_CUDA(h, cudaMemcpyAsync(&v, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  *out = v;
+  return LPM_OK;
+}
+
+}  // namespace
+
+int launch_update_state(lpm_handle* h) {
+  if (h->law == 0) return LPM_OK;  // ParticleElastic has no state update
+  const int T = 128;
+  k_update_state<<<grid_for(h->n, T), T, 0, h->stream>>>(law_view(h));
+  LPM_LAUNCHED(h, "k_update_state");
+  return LPM_OK;
+}
+
+int launch_static_damage(lpm_handle* h, int* any_new) {
+  int* flag = (int*)h->d.red.ticket + 15;
+  LPM_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+  const int T = 128;
+  const LawView v = law_view(h);
+  if (h->law == 1 || h->law == 2) {
+    if (!h->d.nl_ptr) {
+      h->err = "damage law without nonlocal neighbours (lpm_set_nonlocal)";
+      return LPM_ERR_STATE;
+    }
+    k_nonlocal_rate<<<grid_for(h->n, T), T, 0, h->stream>>>(v);
+    LPM_LAUNCHED(h, "k_nonlocal_rate");
+  }
+  if (h->law <= 2) {
+    k_static_damage<<<grid_for(h->n, T), T, 0, h->stream>>>(v, flag);
+    LPM_LAUNCHED(h, "k_static_damage");
+  }
+  return read_flag(h, flag, any_new);
+}
+
+int launch_fatigue_damage(lpm_handle* h, double dt, int* any_new) {
+  int* flag = (int*)h->d.red.ticket + 15;
+  LPM_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+  if (h->law == 3) {
+    if (!h->d.nl_ptr) {
+      h->err = "fatigue law without nonlocal neighbours (lpm_set_nonlocal)";
+      return LPM_ERR_STATE;
+    }
+    const int T = 128;
+    const LawView v = law_view(h);
+    k_nonlocal_rate<<<grid_for(h->n, T), T, 0, h->stream>>>(v);
+    LPM_LAUNCHED(h, "k_nonlocal_rate");
+    k_fatigue_damage<<<grid_for(h->n, T), T, 0, h->stream>>>(v, dt, flag);
+    LPM_LAUNCHED(h, "k_fatigue_damage");
+  }
+  return read_flag(h, flag, any_new);
+}
+
+}  // namespace lpm

@@ -74,57 +74,86 @@ __global__ void k_fill_candidates(int n, const int64_t* __restrict__ bptr, const
 }
 
 __global__ void k_compact_pattern(int n, const int64_t* __restrict__ cand_ptr, const int* __restrict__ cand,
-                                  const int64_t* __restrict__ cptr, int* __restrict__ cidx, int* __restrict__ diag_slot) {
+                                  const int64_t* __restrict__ cptr, int* __restrict__ cidx) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int* c = cand + cand_ptr[i];
   const int64_t q0 = cptr[i], len = cptr[i + 1] - q0;
+  for (int64_t a = 0; a < len; ++a) cidx[q0 + a] = c[a];
+}
+
+// Sliced layout: slot columns, row lengths and the diagonal slot.
+__global__ void k_fill_sell(int n, const int64_t* __restrict__ cptr, const int* __restrict__ cidx,
+                            const int64_t* __restrict__ sell_ptr, int* __restrict__ scol, int* __restrict__ rowlen,
+                            int* __restrict__ diag_slot) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int64_t q0 = cptr[j];
+  const int len = (int)(cptr[j + 1] - q0);
+  const int64_t base = sell_ptr[j / kSlice] + (j % kSlice);
   int ds = -1;
-  for (int64_t a = 0; a < len; ++a) {
-    cidx[q0 + a] = c[a];
-    if (c[a] == i) ds = (int)(q0 + a);
+  for (int k = 0; k < len; ++k) {
+    const int c = cidx[q0 + k];
+    scol[base + (int64_t)k * kSlice] = c;
+    if (c == j) ds = (int)(base + (int64_t)k * kSlice);
   }
-  diag_slot[i] = ds;
+  rowlen[j] = len;
+  diag_slot[j] = ds;
 }
 
 struct AsmView {
-  const int64_t *bptr, *lptr, *cptr;
-  const int *bp2, *cidx;
-  const double *cs, *cs_sum, *Kn, *Tv, *bdamage;
+  const int64_t *bptr, *lptr, *sell_ptr;
+  const int *scol, *rowlen, *sbond, *sp2, *opp;
+  const double *cs, *cs_sum, *tsum, *msum, *Kn, *Tv, *bdamage;
   double* A;
-  int64_t nblk;
-  int n, sym;
+  int64_t nslots;
+  int n, nslice, sym;
 };
 
-// derivative.h:8-45
-template <int DIM>
-__device__ __forceinline__ void diag_block(const AsmView& v, int i, double (&K)[3][3]) {
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) K[r][c] = 0.0;
-  for (int l = 0; l < NL; ++l) {
-    const double* S = v.cs_sum + (NL * i + l) * 3;
-    const double S0 = S[0], S1 = S[1], S2 = S[2];
-    const double Sv[3] = {S0, S1, S2};
-    int64_t lb, le;
-    layer_range(v.bptr, v.lptr, i, l, lb, le);
-    for (int64_t b = lb; b < le; ++b) {
-      const double nv[3] = {v.cs[3 * b], v.cs[3 * b + 1], v.cs[3 * b + 2]};
-      const double w = 1 - v.bdamage[b], kn = v.Kn[b], tv = v.Tv[b], kt = kn + tv;
-#pragma unroll
-      for (int r = 0; r < DIM; ++r)
-#pragma unroll
-        for (int c = r; c < DIM; ++c) K[r][c] += w * ((kn * nv[c] + tv * Sv[c]) * nv[r] + kt * nv[r] * nv[c]);
-    }
-  }
-  K[1][0] = v.sym ? K[0][1] : K[1][0];
-  K[2][0] = K[0][2];
-  K[2][1] = K[1][2];
+// The analytical tangent (derivative.h) restated per block K_ij, i != j, as
+// a sum over layers l of
+//   own    (i->j a layer-l bond b):   w_b[(-Kn n_b[s] + Tv S_j[s]) n_b[r] - (Kn+Tv) n_b[r] n_b[s]]
+//   other  (same b, derivative.h:91-99 summed over the other bonds of i):
+//          -1/2 [w_b Tv_b (S_i - n_b) + (T_i - w_b Tv_b n_b)][r] n_b[s]
+//   paths  (bonds i->k, k->j of layer l, derivative.h:101-115 and 122-139):
+//          -1/2 (w_kj Tv_kj + w_ik Tv_ik) n_ik[r] n_kj[s]
+// with S_i = sum of i's layer-l direction cosines, T_i = sum w Tv n over i's
+// layer-l bonds.  The diagonal block (derivative.h:8-45) is
+//   K_ii[r][s] = sum_l M_i[r][s] + T_i[r] S_i[s]   (r <= s),  M_i = sum w (2Kn+Tv) n n^T,
+// then mirrored as derivative.h:37-42 does ([1][0] stays 0 in the as-written
+// variant).  Common neighbours k of i and j come from a merge of the two
+// particles' partner-sorted layer-l bond lists.
+__device__ __forceinline__ void seg(const int64_t* bptr, const int64_t* lptr, int i, int l, int64_t& b, int64_t& e) {
+  b = l == 0 ? bptr[i] : lptr[i];
+  e = l == 0 ? lptr[i] : bptr[i + 1];
 }
 
-// derivative.h:47-142 (layer 0) and 144-239 (layer 1), summed as
-// stiffness.h:72-98 does.
+template <int DIM>
+__device__ __forceinline__ void diag_block(const AsmView& v, int i, double (&K)[3][3]) {
+  double k00 = 0, k01 = 0, k02 = 0, k11 = 0, k12 = 0, k22 = 0;
+#pragma unroll
+  for (int l = 0; l < NL; ++l) {
+    const double* M = v.msum + (NL * i + l) * 6;
+    const double* T = v.tsum + (NL * i + l) * 3;
+    const double* S = v.cs_sum + (NL * i + l) * 3;
+    k00 += M[0] + T[0] * S[0];
+    k01 += M[1] + T[0] * S[1];
+    k02 += M[2] + T[0] * S[2];
+    k11 += M[3] + T[1] * S[1];
+    k12 += M[4] + T[1] * S[2];
+    k22 += M[5] + T[2] * S[2];
+  }
+  K[0][0] = k00;
+  K[0][1] = k01;
+  K[0][2] = k02;
+  K[1][0] = v.sym ? k01 : 0.0;
+  K[1][1] = k11;
+  K[1][2] = k12;
+  K[2][0] = k02;
+  K[2][1] = k12;
+  K[2][2] = k22;
+}
+
 template <int DIM>
 __device__ __forceinline__ void off_block(const AsmView& v, int i, int j, double (&K)[3][3]) {
 #pragma unroll
@@ -137,73 +166,44 @@ __device__ __forceinline__ void off_block(const AsmView& v, int i, int j, double
     for (int r = 0; r < 3; ++r)
 #pragma unroll
       for (int c = 0; c < 3; ++c) B[r][c] = 0.0;
-    int64_t lb, le;
-    layer_range(v.bptr, v.lptr, i, l, lb, le);
-    int64_t b1 = -1;
-    for (int64_t b = lb; b < le; ++b)
-      if (v.bp2[b] == j) {
-        b1 = b;
-        break;
-      }
-    if (b1 >= 0) {
-      const double n1[3] = {v.cs[3 * b1], v.cs[3 * b1 + 1], v.cs[3 * b1 + 2]};
-      const double w1t = (1 - v.bdamage[b1]) * v.Tv[b1];
-      for (int64_t b2 = lb; b2 < le; ++b2) {
-        const int k = v.bp2[b2];
-        const double n2[3] = {v.cs[3 * b2], v.cs[3 * b2 + 1], v.cs[3 * b2 + 2]};
-        const double w2 = 1 - v.bdamage[b2];
-        if (k == j) {
-          const double* S = v.cs_sum + (NL * j + l) * 3;
-          const double Sj[3] = {S[0], S[1], S[2]};
-          const double kn = v.Kn[b2], tv = v.Tv[b2], kt = kn + tv;
+    int64_t ia, ea, ib, eb;
+    seg(v.bptr, v.lptr, i, l, ia, ea);
+    seg(v.bptr, v.lptr, j, l, ib, eb);
+    int direct = -1;
+    // merge of the partner-sorted lists; the direct bond i->j shows up as
+    // partner j in i's list
+    while (ia < ea) {
+      const int pa = v.sp2[ia];
+      if (pa == j) direct = v.sbond[ia];
+      while (ib < eb && v.sp2[ib] < pa) ++ib;
+      if (ib < eb && v.sp2[ib] == pa) {
+        const int b1 = v.sbond[ia];           // i -> k
+        const int b3 = v.opp[v.sbond[ib]];    // k -> j, opposite of j -> k
+        const double h = 0.5 * ((1 - v.bdamage[b3]) * v.Tv[b3] + (1 - v.bdamage[b1]) * v.Tv[b1]);
+        const double n1[3] = {v.cs[3 * (int64_t)b1], v.cs[3 * (int64_t)b1 + 1], v.cs[3 * (int64_t)b1 + 2]};
+        const double n3[3] = {v.cs[3 * (int64_t)b3], v.cs[3 * (int64_t)b3 + 1], v.cs[3 * (int64_t)b3 + 2]};
 #pragma unroll
-          for (int r = 0; r < DIM; ++r)
+        for (int r = 0; r < DIM; ++r) {
+          const double hr = h * n1[r];
 #pragma unroll
-            for (int c = 0; c < DIM; ++c) B[r][c] += w2 * ((-kn * n2[c] + tv * Sj[c]) * n2[r] - kt * n2[r] * n2[c]);
-        } else {
-          const double w2t = w2 * v.Tv[b2];
-          const double hh = 0.5 * (w1t + w2t);
-#pragma unroll
-          for (int r = 0; r < DIM; ++r)
-#pragma unroll
-            for (int c = 0; c < DIM; ++c) B[r][c] -= hh * n2[r] * n1[c];
-          int64_t kb, ke;
-          layer_range(v.bptr, v.lptr, k, l, kb, ke);
-          for (int64_t b3 = kb; b3 < ke; ++b3) {
-            if (v.bp2[b3] != j) continue;
-            const double n3[3] = {v.cs[3 * b3], v.cs[3 * b3 + 1], v.cs[3 * b3 + 2]};
-            const double h3 = 0.5 * ((1 - v.bdamage[b3]) * v.Tv[b3] + w2t);
-#pragma unroll
-            for (int r = 0; r < DIM; ++r)
-#pragma unroll
-              for (int c = 0; c < DIM; ++c) B[r][c] -= h3 * n2[r] * n3[c];
-          }
+          for (int c = 0; c < DIM; ++c) B[r][c] -= hr * n3[c];
         }
       }
-    } else {
-      for (int64_t ba = lb; ba < le; ++ba) {
-        const int k = v.bp2[ba];
-        int64_t kb, ke;
-        layer_range(v.bptr, v.lptr, k, l, kb, ke);
-        double n1[3];
-        bool loaded = false;
-        double w1t = 0.0;
-        for (int64_t bb = kb; bb < ke; ++bb) {
-          if (v.bp2[bb] != j) continue;
-          if (!loaded) {
-            n1[0] = v.cs[3 * ba];
-            n1[1] = v.cs[3 * ba + 1];
-            n1[2] = v.cs[3 * ba + 2];
-            w1t = (1 - v.bdamage[ba]) * v.Tv[ba];
-            loaded = true;
-          }
-          const double n2[3] = {v.cs[3 * bb], v.cs[3 * bb + 1], v.cs[3 * bb + 2]};
-          const double hh = 0.5 * ((1 - v.bdamage[bb]) * v.Tv[bb] + w1t);
+      ++ia;
+    }
+    if (direct >= 0) {
+      const int64_t b = direct;
+      const double n[3] = {v.cs[3 * b], v.cs[3 * b + 1], v.cs[3 * b + 2]};
+      const double w = 1 - v.bdamage[b], kn = v.Kn[b], tv = v.Tv[b], kt = kn + tv, wt = w * tv;
+      const double* Sj = v.cs_sum + (NL * j + l) * 3;
+      const double* Si = v.cs_sum + (NL * i + l) * 3;
+      const double* Ti = v.tsum + (NL * i + l) * 3;
 #pragma unroll
-          for (int r = 0; r < DIM; ++r)
+      for (int r = 0; r < DIM; ++r) {
+        const double o = 0.5 * (wt * (Si[r] - n[r]) + (Ti[r] - wt * n[r]));
 #pragma unroll
-            for (int c = 0; c < DIM; ++c) B[r][c] -= hh * n1[r] * n2[c];
-        }
+        for (int c = 0; c < DIM; ++c)
+          B[r][c] += w * ((-kn * n[c] + tv * Sj[c]) * n[r] - kt * n[r] * n[c]) - o * n[c];
       }
     }
 #pragma unroll
@@ -213,25 +213,30 @@ __device__ __forceinline__ void off_block(const AsmView& v, int i, int j, double
   }
 }
 
-// One warp per row j of A = K^T; lane t takes the row's blocks t, t+32, ...
+// One warp per slice of A = K^T: lane t owns row j = 32*slice + t and,
+// column by column (k), computes block K_ij with i the k-th entry of conns(j)
+// and stores its transpose in the row's k-th slot.
 template <int DIM>
 __global__ void __launch_bounds__(256) k_assemble(AsmView v) {
   const int lane = threadIdx.x & 31;
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long j = w0; j < v.n; j += nw) {
-    const int64_t q0 = v.cptr[j], q1 = v.cptr[j + 1];
-    for (int64_t q = q0 + lane; q < q1; q += 32) {
-      const int i = v.cidx[q];
+  for (long long sl = w0; sl < v.nslice; sl += nw) {
+    const int j = (int)(sl * kSlice) + lane;
+    const int len = j < v.n ? v.rowlen[j] : 0;
+    const int64_t base = v.sell_ptr[sl] + lane;
+    for (int k = 0; k < len; ++k) {
+      const int64_t slot = base + (int64_t)k * kSlice;
+      const int i = v.scol[slot];
       double K[3][3];
-      if (i == (int)j)
+      if (i == j)
         diag_block<DIM>(v, i, K);
       else
-        off_block<DIM>(v, i, (int)j, K);
+        off_block<DIM>(v, i, j, K);
 #pragma unroll
       for (int r = 0; r < DIM; ++r)
 #pragma unroll
-        for (int s = 0; s < DIM; ++s) v.A[(r * DIM + s) * v.nblk + q] = K[s][r];
+        for (int s = 0; s < DIM; ++s) v.A[(r * DIM + s) * v.nslots + slot] = K[s][r];
     }
   }
 }
@@ -240,7 +245,7 @@ __global__ void __launch_bounds__(256) k_assemble(AsmView v) {
 // (stiffness.h:277: disp_constraint or damage_visual == 1).
 template <int DIM>
 __global__ void k_diag_norm_fixed(int n, const int* __restrict__ diag_slot, const double* __restrict__ A,
-                                  int64_t nblk, const int* __restrict__ mask, const double* __restrict__ dvis,
+                                  int64_t nslots, const int* __restrict__ mask, const double* __restrict__ dvis,
                                   unsigned char* __restrict__ fixed, double* partials, unsigned int* ticket,
                                   double* norms) {
   double v[1] = {0.0};
@@ -250,7 +255,7 @@ __global__ void k_diag_norm_fixed(int n, const int* __restrict__ diag_slot, cons
 #pragma unroll
     for (int r = 0; r < DIM; ++r) {
       if (s >= 0) {
-        const double a = A[(r * DIM + r) * nblk + s];
+        const double a = A[(r * DIM + r) * nslots + s];
         v[0] += a * a;
       }
       fixed[DIM * i + r] = (mask[3 * i + r] == 1 || dead) ? 1 : 0;
@@ -263,24 +268,30 @@ __global__ void k_diag_norm_fixed(int n, const int* __restrict__ diag_slot, cons
 // Zero the rows and columns of fixed DOFs, norm on their diagonal
 // (stiffness.h:273-291).  Entry (r, s) of block (j, i) of A is K(i s, j r).
 template <int DIM>
-__global__ void __launch_bounds__(256) k_apply_bc(int n, const int64_t* __restrict__ cptr, const int* __restrict__ cidx,
+__global__ void __launch_bounds__(256) k_apply_bc(int n, int nslice, const int64_t* __restrict__ sell_ptr,
+                                                  const int* __restrict__ scol, const int* __restrict__ rowlen,
                                                   const unsigned char* __restrict__ fixed, const double* norms,
-                                                  double* __restrict__ A, int64_t nblk) {
+                                                  double* __restrict__ A, int64_t nslots) {
   const int lane = threadIdx.x & 31;
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
   const double nd = norms[2];
-  for (long long j = w0; j < n; j += nw) {
+  for (long long sl = w0; sl < nslice; sl += nw) {
+    const int j = (int)(sl * kSlice) + lane;
+    if (j >= n) continue;
     unsigned char fj[DIM];
 #pragma unroll
     for (int r = 0; r < DIM; ++r) fj[r] = fixed[DIM * j + r];
-    for (int64_t q = cptr[j] + lane; q < cptr[j + 1]; q += 32) {
-      const int i = cidx[q];
+    const int len = rowlen[j];
+    const int64_t base = sell_ptr[sl] + lane;
+    for (int k = 0; k < len; ++k) {
+      const int64_t slot = base + (int64_t)k * kSlice;
+      const int i = scol[slot];
 #pragma unroll
       for (int r = 0; r < DIM; ++r)
 #pragma unroll
         for (int s = 0; s < DIM; ++s)
-          if (fj[r] || fixed[DIM * i + s]) A[(r * DIM + s) * nblk + q] = (i == (int)j && r == s) ? nd : 0.0;
+          if (fj[r] || fixed[DIM * i + s]) A[(r * DIM + s) * nslots + slot] = (i == j && r == s) ? nd : 0.0;
     }
   }
 }
@@ -319,16 +330,38 @@ int build_pattern(lpm_handle* h) {
     h->err = "pattern has 2^31 or more blocks";
     return LPM_ERR_ARG;
   }
+  // sliced layout: each slice is as long as its longest row
+  h->nslice = (n + kSlice - 1) / kSlice;
+  std::vector<int64_t> sp((size_t)h->nslice + 1, 0);
+  for (int sl = 0; sl < h->nslice; ++sl) {
+    int64_t mx = 0;
+    for (int j = sl * kSlice; j < std::min(n, (sl + 1) * kSlice); ++j) mx = std::max(mx, hc[(size_t)j]);
+    sp[(size_t)sl + 1] = sp[(size_t)sl] + mx * kSlice;
+  }
+  h->nslots = sp[(size_t)h->nslice];
+  if (h->nslots >= (int64_t)1 << 31) {
+    cudaFreeAsync(cand, h->stream);
+    h->err = "sliced operator has 2^31 or more slots";
+    return LPM_ERR_ARG;
+  }
   d.cptr = (int64_t*)dev_alloc(h, sizeof(int64_t) * ((size_t)n + 1));
   d.cidx = (int*)dev_alloc(h, sizeof(int) * (size_t)std::max<int64_t>(h->nblk, 1));
   d.diag_slot = (int*)dev_alloc(h, sizeof(int) * (size_t)n);
-  if (!d.cptr || !d.cidx || !d.diag_slot) {
+  d.sell_ptr = (int64_t*)dev_alloc(h, sizeof(int64_t) * ((size_t)h->nslice + 1));
+  d.scol = (int*)dev_alloc(h, sizeof(int) * (size_t)std::max<int64_t>(h->nslots, 1));
+  d.rowlen = (int*)dev_alloc(h, sizeof(int) * (size_t)n);
+  if (!d.cptr || !d.cidx || !d.diag_slot || !d.sell_ptr || !d.scol || !d.rowlen) {
     cudaFreeAsync(cand, h->stream);
     return LPM_ERR_NOMEM;
   }
   LPM_CUDA(h, cudaMemcpyAsync(d.cptr, cp.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, h->stream));
-  k_compact_pattern<<<grid_for(n, T), T, 0, h->stream>>>(n, cand_ptr, cand, d.cptr, d.cidx, d.diag_slot);
+  LPM_CUDA(h, cudaMemcpyAsync(d.sell_ptr, sp.data(), sizeof(int64_t) * (h->nslice + 1), cudaMemcpyHostToDevice,
+                              h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.scol, 0, sizeof(int) * (size_t)std::max<int64_t>(h->nslots, 1), h->stream));
+  k_compact_pattern<<<grid_for(n, T), T, 0, h->stream>>>(n, cand_ptr, cand, d.cptr, d.cidx);
   LPM_LAUNCHED(h, "k_compact_pattern");
+  k_fill_sell<<<grid_for(n, T), T, 0, h->stream>>>(n, d.cptr, d.cidx, d.sell_ptr, d.scol, d.rowlen, d.diag_slot);
+  LPM_LAUNCHED(h, "k_fill_sell");
   LPM_CUDA(h, cudaFreeAsync(cand, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   return LPM_OK;
@@ -337,15 +370,17 @@ int build_pattern(lpm_handle* h) {
 int launch_assemble(lpm_handle* h, int tangent, int bc) {
   Dev& d = h->d;
   const int dim = h->dim;
-  const size_t vals = (size_t)h->nblk * dim * dim;
+  const size_t vals = (size_t)h->nslots * dim * dim;
   if (!d.A64) {
     d.A64 = (double*)dev_alloc(h, sizeof(double) * std::max<size_t>(vals, 1));
     if (!d.A64) return LPM_ERR_NOMEM;
+    // padding slots stay zero for the life of the handle
+    LPM_CUDA(h, cudaMemsetAsync(d.A64, 0, sizeof(double) * std::max<size_t>(vals, 1), h->stream));
   }
-  AsmView v{d.bptr, d.lptr, d.cptr, d.bp2, d.cidx, d.cs, d.cs_sum, d.Kn, d.Tv, d.bdamage, d.A64, h->nblk, h->n,
-            tangent == LPM_TANGENT_SYMMETRIC ? 1 : 0};
+  AsmView v{d.bptr, d.lptr, d.sell_ptr, d.scol, d.rowlen, d.sbond, d.sp2, d.opp, d.cs, d.cs_sum, d.tsum, d.msum,
+            d.Kn, d.Tv, d.bdamage, d.A64, h->nslots, h->n, h->nslice, tangent == LPM_TANGENT_SYMMETRIC ? 1 : 0};
   const int T = 256;
-  const int G = grid_for((long long)h->n * 32, T, 152 * 64);
+  const int G = grid_for((long long)h->nslice * 32, T, 152 * 64);
   if (dim == 3)
     k_assemble<3><<<G, T, 0, h->stream>>>(v);
   else
@@ -354,16 +389,18 @@ int launch_assemble(lpm_handle* h, int tangent, int bc) {
   if (bc == LPM_BC_ELIMINATE) {
     const int GR = grid_for(h->n, kRedThreads, kMaxRedBlocks);
     if (dim == 3)
-      k_diag_norm_fixed<3><<<GR, kRedThreads, 0, h->stream>>>(h->n, d.diag_slot, d.A64, h->nblk, d.mask, d.dvis,
+      k_diag_norm_fixed<3><<<GR, kRedThreads, 0, h->stream>>>(h->n, d.diag_slot, d.A64, h->nslots, d.mask, d.dvis,
                                                               d.fixed, d.red.partials, d.red.ticket + 1, d.norms);
     else
-      k_diag_norm_fixed<2><<<GR, kRedThreads, 0, h->stream>>>(h->n, d.diag_slot, d.A64, h->nblk, d.mask, d.dvis,
+      k_diag_norm_fixed<2><<<GR, kRedThreads, 0, h->stream>>>(h->n, d.diag_slot, d.A64, h->nslots, d.mask, d.dvis,
                                                               d.fixed, d.red.partials, d.red.ticket + 1, d.norms);
     LPM_LAUNCHED(h, "k_diag_norm_fixed");
     if (dim == 3)
-      k_apply_bc<3><<<G, T, 0, h->stream>>>(h->n, d.cptr, d.cidx, d.fixed, d.norms, d.A64, h->nblk);
+      k_apply_bc<3><<<G, T, 0, h->stream>>>(h->n, h->nslice, d.sell_ptr, d.scol, d.rowlen, d.fixed, d.norms, d.A64,
+                                            h->nslots);
     else
-      k_apply_bc<2><<<G, T, 0, h->stream>>>(h->n, d.cptr, d.cidx, d.fixed, d.norms, d.A64, h->nblk);
+      k_apply_bc<2><<<G, T, 0, h->stream>>>(h->n, h->nslice, d.sell_ptr, d.scol, d.rowlen, d.fixed, d.norms, d.A64,
+                                            h->nslots);
     LPM_LAUNCHED(h, "k_apply_bc");
   }
   h->have_K = true;
@@ -375,7 +412,7 @@ int launch_assemble(lpm_handle* h, int tangent, int bc) {
 // FP32 copy of the operator for the mixed-precision solve.
 int convert_A32(lpm_handle* h) {
   Dev& d = h->d;
-  const size_t vals = (size_t)h->nblk * h->dim * h->dim;
+  const size_t vals = (size_t)h->nslots * h->dim * h->dim;
   if (!d.A32) {
     d.A32 = (float*)dev_alloc(h, sizeof(float) * std::max<size_t>(vals, 1));
     if (!d.A32) return LPM_ERR_NOMEM;

@@ -152,3 +152,26 @@ def bond_constants(cell, layer, KnTv):
     Kn = np.where(layer == 0, kn0, kn1).astype(np.float64)
     Tv = np.full(layer.shape, tv, dtype=np.float64)
     return Kn, Tv
+
+
+def nonlocal_neighbors(xyz, cutoff):
+    """Assembly::searchNonlocalNeighbors (assembly.h:117-130): for every
+    particle, the ids (ascending, itself included) closer than `cutoff`
+    (= cutoff_ratio * nonlocal_L), as CSR (ptr, idx)."""
+    from scipy.spatial import cKDTree
+
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    tree = cKDTree(xyz)
+    pairs = tree.query_pairs(cutoff * (1 + 1e-9) + 1e-12, output_type="ndarray")
+    n = len(xyz)
+    i = np.concatenate([pairs[:, 0], pairs[:, 1], np.arange(n)])
+    j = np.concatenate([pairs[:, 1], pairs[:, 0], np.arange(n)])
+    d = xyz[i] - xyz[j]
+    dist = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+    keep = dist < cutoff
+    i, j = i[keep], j[keep]
+    order = np.lexsort((j, i))
+    i, j = i[order], j[order]
+    ptr = np.zeros(n + 1, np.int64)
+    np.add.at(ptr, i + 1, 1)
+    return np.cumsum(ptr), j.astype(np.int32)

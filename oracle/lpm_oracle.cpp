@@ -11,6 +11,7 @@
 #include "lpm_oracle.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -47,10 +48,17 @@ struct lo_sys {
   std::vector<long> cptr, tpos;
   std::vector<int> cidx;
   std::vector<double> K;
-  // law
+  // law: 0 elastic, 1 elastic damage, 2 J2 plasticity, 3 HCF fatigue
   int law = 0;
-  std::vector<double> law_params;
+  int np = 0;                // parameters per particle
+  std::vector<double> pp;    // [n * np] per-particle law parameters
   std::vector<double> crit;  // per-particle critical bond strain (elastic law)
+  std::vector<int> ptype;    // particle type (undamaged type skips damage)
+  int undamaged = -1;
+  // nonlocal neighbours (Assembly::searchNonlocalNeighbors) and length scale
+  std::vector<long> nl_ptr;
+  std::vector<int> nl_idx;
+  std::vector<double> nonlocal_L, ddot_nl;
   // log
   std::vector<double> log;
 };
@@ -92,12 +100,16 @@ void update_geometry(lo_sys* s) {
   }
 }
 
-// particle_elastic.h:38-50 (law 0).
+// particle_elastic.h:38-50 (law 0); the damage laws first raise the bond
+// damage to the larger particle damage (particle_elastic_damage.h:74-87,
+// particle_j2plasticity.h:63-76, particle_fatigue_hcf.h:65-80).
 void update_bond_force(lo_sys* s) {
+  const bool dmg = s->law != 0;
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < s->n; ++i) {
     for (long b = s->bptr[i]; b < s->bptr[i + 1]; ++b) {
       double f = 2. * s->Kn[b] * s->dLe[b] + 2. * s->Tv[b] * s->dle_tot[NL * (size_t)i + s->blayer[b]];
+      if (dmg) s->bdamage[b] = std::max(s->bdamage[b], std::max(s->damage[i], s->damage[s->bp2[b]]));
       f *= (1.0 - s->bdamage[b]);
       s->bforce[b] = f;
     }
@@ -298,6 +310,138 @@ double dot(const std::vector<double>& a, const std::vector<double>& b) {
   return s;
 }
 
+// strain energy density, particle_elastic_damage.h:89-104 (and the total
+// of particle_fatigue_hcf.h:82-125, which returns the same sum)
+double strain_energy(const lo_sys* s, int i) {
+  const double Vm = s->particle_volume * s->nbonds[i] / s->nneighbors;
+  double e = 0;
+  for (int l = 0; l < NL; ++l) {
+    for (long b = s->bptr[i]; b < s->bptr[i + 1]; ++b)
+      if (s->blayer[b] == l) e += 0.5 * (s->Kn[b] * s->dLe[b] * s->dLe[b]) / Vm;
+    e += 0.5 * s->tdle_tot[NL * (size_t)i + l] * s->dle_tot[NL * (size_t)i + l] / Vm;
+  }
+  return e;
+}
+
+// Assembly::updateStateVar -> Particle*::updateParticleStateVariables
+void update_state(lo_sys* s) {
+  const int ns = s->nstate;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < s->n; ++i) {
+    const double* P = &s->pp[(size_t)i * s->np];
+    double* sv = &s->state[(size_t)i * ns];
+    const double* svl = &s->state_last[(size_t)i * ns];
+    if (s->law == 1) {  // particle_elastic_damage.h:150-161
+      const double k0 = P[0], k1 = P[1];
+      sv[0] = strain_energy(s, i);
+      const double delta = sv[0] - svl[0];
+      const double f = sv[0] - k1 * s->damage[i] - k0;
+      s->ddot_local[i] = (f > 0 && delta > 0) ? (1 / k1) * delta : 0;
+    } else if (s->law == 2) {  // particle_j2plasticity.h:78-140
+      const double E = P[0], mu = P[1], sigmay = P[2], xi = P[3], H = P[4], A = P[5];
+      double st[6];
+      for (int j = 0; j < 6; ++j) st[j] = s->stress[6 * (size_t)i + j];
+      const double sigma_m = 1.0 / 3.0 * (st[0] + st[1] + st[2]);
+      for (int j = 0; j < 3; ++j) st[j] -= sigma_m;
+      for (int j = 0; j < 6; ++j) st[j] -= sv[j + 1];
+      double seq = 0;
+      for (int j = 0; j < 6; ++j) seq += (j < 3 ? 1.0 : 2.0) * st[j] * st[j];
+      seq = std::sqrt(3.0 / 2.0 * seq);
+      const double yf = seq - (sigmay + (1.0 - xi) * H * sv[0]);
+      const double G = E / 2 / (1 + mu);
+      double dl = 0.0;
+      if (yf > 0.0) dl = yf / (3 * G + H);
+      sv[0] += dl;
+      double dp[6] = {0, 0, 0, 0, 0, 0};
+      for (int j = 0; j < 6; ++j)
+        if (std::fabs(seq) > EPS_) {
+          dp[j] = dl * 1.5 * st[j] / seq;
+          sv[j + 1] += 2. / 3. * xi * H * dp[j];
+        }
+      for (int l = 0; l < NL; ++l)
+        for (long b = s->bptr[i]; b < s->bptr[i + 1]; ++b) {
+          if (s->blayer[b] != l) continue;
+          const double* c = &s->cs[3 * b];
+          const double ddLp = s->dis[b] * (dp[0] * c[0] * c[0] + dp[1] * c[1] * c[1] + dp[2] * c[2] * c[2] +
+                                           2 * dp[3] * c[1] * c[2] + 2 * dp[4] * c[0] * c[2] + 2 * dp[5] * c[0] * c[1]);
+          s->dLp[b] += ddLp;
+        }
+      const double tri = seq > EPS_ ? sigma_m / seq : 0.0;
+      s->ddot_local[i] = dl * (1.0 + A * tri);
+    } else if (s->law == 3) {  // particle_fatigue_hcf.h:127-145
+      const double A = P[0], B = P[1], d = P[2];
+      const double u = strain_energy(s, i);
+      sv[1] = std::min(u, sv[1]);
+      sv[2] = std::max(u, sv[2]);
+      sv[0] = std::max(sv[2], sv[0]);
+      s->ddot_local[i] = (sv[2] - sv[1] > 0) ? A * std::pow(sv[0], B) * std::pow(sv[2] - sv[1], d) : 0;
+    }
+  }
+}
+
+// func_phi, lpm.h:45-49
+inline double phi(double x, double L) { return std::pow(1 / (1 + std::pow(x / L, 8.0)), 2.0); }
+
+// nonlocal damage rate, solver_static.h:34-54 / solver_fatigue.h:79-116
+void nonlocal_rate(lo_sys* s) {
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < s->n; ++i) {
+    if (s->ptype[i] == s->undamaged) continue;
+    double A = 0, D = 0;
+    const double* xi = &s->x[3 * (size_t)i];
+    for (long q = s->nl_ptr[i]; q < s->nl_ptr[i + 1]; ++q) {
+      const int j = s->nl_idx[q];
+      if (s->ptype[j] == s->undamaged) continue;
+      const double* xj = &s->x[3 * (size_t)j];
+      const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+      const double dis = std::sqrt(dx * dx + dy * dy + dz * dz);
+      const double Vm = s->particle_volume * s->nbonds[j] / s->nneighbors;
+      D += s->ddot_local[j] * phi(dis, s->nonlocal_L[i]) * Vm;
+      A += phi(dis, s->nonlocal_L[i]) * Vm;
+    }
+    s->ddot_nl[i] = D / A;
+  }
+}
+
+// SolverStatic::updateStaticDamage (solver_static.h:31-62)
+bool static_damage(lo_sys* s) {
+  nonlocal_rate(s);
+  bool any = false;
+  for (int i = 0; i < s->n; ++i) {
+    if (s->ptype[i] == s->undamaged) continue;
+    if (s->law == 0) {  // particle_elastic.h:52-68
+      for (long b = s->bptr[i]; b < s->bptr[i + 1]; ++b)
+        if (s->bstrain[b] >= s->crit[i] && std::abs(s->bdamage[b] - 1.0) > EPS_) {
+          s->bdamage[b] = 1;
+          any = true;
+        }
+    } else if (s->law == 1 || s->law == 2) {  // particle_elastic_damage.h:163-173, particle_j2plasticity.h:142-152
+      const double thr = s->pp[(size_t)i * s->np + (s->law == 1 ? 2 : 6)];
+      s->damage[i] += s->ddot_nl[i];
+      if (s->damage[i] >= thr) s->damage[i] = 1;
+      any = (std::abs(s->damage[i] - s->damage_last[i]) > 1e-3) || any;
+    }
+  }
+  return any;
+}
+
+// SolverFatigue::updateFatigueDamage (solver_fatigue.h:75-126) with
+// ParticleFatigueHCF::updateParticleFatigueDamage (particle_fatigue_hcf.h:147-160)
+bool fatigue_damage(lo_sys* s, double dt) {
+  nonlocal_rate(s);
+  bool any = false;
+  for (int i = 0; i < s->n; ++i) {
+    if (s->ptype[i] == s->undamaged || s->law != 3) continue;
+    const double thr = s->pp[(size_t)i * s->np + 3];
+    s->damage[i] += s->ddot_nl[i] * dt;
+    if (s->damage[i] >= thr) s->damage[i] = 1;
+    s->state[(size_t)i * s->nstate + 1] = INT_MAX;
+    s->state[(size_t)i * s->nstate + 2] = 0;
+    any = (std::abs(s->damage[i] - s->damage_last[i]) > 1e-3) || any;
+  }
+  return any;
+}
+
 }  // namespace
 
 extern "C" {
@@ -346,6 +490,10 @@ lo_sys* lo_create(int dim, int n, long nb, const double* xyz, const int* p1, con
   s->state.assign(N * s->nstate, 0);
   s->state_last = s->state;
   s->crit.assign(N, 1.0);
+  s->ptype.assign(N, 0);
+  s->nonlocal_L.assign(N, 0.0);
+  s->ddot_nl.assign(N, 0.0);
+  s->nl_ptr.assign(N + 1, 0);
   // bond CSR: stable counting sort by (p1, layer)
   std::vector<long> cnt(N * NL + 1, 0);
   for (long b = 0; b < nb; ++b) cnt[(size_t)p1[b] * NL + layer[b] + 1]++;
@@ -499,11 +647,42 @@ void lo_set_bond(lo_sys* s, int field, const double* in) {
 }
 void lo_set_mask(lo_sys* s, const int* mask) { std::copy(mask, mask + 3 * (size_t)s->n, s->mask.begin()); }
 
-void lo_set_law(lo_sys* s, int law, const double* params, int nparams) {
+void lo_set_law(lo_sys* s, int law, const double* params, int nparams, int per_particle) {
   s->law = law;
-  s->law_params.assign(params, params + nparams);
-  if (law == 0 && nparams >= 1) std::fill(s->crit.begin(), s->crit.end(), params[0]);
+  s->np = nparams;
+  const size_t N = (size_t)s->n;
+  s->pp.assign(N * (size_t)nparams, 0.0);
+  for (size_t i = 0; i < N; ++i)
+    for (int k = 0; k < nparams; ++k) s->pp[i * nparams + k] = per_particle ? params[i * nparams + k] : params[k];
+  if (law == 0 && nparams >= 1)
+    for (size_t i = 0; i < N; ++i) s->crit[i] = s->pp[i * nparams];
+  // state variables (constructors of the particle classes)
+  s->nstate = law == 2 ? 7 : (law == 3 ? 3 : 1);
+  s->state.assign(N * s->nstate, 0.0);
+  if (law == 3)
+    for (size_t i = 0; i < N; ++i) s->state[i * 3 + 1] = INT_MAX;
+  s->state_last = s->state;
 }
+
+void lo_set_types(lo_sys* s, const int* types, int undamaged) {
+  std::copy(types, types + s->n, s->ptype.begin());
+  s->undamaged = undamaged;
+}
+
+void lo_set_nonlocal(lo_sys* s, const long* ptr, const int* idx, const double* L) {
+  s->nl_ptr.assign(ptr, ptr + s->n + 1);
+  s->nl_idx.assign(idx, idx + ptr[s->n]);
+  s->nonlocal_L.assign(L, L + s->n);
+}
+
+void lo_update_state(lo_sys* s) { update_state(s); }
+int lo_static_damage(lo_sys* s) { return static_damage(s) ? 1 : 0; }
+int lo_fatigue_damage(lo_sys* s, double dt) { return fatigue_damage(s, dt) ? 1 : 0; }
+void lo_get_ddot(const lo_sys* s, double* local, double* nonlocal) {
+  if (local) std::copy(s->ddot_local.begin(), s->ddot_local.end(), local);
+  if (nonlocal) std::copy(s->ddot_nl.begin(), s->ddot_nl.end(), nonlocal);
+}
+int lo_num_state(const lo_sys* s) { return s->nstate; }
 
 void lo_update_geometry_force(lo_sys* s) {
   update_geometry(s);
@@ -646,18 +825,6 @@ void lo_reset_state(lo_sys* s, int reset_xyz) {
   s->dLp = s->dLp_last;
 }
 
-// Brittle bond breaking of the elastic law (particle_elastic.h:52-68).
-static bool elastic_static_damage(lo_sys* s) {
-  bool any = false;
-  for (int i = 0; i < s->n; ++i)
-    for (long b = s->bptr[i]; b < s->bptr[i + 1]; ++b)
-      if (s->bstrain[b] >= s->crit[i] && std::abs(s->bdamage[b] - 1.0) > EPS_) {
-        s->bdamage[b] = 1;
-        any = true;
-      }
-  return any;
-}
-
 int lo_load_step(lo_sys* s, const int* apply, const double* d, const double* f, int sym, int bc_elim, int max_iter,
                  double tol, double cg_tol, long cg_maxit, int max_cuts) {
   std::vector<double> dd(d, d + 3 * (size_t)s->n), ff(f ? f : d, (f ? f : d) + 3 * (size_t)s->n);
@@ -682,7 +849,8 @@ int lo_load_step(lo_sys* s, const int* apply, const double* d, const double* f, 
       nn = lo_newton(s, max_iter, tol, cg_tol, cg_maxit);
       if (nn >= max_iter) break;
       damaged = false;
-      if (!bc_elim && s->law == 0) damaged = elastic_static_damage(s);
+      update_state(s);  // Assembly::updateStateVar
+      if (!bc_elim) damaged = static_damage(s);
       lo_store_state(s);
       if (damaged) lo_update_geometry_force(s);
     } while (damaged);

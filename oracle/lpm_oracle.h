@@ -64,9 +64,23 @@ void lo_get_bond(const lo_sys* s, int field, double* out);
 void lo_set_bond(lo_sys* s, int field, const double* in);
 void lo_set_mask(lo_sys* s, const int* mask); /* N*3 disp_constraint */
 
-/* Material law (particle type).  0 elastic (critical bond strain in p[0]);
- * further laws are added with their own parameter layouts. */
-void lo_set_law(lo_sys* s, int law, const double* params, int nparams);
+/* Material law of all particles and its parameters (uniform, or N*nparams
+ * when per_particle is set):
+ *   0 ParticleElastic        {critical_bstrain}
+ *   1 ParticleElasticDamage  {k0, k1, damage_threshold}
+ *   2 ParticleJ2Plasticity   {E, mu, sigmay, xi, H, A, damage_threshold}
+ *   3 ParticleFatigueHCF     {A, B, d, damage_threshold}
+ * Resets the state variables to the constructors' values. */
+void lo_set_law(lo_sys* s, int law, const double* params, int nparams, int per_particle);
+void lo_set_types(lo_sys* s, const int* types, int undamaged_type);
+/* Assembly::searchNonlocalNeighbors result (CSR, ascending ids) and each
+ * particle's nonlocal length scale. */
+void lo_set_nonlocal(lo_sys* s, const long* ptr, const int* idx, const double* L);
+void lo_update_state(lo_sys* s);               /* Assembly::updateStateVar */
+int lo_static_damage(lo_sys* s);               /* SolverStatic::updateStaticDamage */
+int lo_fatigue_damage(lo_sys* s, double dNdt); /* SolverFatigue::updateFatigueDamage */
+void lo_get_ddot(const lo_sys* s, double* local, double* nonlocal);
+int lo_num_state(const lo_sys* s);
 
 /* Assembly::updateGeometry + updateForceState (assembly.h:132-138,178-191) */
 void lo_update_geometry_force(lo_sys* s);

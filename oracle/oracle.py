@@ -20,7 +20,7 @@ XYZ, XYZ0, PIN, PEX, STRESS, DVIS, DLE_TOT, TDLE_TOT, CS_SUM, DAMAGE, XYZ_LAST, 
 BFORCE, BDAMAGE, DLE, DIS, BSTRAIN, CS, KN, TV, DIS0, DLP = range(10)
 
 _PWIDTH = {XYZ: 3, XYZ0: 3, PIN: 3, PEX: 3, STRESS: 6, DVIS: 1, DLE_TOT: 2, TDLE_TOT: 2, CS_SUM: 6,
-           DAMAGE: 1, XYZ_LAST: 3, STATE: 1, DDOT_LOCAL: 1}
+           DAMAGE: 1, XYZ_LAST: 3, DDOT_LOCAL: 1}
 _BWIDTH = {BFORCE: 1, BDAMAGE: 1, DLE: 1, DIS: 1, BSTRAIN: 1, CS: 3, KN: 1, TV: 1, DIS0: 1, DLP: 1}
 
 
@@ -54,7 +54,17 @@ def lib():
         for f in ("lo_get_particle", "lo_set_particle", "lo_get_bond", "lo_set_bond"):
             getattr(L, f).argtypes = [P, ctypes.c_int, dp]
         L.lo_set_mask.argtypes = [P, ip]
-        L.lo_set_law.argtypes = [P, ctypes.c_int, dp, ctypes.c_int]
+        L.lo_set_law.argtypes = [P, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int]
+        L.lo_set_types.argtypes = [P, ip, ctypes.c_int]
+        L.lo_set_nonlocal.argtypes = [P, lp, ip, dp]
+        L.lo_update_state.argtypes = [P]
+        L.lo_static_damage.argtypes = [P]
+        L.lo_static_damage.restype = ctypes.c_int
+        L.lo_fatigue_damage.argtypes = [P, ctypes.c_double]
+        L.lo_fatigue_damage.restype = ctypes.c_int
+        L.lo_get_ddot.argtypes = [P, dp, dp]
+        L.lo_num_state.argtypes = [P]
+        L.lo_num_state.restype = ctypes.c_int
         L.lo_update_geometry_force.argtypes = [P]
         L.lo_residual.argtypes = [P, dp, dp, dp]
         L.lo_assemble.argtypes = [P, ctypes.c_int, ctypes.c_int]
@@ -153,8 +163,41 @@ class OracleSystem:
         lib().lo_set_mask(self.h, _i(m))
 
     def set_law(self, law, params):
+        """params: one row for all particles, or an (N, P) array per particle."""
         p = np.ascontiguousarray(params, dtype=np.float64)
-        lib().lo_set_law(self.h, int(law), _d(p), len(p))
+        per = p.ndim == 2
+        lib().lo_set_law(self.h, int(law), _d(p), p.shape[-1], int(per))
+
+    def set_types(self, types, undamaged):
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        lib().lo_set_types(self.h, _i(t), int(undamaged))
+
+    def set_nonlocal(self, ptr, idx, L):
+        ptr = np.ascontiguousarray(ptr, dtype=np.int64)
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        L = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (self.n,)))
+        lib().lo_set_nonlocal(self.h, _l(ptr), _i(idx), _d(L))
+
+    def update_state(self):
+        lib().lo_update_state(self.h)
+
+    def static_damage(self):
+        return bool(lib().lo_static_damage(self.h))
+
+    def fatigue_damage(self, dNdt):
+        return bool(lib().lo_fatigue_damage(self.h, float(dNdt)))
+
+    def ddot(self):
+        a = np.zeros(self.n)
+        b = np.zeros(self.n)
+        lib().lo_get_ddot(self.h, _d(a), _d(b))
+        return a, b
+
+    def state(self):
+        ns = lib().lo_num_state(self.h)
+        out = np.zeros(self.n * ns)
+        lib().lo_get_particle(self.h, STATE, _d(out))
+        return out.reshape(self.n, ns)
 
     def update(self):
         lib().lo_update_geometry_force(self.h)

@@ -366,6 +366,125 @@ int case_steps(Out& o, const std::string& lattice) {
   return 0;
 }
 
+// "laws": one update of each material law at a deformed, perturbed state.
+//   law=damage  ParticleElasticDamage  (particle_elastic_damage.h)
+//   law=j2      ParticleJ2Plasticity   (particle_j2plasticity.h)
+//   law=hcf     ParticleFatigueHCF     (particle_fatigue_hcf.h)
+// Sequence: updateGeometry/updateForceState, updateStateVar, the nonlocal
+// damage update of SolverStatic (or SolverFatigue for hcf), and a second
+// updateForceState that carries particle damage into the bonds.
+void dump_laws_state(Out& o, const std::string& pfx, Assembly<NL>& ass) {
+  std::vector<double> sv, ddl, ddn, dmg, dlp;
+  for (P* p : ass.pt_sys) {
+    for (double v : p->state_var) sv.push_back(v);
+    ddl.push_back(p->Ddot_local);
+    ddn.push_back(p->Ddot_nonlocal);
+    dmg.push_back(p->damage);
+    for (int l = 0; l < NL; ++l)
+      for (Bond<NL>* b : p->bond_layers[l]) dlp.push_back(b->dLp);
+  }
+  o.f64(pfx + "state_var", sv);
+  o.f64(pfx + "ddot_local", ddl);
+  o.f64(pfx + "ddot_nonlocal", ddn);
+  o.f64(pfx + "damage", dmg);
+  o.f64(pfx + "dLp", dlp);
+}
+
+int case_laws(Out& o, const std::string& lattice) {
+  double a = opt("a", 0.5);
+  std::vector<std::array<double, NDIM>> xyz;
+  LatticeType lt;
+  if (lattice == "hex") {
+    lt = LatticeType::Hexagon2D;
+    xyz = hex_points((int)opt("ncol", 11), (int)opt("nrow", 11), a);
+  } else {
+    lt = LatticeType::SimpleCubic3D;
+    int n = (int)opt("n", 5);
+    xyz = sc_points(n, n, n, a);
+  }
+  UnitCell cell(lt, a / 2.0);
+  std::array<double, 2 * NDIM> box{0, 1, 0, 1, 0, 1};
+  std::string law = opts("law", "damage");
+  ParticleType pt = law == "damage" ? ParticleType::ElasticDamage
+                                    : (law == "j2" ? ParticleType::J2Plasticity : ParticleType::FatigueHCF);
+  Assembly<NL> ass(xyz, box, cell, pt);
+  bool ps = cell.dim == 2;
+  double nl = opt("nonlocal_L", 0.6);
+  int undamaged = (int)opt("undamaged", 4);
+  int k = 0;
+  for (P* p : ass.pt_sys) {
+    p->type = (k % 9 == 4) ? undamaged : 0;  // a sprinkling of undamaged particles
+    ++k;
+    if (law == "damage")
+      dynamic_cast<ParticleElasticDamage<NL>*>(p)->setParticleProperty(nl, ps, opt("E", 3.2e3), opt("nu", 0.28),
+                                                                       opt("k0", 0.1936), opt("k1", 1.0), 10.0,
+                                                                       opt("dthr", 0.99));
+    else if (law == "j2")
+      dynamic_cast<ParticleJ2Plasticity<NL>*>(p)->setParticleProperty(nl, ps, opt("E", 110e3), opt("nu", 0.34),
+                                                                      opt("sigmay", 900.0), opt("xi", 0.3),
+                                                                      opt("H", 1e3), opt("A", 0.5), 1.0);
+    else
+      dynamic_cast<ParticleFatigueHCF<NL>*>(p)->setParticleProperty(nl, ps, opt("E", 71.7e3), opt("nu", 0.306),
+                                                                    opt("fA", 1.94e-4), opt("fB", 0.581),
+                                                                    opt("fd", 1.079), opt("dthr", 1.0), 1.108);
+  }
+  ass.searchNonlocalNeighbors(opt("cutoff_ratio", 1.5));
+  dump_topology(o, ass);
+  std::vector<long long> types, nlp{0}, nli;
+  for (P* p : ass.pt_sys) {
+    types.push_back(p->type);
+    for (P* q : p->neighbors_nonlocal) nli.push_back(q->id);
+    nlp.push_back((long long)nli.size());
+  }
+  o.i64("types", types);
+  o.i64("nl_ptr", nlp);
+  o.i64("nl_idx", nli);
+  // deformed state: uniform stretch along the loading axis plus noise
+  int ax = cell.dim == 2 ? 1 : 2;
+  auto deform = [&](double stretch, unsigned seed) {
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    double amp = opt("amp", 0.01) * a;
+    for (P* p : ass.pt_sys) {
+      std::array<double, NDIM> x = p->xyz_initial;
+      x[ax] *= (1.0 + stretch);
+      x[0] += amp * U(rng);
+      x[1] += amp * U(rng);
+      if (cell.dim == 3) x[2] += amp * U(rng);
+      p->moveTo(x);
+    }
+  };
+  SolverStatic<NL> ss(undamaged, ass, StiffnessMode::Analytical, SolverMode::CG, "/dev/null", 30, 1e-5);
+  SolverFatigue<NL> sf(undamaged, ass, StiffnessMode::Analytical, SolverMode::CG, TimeMapMode::Linear, 1.0,
+                       "/dev/null", 30, 1e-5);
+  double s1 = opt("stretch", 0.015);
+  deform(s1, 11);
+  ass.updateGeometry();
+  ass.updateForceState();
+  dump_state(o, "a_", ass);
+  ass.updateStateVar();
+  dump_laws_state(o, "a_", ass);
+  if (law == "hcf") {
+    // a second, smaller deformation inside the same cycle, then the cycle's damage
+    deform(0.3 * s1, 12);
+    ass.updateGeometry();
+    ass.updateForceState();
+    dump_state(o, "b_", ass);
+    ass.updateStateVar();
+    dump_laws_state(o, "b_", ass);
+    bool any = sf.updateFatigueDamage(opt("dNdt", 1000));
+    o.scalar("any_damaged", any ? 1.0 : 0.0);
+  } else {
+    bool any = ss.updateStaticDamage();
+    o.scalar("any_damaged", any ? 1.0 : 0.0);
+  }
+  dump_laws_state(o, "c_", ass);
+  ass.updateGeometry();
+  ass.updateForceState();
+  dump_state(o, "c_", ass);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -384,6 +503,8 @@ int main(int argc, char** argv) {
   if (c == "kernels-sc") return case_kernels(o, "sc");
   if (c == "steps-hex") return case_steps(o, "hex");
   if (c == "steps-sc") return case_steps(o, "sc");
+  if (c == "laws-hex") return case_laws(o, "hex");
+  if (c == "laws-sc") return case_laws(o, "sc");
   std::fprintf(stderr, "unknown case %s\n", c.c_str());
   return 2;
 }

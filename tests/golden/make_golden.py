@@ -30,6 +30,15 @@ CASES = {
                                         "solver=fatigue", "all_xyz=1"], "1e-10"),
     "steps_sc_fatigue": ("steps-sc", ["n=5", "a=0.2", "mapping=row", "steps=2", "du=0.002", "solver=fatigue",
                                       "all_xyz=1"], "1e-10"),
+    # one update of each material law (state variables, nonlocal damage rate,
+    # damage, plastic bond stretch) at a stretched, perturbed state
+    "law_damage_hex": ("laws-hex", ["ncol=11", "nrow=11", "a=0.5", "law=damage", "nonlocal_L=0.6", "stretch=0.015"],
+                       "1e-10"),
+    "law_j2_sc": ("laws-sc", ["n=5", "a=0.2", "law=j2", "nonlocal_L=0.25", "stretch=0.02", "amp=0.002"], "1e-10"),
+    "law_j2_hex": ("laws-hex", ["ncol=9", "nrow=9", "a=0.5", "law=j2", "nonlocal_L=0.6", "stretch=0.02",
+                                "amp=0.002"], "1e-10"),
+    "law_hcf_hex": ("laws-hex", ["ncol=11", "nrow=11", "a=0.5", "law=hcf", "nonlocal_L=0.6", "stretch=0.004",
+                                 "dNdt=1000"], "1e-10"),
     # configuration 1: 41 x 41 hexagonal plate, 1,661 particles, 10 steps
     "config1_hex": ("steps-hex", ["ncol=41", "nrow=41", "a=0.5", "mapping=row", "steps=10", "du=0.001",
                                   "solver=fatigue"], "1e-10"),

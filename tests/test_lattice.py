@@ -67,3 +67,11 @@ def test_interior_conns_counts():
         o = make_oracle(dim, xyz, p1, p2, layer, Kn, Tv, cell)
         counts = np.diff(o.topology()["cptr"])
         assert counts.max() == nn == cell.nneighbors_AFEM + 1
+
+
+def test_nonlocal_neighbours_match_reference():
+    d = golden("law_damage_hex")
+    cell = lat.UnitCell(lat.HEXAGON2D, 0.25)
+    xyz = d["xyz0"].reshape(-1, 3)
+    ptr, idx = lat.nonlocal_neighbors(xyz, 1.5 * 0.6)
+    assert np.array_equal(ptr, d["nl_ptr"]) and np.array_equal(idx, d["nl_idx"])
