@@ -13,6 +13,8 @@ namespace lpm {
 
 static thread_local std::string g_err;
 
+void set_global_error(const std::string& msg) { g_err = msg; }
+
 int cuda_fail(lpm_handle* h, cudaError_t e, const char* what) {
   std::string m = std::string(what) + ": " + cudaGetErrorString(e);
   if (h) h->err = m;

@@ -155,6 +155,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
 
 // helpers (lpm_capi.cu)
 int cuda_fail(lpm_handle* h, cudaError_t e, const char* what);
+void set_global_error(const std::string& msg);  // text of lpm_last_error(NULL)
 void* dev_alloc(lpm_handle* h, size_t bytes);
 inline int grid_for(long long work, int threads, int cap = 1 << 20) {
   long long g = (work + threads - 1) / threads;
