@@ -245,13 +245,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel_key):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "cg_spmv_sc101.md")
+def profiled_traffic(kernel_key, nblk):
+    """DRAM bytes per launch of the CG sparse product: the bytes per block
+    measured by ncu on the 61^3 lattice (committed summary) times this
+    workload's block count (traffic grows with the blocks processed)."""
+    path = os.path.join(ROOT, "profiles", "cg_spmv_sc61.md")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch") and kernel_key in line:
-                return float(line.split("=")[1].split()[0])
+            if line.startswith("traffic_bytes_per_block") and line.split()[1] == kernel_key:
+                return float(line.split("=")[1].split()[0]) * nblk
     except OSError:
         pass
     return None
@@ -375,7 +377,7 @@ def run_gb300(args):
     byts = spmv_bytes(nblk, n, 3, 4)
     peak, peak_kind = measured_peaks()
     achieved = byts / (avg_ms * 1e-3) / 1e9
-    traffic = profiled_traffic("float")
+    traffic = profiled_traffic("float", nblk)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_mixed * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 CG + f64 refinement/forces", "data": "synthetic",
