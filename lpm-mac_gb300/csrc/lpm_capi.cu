@@ -484,7 +484,7 @@ int lpm_get_K(const lpm_handle* h, double* vals) {
         hh->err = "pattern is not structurally symmetric";
         return LPM_ERR_STATE;
       }
-      const size_t slot = (size_t)(sp[(size_t)j / lpm::kSlice] + (f - b) * lpm::kSlice + j % lpm::kSlice);
+      const size_t slot = (size_t)lpm::sell_slot(lpm::sell_row_base(sp.data(), j), (int)(f - b));
       for (int r = 0; r < dim; ++r)
         for (int s = 0; s < dim; ++s) vals[(size_t)q * e2 + r * dim + s] = A[(size_t)(s * dim + r) * ns + slot];
     }

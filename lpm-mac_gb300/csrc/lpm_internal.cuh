@@ -8,14 +8,16 @@
 //              order, as Particle::bond_layers holds them; SoA per field
 //   pattern    conns CSR (cptr, cidx), ascending ids, self included
 //   operator   A = K^T over the same pattern: block (j, i) of A is K_ij
-//              transposed.  Sliced block-ELL storage: rows are grouped in
-//              slices of 32 consecutive rows; block k of row j sits in slot
-//              sell_ptr[j/32] + 32*k + j%32, so the 32 rows of a slice read
-//              their k-th blocks from 32 consecutive slots.  Values are
-//              stored one array per block element ("element-major"):
-//              A[e * nslots + slot], e = r*dim + s.  A thread owns a row;
-//              rows shorter than their slice leave padding slots (zeros,
-//              never read by the row loops)
+//              transposed.  Sliced block-ELL storage in groups of four: rows
+//              are grouped in slices of 32 consecutive rows, each slice is
+//              as long as its longest row rounded up to 4, and block k of
+//              row j sits in slot
+//                sell_ptr[j/32] + 128*(k/4) + 4*(j%32) + k%4,
+//              so a thread reads four consecutive blocks of its row with one
+//              vector load and the 32 rows of a slice read 512 contiguous
+//              bytes.  Values are stored one array per block element
+//              ("element-major"): A[e * nslots + slot], e = r*dim + s.
+//              Padding slots hold zeros and point at the row itself
 #pragma once
 
 #include <cuda_runtime.h>
@@ -45,6 +47,7 @@ struct CgScalars {
   int ru;             // mixed solve: a reliable update is pending
   double rmax;        // mixed solve: largest |r| since the last reliable update
   long long ru_count; // mixed solve: reliable updates taken
+  double zcoef;       // mixed solve: p = zcoef z + beta p (1 except right after an update)
 };
 
 // Deterministic grid reductions: each block writes a partial, the last block
@@ -55,6 +58,15 @@ struct RedBuf {
 };
 constexpr int kMaxRedBlocks = 2048;
 constexpr int kSlice = 32;  // rows per slice of the sliced operator
+constexpr int kVec = 4;     // consecutive blocks of a row stored together
+
+// first slot of row j (its blocks k sit at row_base + 128*(k/4) + k%4)
+__host__ __device__ __forceinline__ int64_t sell_row_base(const int64_t* sell_ptr, int j) {
+  return sell_ptr[j / kSlice] + (int64_t)(j % kSlice) * kVec;
+}
+__host__ __device__ __forceinline__ int64_t sell_slot(int64_t row_base, int k) {
+  return row_base + (int64_t)(k / kVec) * (kSlice * kVec) + (k % kVec);
+}
 
 struct Group {
   int* ids;
@@ -83,6 +95,7 @@ struct Dev {
   // operator values
   double* A64;
   float* A32;
+  float* S32;  // [n * dim * dim] block row sums of A64, rounded (difference-form FP32 product)
   // solver vectors (n_dof each)
   double *rhs, *disp, *x64, *r64, *p64, *q64, *invd64;
   float *b32, *x32, *r32, *p32, *q32, *invd32;

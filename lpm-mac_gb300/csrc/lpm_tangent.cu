@@ -90,13 +90,15 @@ __global__ void k_fill_sell(int n, const int64_t* __restrict__ cptr, const int* 
   if (j >= n) return;
   const int64_t q0 = cptr[j];
   const int len = (int)(cptr[j + 1] - q0);
-  const int64_t base = sell_ptr[j / kSlice] + (j % kSlice);
+  const int64_t base = sell_row_base(sell_ptr, j);
   int ds = -1;
   for (int k = 0; k < len; ++k) {
     const int c = cidx[q0 + k];
-    scol[base + (int64_t)k * kSlice] = c;
-    if (c == j) ds = (int)(base + (int64_t)k * kSlice);
+    scol[sell_slot(base, k)] = c;
+    if (c == j) ds = (int)sell_slot(base, k);
   }
+  // padding of the row's last group of four points at the row itself
+  for (int k = len; k % kVec != 0; ++k) scol[sell_slot(base, k)] = j;
   rowlen[j] = len;
   diag_slot[j] = ds;
 }
@@ -224,9 +226,9 @@ __global__ void __launch_bounds__(256) k_assemble(AsmView v) {
   for (long long sl = w0; sl < v.nslice; sl += nw) {
     const int j = (int)(sl * kSlice) + lane;
     const int len = j < v.n ? v.rowlen[j] : 0;
-    const int64_t base = v.sell_ptr[sl] + lane;
+    const int64_t base = j < v.n ? sell_row_base(v.sell_ptr, j) : 0;
     for (int k = 0; k < len; ++k) {
-      const int64_t slot = base + (int64_t)k * kSlice;
+      const int64_t slot = sell_slot(base, k);
       const int i = v.scol[slot];
       double K[3][3];
       if (i == j)
@@ -283,9 +285,9 @@ __global__ void __launch_bounds__(256) k_apply_bc(int n, int nslice, const int64
 #pragma unroll
     for (int r = 0; r < DIM; ++r) fj[r] = fixed[DIM * j + r];
     const int len = rowlen[j];
-    const int64_t base = sell_ptr[sl] + lane;
+    const int64_t base = sell_row_base(sell_ptr, j);
     for (int k = 0; k < len; ++k) {
-      const int64_t slot = base + (int64_t)k * kSlice;
+      const int64_t slot = sell_slot(base, k);
       const int i = scol[slot];
 #pragma unroll
       for (int r = 0; r < DIM; ++r)
@@ -299,6 +301,25 @@ __global__ void __launch_bounds__(256) k_apply_bc(int n, int nslice, const int64
 __global__ void k_to_fp32(int64_t m, const double* __restrict__ a, float* __restrict__ b) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
     b[t] = (float)a[t];
+}
+
+// S_i = sum_j A_ij over the blocks of row i, summed in FP64 and rounded once.
+template <int DIM>
+__global__ void k_block_rowsum(int n, const int64_t* __restrict__ sell_ptr, const int* __restrict__ rowlen,
+                               const double* __restrict__ A, int64_t nslots, float* __restrict__ S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t base = sell_row_base(sell_ptr, i);
+  double acc[DIM * DIM];
+#pragma unroll
+  for (int e = 0; e < DIM * DIM; ++e) acc[e] = 0.0;
+  for (int k = 0; k < rowlen[i]; ++k) {
+    const int64_t s = sell_slot(base, k);
+#pragma unroll
+    for (int e = 0; e < DIM * DIM; ++e) acc[e] += A[e * nslots + s];
+  }
+#pragma unroll
+  for (int e = 0; e < DIM * DIM; ++e) S[(int64_t)i * DIM * DIM + e] = (float)acc[e];
 }
 
 }  // namespace
@@ -336,6 +357,7 @@ int build_pattern(lpm_handle* h) {
   for (int sl = 0; sl < h->nslice; ++sl) {
     int64_t mx = 0;
     for (int j = sl * kSlice; j < std::min(n, (sl + 1) * kSlice); ++j) mx = std::max(mx, hc[(size_t)j]);
+    mx = (mx + kVec - 1) / kVec * kVec;  // whole groups of four
     sp[(size_t)sl + 1] = sp[(size_t)sl] + mx * kSlice;
   }
   h->nslots = sp[(size_t)h->nslice];
@@ -409,16 +431,27 @@ int launch_assemble(lpm_handle* h, int tangent, int bc) {
   return LPM_OK;
 }
 
-// FP32 copy of the operator for the mixed-precision solve.
+// FP32 copy of the operator for the mixed-precision solve, with the block
+// row sums the difference-form product needs.
 int convert_A32(lpm_handle* h) {
   Dev& d = h->d;
-  const size_t vals = (size_t)h->nslots * h->dim * h->dim;
+  const int dim = h->dim;
+  const size_t vals = (size_t)h->nslots * dim * dim;
   if (!d.A32) {
     d.A32 = (float*)dev_alloc(h, sizeof(float) * std::max<size_t>(vals, 1));
     if (!d.A32) return LPM_ERR_NOMEM;
   }
+  if (!d.S32) {
+    d.S32 = (float*)dev_alloc(h, sizeof(float) * std::max<size_t>((size_t)h->n * dim * dim, 1));
+    if (!d.S32) return LPM_ERR_NOMEM;
+  }
   k_to_fp32<<<grid_for((long long)vals, 256, 152 * 32), 256, 0, h->stream>>>((int64_t)vals, d.A64, d.A32);
   LPM_LAUNCHED(h, "k_to_fp32");
+  if (dim == 3)
+    k_block_rowsum<3><<<(h->n + 127) / 128, 128, 0, h->stream>>>(h->n, d.sell_ptr, d.rowlen, d.A64, h->nslots, d.S32);
+  else
+    k_block_rowsum<2><<<(h->n + 127) / 128, 128, 0, h->stream>>>(h->n, d.sell_ptr, d.rowlen, d.A64, h->nslots, d.S32);
+  LPM_LAUNCHED(h, "k_block_rowsum");
   h->a32_valid = true;
   return LPM_OK;
 }
