@@ -229,6 +229,35 @@ def e2e_run(g, bcs, opts, steps, world):
     return t1 - t0, h2d, d2h
 
 
+def force_assembly_rate(g, capi, reps, local):
+    """Device time of the force pass (lpm_update_geometry_force) and of the
+    tangent assembly (symmetric variant, BC elimination) on the lattice as
+    it stands, `reps` launches each, CUDA events on the library's stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
+    out = {}
+    for name, fn in (("force", lambda: g.update()),
+                     ("assembly", lambda: g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_ELIMINATE))):
+        fn()
+        g.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        out[name] = e0.elapsed_time(e1) / reps
+    return out
+
+
+def force_bytes(nb, n):
+    """Algorithmic bytes of one force pass: per directed bond the partner
+    index, dis0, dLp, bdamage, Kn, Tv and the bond force written; per
+    particle positions, internal force, layer sums and stress."""
+    return nb * 52 + n * (24 + 24 + 64 + 48)
+
+
 def spmv_bytes(nblk, n, dim, value_bytes):
     """Algorithmic bytes of one CG sparse-product launch: every block's
     dim*dim values and column index, the row pointers, the search direction
@@ -409,7 +438,13 @@ def run_gb300(args):
                         "spmv_fp64_gflops": 2 * nblk * 9 / (avg64 * 1e-3) / 1e9,
                         "mixed_speedup": value / fv}
         f["handle"].close()
-    line["bonds_per_s_force"] = None
+    fa = force_assembly_rate(g, capi, 5, local)
+    fb = force_bytes(nb, n)
+    line["bonds_per_s"] = {"force": world * nb / (fa["force"] * 1e-3),
+                           "force_plus_assembly": world * nb / ((fa["force"] + fa["assembly"]) * 1e-3),
+                           "force_ms": fa["force"], "assembly_ms": fa["assembly"], "directed_bonds": nb,
+                           "force_achieved_gbs": fb / (fa["force"] * 1e-3) / 1e9,
+                           "force_algorithmic_bytes": fb}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         oracle, o = cpu_oracle_system(w, threads)

@@ -261,6 +261,47 @@ int lpm_get_stream(const lpm_handle* h, void** stream);
 /* Blocks until the handle's stream is idle. */
 int lpm_synchronize(lpm_handle* h);
 
+/* ---- Adjoint (backward) of a converged load step ----
+ * No counterpart in the reference, whose only derivative of the internal
+ * force is the forward-difference tangent (Stiffness::localStiffnessFD,
+ * stiffness.h:103-154).  lpm_load_step is the forward half of the pair.
+ *
+ * Response J = sum dJdx . x + sum dJdpin . Pin over the N*dim particle DOFs
+ * (x the current positions, Pin the internal forces; either array may be
+ * NULL).  A reaction over a constrained group is dJdpin = 1 on the group's
+ * DOFs along the axis; a gauge displacement is dJdx.  At the converged
+ * state (free DOFs in equilibrium) lpm_backward_step solves the adjoint
+ * system H_ff lambda = (dJdx + H dJdpin)_f with H = dPin/dx, the exact
+ * Jacobian applied matrix-free (not the analytical tangent, which leaves out
+ * the change of bond directions), by Jacobi-PCG at cg_tol (cg_maxit < 0:
+ * 2*n_dof), and returns dJ/dKn and dJ/dTv for every directed bond in stored
+ * bond order (lpm_get_bonds).  accumulate = 1 adds to the gradients of the
+ * previous calls (a response summed over load steps); 0 starts afresh.
+ * Every bond must be intact or broken on both sides (the energy-conserving
+ * case, H symmetric); partially damaged bonds give LPM_ERR_STATE.  The
+ * device gradients persist between calls; dJdKn/dJdTv may be NULL. */
+typedef struct {
+  int64_t cg_iters;  /* adjoint CG iterations */
+  double relres;     /* final relative residual of the adjoint solve */
+} lpm_adjoint_result;
+int lpm_backward_step(lpm_handle* h, const double* dJdx, const double* dJdpin, double cg_tol, int64_t cg_maxit,
+                      int accumulate, double* dJdKn, double* dJdTv, lpm_adjoint_result* res);
+/* y = H v with H = dPin/dx at the current state (all DOFs, N*dim each):
+ * the exact Jacobian-vector product the adjoint uses. */
+int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y);
+
+/* Device-resident snapshots of a step's state: positions, last converged
+ * positions, external loads, constraints, particle damage and state
+ * variables, bond damage, plastic stretch and their last converged copies.
+ * Restore reloads one and recomputes the force state.  They extend
+ * Assembly::storeStateVar/resetStateVar (assembly.h:140-166), which keep a
+ * single copy, to the many an adjoint over a load history replays from
+ * (checkpoint every k steps, recompute the steps between).  About
+ * 1 GB per snapshot at a million particles (18M bonds). */
+int lpm_checkpoint_save(lpm_handle* h, int* id);
+int lpm_checkpoint_restore(lpm_handle* h, int id);
+int lpm_checkpoint_drop(lpm_handle* h, int id);
+
 /* Allocation-free Jacobi-CG solve.  No counterpart in the reference: it is
  * for callers that cannot allocate device memory while they solve (a stream
  * being captured into a CUDA graph, a real-time loop that reserved its

@@ -52,6 +52,10 @@ class StepOpts(ctypes.Structure):
                 ("cg_maxit", ctypes.c_int64), ("max_cuts", ctypes.c_int)]
 
 
+class AdjointResult(ctypes.Structure):
+    _fields_ = [("cg_iters", ctypes.c_int64), ("relres", ctypes.c_double)]
+
+
 class StepResult(ctypes.Structure):
     _fields_ = [("newton_iters", ctypes.c_int), ("cuts", ctypes.c_int), ("damage_rounds", ctypes.c_int),
                 ("pad", ctypes.c_int), ("cg_iters", ctypes.c_int64)]
@@ -116,6 +120,11 @@ def load(build_if_needed=True):
         "lpm_set_kernel_timing": [H, ctypes.c_int],
         "lpm_get_stream": [H, ctypes.POINTER(ctypes.c_void_p)],
         "lpm_synchronize": [H],
+        "lpm_backward_step": [H, dp, dp, ctypes.c_double, i64, ctypes.c_int, dp, dp, ctypes.POINTER(AdjointResult)],
+        "lpm_apply_jacobian": [H, dp, dp],
+        "lpm_checkpoint_save": [H, ip],
+        "lpm_checkpoint_restore": [H, ctypes.c_int],
+        "lpm_checkpoint_drop": [H, ctypes.c_int],
     }
     for name, args in sigs.items():
         f = getattr(L, name)
@@ -135,7 +144,9 @@ def exported_symbols():
             "lpm_add_group", "lpm_apply_disp_bc", "lpm_apply_force_bc",
             "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
-            "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize"]
+            "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
+            "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
+            "lpm_checkpoint_drop"]
 
 
 def set_device(device):
@@ -191,6 +202,9 @@ class Lattice:
         L.lpm_num_blocks(h, ctypes.byref(nk))
         self.nblk = nk.value
         self.ndof = self.dim * self.n
+        # input index of each stored bond: stored order is by owner, then
+        # layer, input order within (stable)
+        self.bond_perm = np.lexsort((layer, p1))
 
     def close(self):
         if getattr(self, "h", None):
@@ -374,3 +388,38 @@ class Lattice:
 
     def synchronize(self):
         self._check(self._L.lpm_synchronize(self.h))
+
+    # -- adjoint -----------------------------------------------------------
+    def backward_step(self, dJdx=None, dJdpin=None, cg_tol=1e-10, cg_maxit=-1, accumulate=False):
+        """Gradients of J = dJdx . x + dJdpin . Pin (arrays of N*dim, or None)
+        with respect to every directed bond's Kn and Tv (stored bond order),
+        at the current converged state.  Returns (dJ/dKn, dJ/dTv, cg_iters,
+        relres)."""
+        null = ctypes.POINTER(ctypes.c_double)()
+        a = None if dJdx is None else np.ascontiguousarray(dJdx, dtype=np.float64).reshape(self.ndof)
+        c = None if dJdpin is None else np.ascontiguousarray(dJdpin, dtype=np.float64).reshape(self.ndof)
+        gk = np.zeros(self.nb)
+        gt = np.zeros(self.nb)
+        r = AdjointResult()
+        self._check(self._L.lpm_backward_step(self.h, null if a is None else _d(a), null if c is None else _d(c),
+                                              float(cg_tol), int(cg_maxit), int(bool(accumulate)), _d(gk), _d(gt),
+                                              ctypes.byref(r)), allow=(OK, NOT_CONVERGED))
+        return gk, gt, r.cg_iters, r.relres
+
+    def apply_jacobian(self, v):
+        """H v with H = dPin/dx at the current state (N*dim vectors)."""
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(self.ndof)
+        y = np.zeros(self.ndof)
+        self._check(self._L.lpm_apply_jacobian(self.h, _d(v), _d(y)))
+        return y
+
+    def checkpoint_save(self):
+        i = ctypes.c_int()
+        self._check(self._L.lpm_checkpoint_save(self.h, ctypes.byref(i)))
+        return i.value
+
+    def checkpoint_restore(self, cid):
+        self._check(self._L.lpm_checkpoint_restore(self.h, int(cid)))
+
+    def checkpoint_drop(self, cid):
+        self._check(self._L.lpm_checkpoint_drop(self.h, int(cid)))

@@ -1,0 +1,412 @@
+// Adjoint of a converged load step, and device-resident step checkpoints.
+//
+// Response J = a . x + c . Pin(x; Kn, Tv) for given weights a, c on the
+// particle DOFs (a gauge displacement, a reaction sum over a constrained
+// group, ...).  At a converged step the free DOFs are in equilibrium,
+// Pex_f = Pin_f(x), so with H = dPin/dx
+//     dJ/dtheta = (c - lambda) . dPin/dtheta,   H_ff lambda_f = (a + H^T c)_f,
+// lambda = 0 on the constrained DOFs.  The bond constants theta = (Kn_b,
+// Tv_b) of every directed bond enter Pin only through the bond forces
+// f_b = w_b (2 Kn_b dLe_b + 2 Tv_b D_i^l), D_i^l = sum over i's layer-l bonds
+// of dLe, so that with mu = c - lambda
+//     dJ/dKn_b = w_b dLe_b cs_b . (mu_i - mu_j),
+//     dJ/dTv_b = w_b D_i^l cs_b . (mu_i - mu_j).
+//
+// H is applied matrix-free: H v is the forward-mode derivative of the force
+// pass (particle.h:163-215, particle_elastic.h:38-50) with the bond damage
+// held fixed,
+//     d dLe_b = cs_b . (v_i - v_j),   d cs_b = ((v_i - v_j) - cs_b d dLe_b) / dis_b,
+//     d f_b   = w_b (2 Kn_b d dLe_b + 2 Tv_b d D_i^l),
+//     d Pin_i = sum_b d cs_b F_b + cs_b (d f_b + d f_opp(b)) / 2,   F_b = (f_b + f_opp(b)) / 2.
+// It is the exact Jacobian of Pin, unlike the analytical tangent of
+// derivative.h, which leaves out the change of the bond directions.  When
+// every bond is either intact or broken, Pin is the gradient of the lattice
+// energy  sum_b Kn_b dLe_b^2 / 2 + sum_(i,l) Tv_i (D_i^l)^2 / 2, so H is
+// symmetric and H_ff lambda = g is solved by Jacobi-PCG on the exact H with
+// its exact diagonal as the preconditioner.  Partially damaged bonds break
+// the symmetry; the adjoint then refuses the state.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+#include "lpm_cgvec.cuh"
+#include "lpm_device.cuh"
+
+namespace lpm {
+namespace {
+
+__device__ __forceinline__ void load_v(const double* __restrict__ v, int dim, int i, double (&o)[3]) {
+  o[0] = v[(int64_t)dim * i];
+  o[1] = v[(int64_t)dim * i + 1];
+  o[2] = dim == 3 ? v[(int64_t)dim * i + 2] : 0.0;
+}
+
+// Pass 1 of H v: per particle, the per-layer sums of d dLe over its bonds,
+// then d f of each of its bonds.
+__global__ void k_jvp_bonds(int n, int dim, const int64_t* __restrict__ bptr, const int* __restrict__ bp2,
+                            const int* __restrict__ blayer, const double* __restrict__ cs,
+                            const double* __restrict__ bdamage, const double* __restrict__ Kn,
+                            const double* __restrict__ Tv, const double* __restrict__ v, double* __restrict__ dfb,
+                            const CgScalars* cg) {
+  if (cg && cg->done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double vi[3];
+  load_v(v, dim, i, vi);
+  const int64_t b0 = bptr[i], b1 = bptr[i + 1];
+  double dD0 = 0.0, dD1 = 0.0;
+  for (int64_t b = b0; b < b1; ++b) {
+    if (is_broken(bdamage[b])) continue;
+    double vj[3];
+    load_v(v, dim, bp2[b], vj);
+    const double dd = cs[3 * b] * (vi[0] - vj[0]) + cs[3 * b + 1] * (vi[1] - vj[1]) + cs[3 * b + 2] * (vi[2] - vj[2]);
+    if (blayer[b] == 0)
+      dD0 += dd;
+    else
+      dD1 += dd;
+  }
+  for (int64_t b = b0; b < b1; ++b) {
+    if (is_broken(bdamage[b])) {
+      dfb[b] = 0.0;
+      continue;
+    }
+    double vj[3];
+    load_v(v, dim, bp2[b], vj);
+    const double dd = cs[3 * b] * (vi[0] - vj[0]) + cs[3 * b + 1] * (vi[1] - vj[1]) + cs[3 * b + 2] * (vi[2] - vj[2]);
+    dfb[b] = (1.0 - bdamage[b]) * (2.0 * Kn[b] * dd + 2.0 * Tv[b] * (blayer[b] == 0 ? dD0 : dD1));
+  }
+}
+
+// Pass 2 of H v: y_i = d Pin_i (zero on constrained DOFs when `mask` is
+// given).  With `cg` set it also forms p.q over the grid and, in the last
+// block, alpha = (r.z) / (p.q) for the CG update.
+__global__ void __launch_bounds__(256) k_jvp_particles(int n, int dim, const int64_t* __restrict__ bptr,
+                                                       const int* __restrict__ bp2, const int* __restrict__ opp,
+                                                       const double* __restrict__ cs, const double* __restrict__ dis,
+                                                       const double* __restrict__ bdamage,
+                                                       const double* __restrict__ bforce,
+                                                       const double* __restrict__ dfb, const double* __restrict__ v,
+                                                       const int* __restrict__ mask, double* __restrict__ y,
+                                                       CgScalars* cg, double* partials, unsigned int* ticket) {
+  if (cg && cg->done) return;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double vi[3];
+    load_v(v, dim, i, vi);
+    double P[3] = {0.0, 0.0, 0.0};
+    for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+      if (is_broken(bdamage[b])) continue;
+      double vj[3];
+      load_v(v, dim, bp2[b], vj);
+      const double c0 = cs[3 * b], c1 = cs[3 * b + 1], c2 = cs[3 * b + 2];
+      const double u0 = vi[0] - vj[0], u1 = vi[1] - vj[1], u2 = vi[2] - vj[2];
+      const double dd = c0 * u0 + c1 * u1 + c2 * u2;
+      const double rd = 1.0 / dis[b];
+      const int o = opp[b];
+      const double F = 0.5 * (bforce[b] + bforce[o]);
+      const double dF = 0.5 * (dfb[b] + dfb[o]);
+      P[0] += (u0 - c0 * dd) * rd * F + c0 * dF;
+      P[1] += (u1 - c1 * dd) * rd * F + c1 * dF;
+      P[2] += (u2 - c2 * dd) * rd * F + c2 * dF;
+    }
+    for (int k = 0; k < dim; ++k) {
+      const double yk = (mask && mask[3 * i + k]) ? 0.0 : P[k];
+      y[(int64_t)dim * i + k] = yk;
+      acc += vi[k] * yk;
+    }
+  }
+  if (!cg) return;
+  double w[1] = {acc}, tot[1];
+  if (grid_sum<1>(w, partials, ticket, tot) && threadIdx.x == 0) cg->alpha = cg->abs_new / tot[0];
+}
+
+// Exact diagonal of H (one DOF of particle i moved, its partners' layer sums
+// included) as the Jacobi preconditioner; 1 on constrained DOFs.
+__global__ void k_jac_invdiag(int n, int dim, const int64_t* __restrict__ bptr, const int* __restrict__ blayer,
+                              const int* __restrict__ opp, const double* __restrict__ cs,
+                              const double* __restrict__ dis, const double* __restrict__ bdamage,
+                              const double* __restrict__ bforce, const double* __restrict__ Kn,
+                              const double* __restrict__ Tv, const int* __restrict__ mask,
+                              double* __restrict__ invd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t b0 = bptr[i], b1 = bptr[i + 1];
+  for (int k = 0; k < dim; ++k) {
+    double S0 = 0.0, S1 = 0.0;  // d D_i^l for a unit move of DOF k of particle i
+    for (int64_t b = b0; b < b1; ++b) {
+      if (is_broken(bdamage[b])) continue;
+      if (blayer[b] == 0)
+        S0 += cs[3 * b + k];
+      else
+        S1 += cs[3 * b + k];
+    }
+    double h = 0.0;
+    for (int64_t b = b0; b < b1; ++b) {
+      if (is_broken(bdamage[b])) continue;
+      const double ck = cs[3 * b + k];
+      const int o = opp[b];
+      const double F = 0.5 * (bforce[b] + bforce[o]);
+      const double df = (1.0 - bdamage[b]) * (2.0 * Kn[b] * ck + 2.0 * Tv[b] * (blayer[b] == 0 ? S0 : S1));
+      // the partner's sum moves only through this bond: d dLe = ck
+      const double dfo = (1.0 - bdamage[o]) * (2.0 * Kn[o] * ck + 2.0 * Tv[o] * ck);
+      h += (1.0 - ck * ck) / dis[b] * F + ck * 0.5 * (df + dfo);
+    }
+    invd[(int64_t)dim * i + k] = (mask[3 * i + k] || h == 0.0) ? 1.0 : 1.0 / h;
+  }
+}
+
+// g = (a + y) on free DOFs, 0 on constrained ones.
+__global__ void k_adj_rhs(int n, int dim, const double* __restrict__ a, const double* __restrict__ y,
+                          const int* __restrict__ mask, double* __restrict__ g) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * dim) return;
+  const int i = t / dim, k = t % dim;
+  g[t] = mask[3 * i + k] ? 0.0 : (a ? a[t] : 0.0) + (y ? y[t] : 0.0);
+}
+
+// mu = c - lambda (lambda is zero on constrained DOFs).
+__global__ void k_adj_mu(int64_t m, const double* __restrict__ c, const double* __restrict__ lam,
+                         double* __restrict__ mu) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  mu[t] = (c ? c[t] : 0.0) - lam[t];
+}
+
+// dJ/dKn_b and dJ/dTv_b from mu, per directed bond (stored bond order).
+__global__ void k_param_grad(int n, int dim, const int64_t* __restrict__ bptr, const int* __restrict__ bp2,
+                             const int* __restrict__ blayer, const double* __restrict__ cs,
+                             const double* __restrict__ dLe, const double* __restrict__ dle_tot,
+                             const double* __restrict__ bdamage, const double* __restrict__ mu, int accumulate,
+                             double* __restrict__ gKn, double* __restrict__ gTv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double mi[3];
+  load_v(mu, dim, i, mi);
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    double gk = 0.0, gt = 0.0;
+    if (!is_broken(bdamage[b])) {
+      double mj[3];
+      load_v(mu, dim, bp2[b], mj);
+      const double cd = cs[3 * b] * (mi[0] - mj[0]) + cs[3 * b + 1] * (mi[1] - mj[1]) + cs[3 * b + 2] * (mi[2] - mj[2]);
+      const double w = 1.0 - bdamage[b];
+      gk = w * dLe[b] * cd;
+      gt = w * dle_tot[NL * i + blayer[b]] * cd;
+    }
+    gKn[b] = accumulate ? gKn[b] + gk : gk;
+    gTv[b] = accumulate ? gTv[b] + gt : gt;
+  }
+}
+
+// 1 in flag when some bond is partially damaged (EPS < d < 1 - EPS) or
+// broken while its opposite bond is not.
+__global__ void k_partial_damage(int64_t nb, const double* __restrict__ bdamage, const int* __restrict__ opp,
+                                 int* flag) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const double d = bdamage[b];
+  if ((d > EPS && d < 1.0 - EPS) || is_broken(d) != is_broken(bdamage[opp[b]])) atomicOr(flag, 1);
+}
+
+}  // namespace
+
+// Work buffers of the adjoint, allocated on first use (gradients zeroed).
+int adjoint_buffers(lpm_handle* h) {
+  Dev& d = h->d;
+  const size_t m = (size_t)h->n * h->dim;
+  double** vecs[9] = {&d.adj_g, &d.adj_lam, &d.adj_r, &d.adj_p, &d.adj_q, &d.adj_invd, &d.adj_mu, &d.adj_a, &d.adj_c};
+  for (double** v : vecs)
+    if (!*v) {
+      *v = (double*)dev_alloc(h, sizeof(double) * std::max<size_t>(m, 1));
+      if (!*v) return LPM_ERR_NOMEM;
+    }
+  double** bvecs[3] = {&d.adj_dfb, &d.adj_gkn, &d.adj_gtv};
+  for (double** v : bvecs)
+    if (!*v) {
+      *v = (double*)zeros_dev(h, sizeof(double) * std::max<size_t>((size_t)h->nb, 1));
+      if (!*v) return LPM_ERR_NOMEM;
+    }
+  if (!d.adj_flag) {
+    d.adj_flag = (int*)dev_alloc(h, sizeof(int));
+    if (!d.adj_flag) return LPM_ERR_NOMEM;
+  }
+  return LPM_OK;
+}
+
+// y = H v (mask: zero the constrained rows); with cg, p.q and alpha too.
+static int apply_jacobian(lpm_handle* h, const double* v, double* y, bool masked, CgScalars* cg) {
+  Dev& d = h->d;
+  const int T = 128;
+  k_jvp_bonds<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, h->dim, d.bptr, d.bp2, d.blayer, d.cs, d.bdamage, d.Kn,
+                                                       d.Tv, v, d.adj_dfb, cg);
+  LPM_LAUNCHED(h, "k_jvp_bonds");
+  k_jvp_particles<<<grid_for(h->n, 256, kMaxRedBlocks), 256, 0, h->stream>>>(
+      h->n, h->dim, d.bptr, d.bp2, d.opp, d.cs, d.dis, d.bdamage, d.bforce, d.adj_dfb, v, masked ? d.mask : nullptr, y,
+      cg, d.red.partials, d.red.ticket + 8);
+  LPM_LAUNCHED(h, "k_jvp_particles");
+  return LPM_OK;
+}
+
+int adjoint_apply(lpm_handle* h, const double* v_dev, double* y_dev) {
+  int st = adjoint_buffers(h);
+  if (st) return st;
+  return apply_jacobian(h, v_dev, y_dev, false, nullptr);
+}
+
+int adjoint_step(lpm_handle* h, const double* a_dev, const double* c_dev, double tol, long long maxit, int accumulate,
+                 double* gKn_dev, double* gTv_dev, long long* iters, double* relres) {
+  Dev& d = h->d;
+  const int dim = h->dim;
+  const int64_t m = (int64_t)h->n * dim;
+  int st = adjoint_buffers(h);
+  if (st) return st;
+  // the symmetric solve needs every bond intact or broken
+  LPM_CUDA(h, cudaMemsetAsync(d.adj_flag, 0, sizeof(int), h->stream));
+  k_partial_damage<<<grid_for(h->nb, 256), 256, 0, h->stream>>>(h->nb, d.bdamage, d.opp, d.adj_flag);
+  LPM_LAUNCHED(h, "k_partial_damage");
+  int flag = 0;
+  LPM_CUDA(h, cudaMemcpyAsync(&flag, d.adj_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (flag) {
+    h->err = "adjoint: partially or one-sidedly damaged bonds make the Jacobian non-symmetric";
+    return LPM_ERR_STATE;
+  }
+  // g = a + H c on the free DOFs
+  const int TV = 256;
+  if (c_dev) {
+    st = apply_jacobian(h, c_dev, d.adj_q, false, nullptr);
+    if (st) return st;
+  }
+  k_adj_rhs<<<grid_for(m, TV), TV, 0, h->stream>>>(h->n, dim, a_dev, c_dev ? d.adj_q : nullptr, d.mask, d.adj_g);
+  LPM_LAUNCHED(h, "k_adj_rhs");
+  k_jac_invdiag<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, dim, d.bptr, d.blayer, d.opp, d.cs, d.dis,
+                                                            d.bdamage, d.bforce, d.Kn, d.Tv, d.mask, d.adj_invd);
+  LPM_LAUNCHED(h, "k_jac_invdiag");
+  // H_ff lambda = g by Jacobi-PCG on the exact Jacobian
+  if (maxit < 0) maxit = 2LL * m;
+  const int GV = grid_for(m, 256, kMaxRedBlocks);
+  k_cg_init<double><<<GV, 256, 0, h->stream>>>(m, d.adj_g, d.adj_lam, d.adj_r, d.adj_p, d.adj_invd, d.cg, tol, maxit,
+                                               d.red.partials, d.red.ticket + 2);
+  LPM_LAUNCHED(h, "k_cg_init");
+  long long batch = 8;
+  for (;;) {
+    for (long long k = 0; k < batch; ++k) {
+      st = apply_jacobian(h, d.adj_p, d.adj_q, true, d.cg);
+      if (st) return st;
+      k_cg_update<double><<<GV, 256, 0, h->stream>>>(m, d.adj_lam, d.adj_r, d.adj_p, d.adj_q, d.adj_invd, d.cg,
+                                                     d.red.partials, d.red.ticket + 4);
+      LPM_LAUNCHED(h, "k_cg_update");
+      k_cg_pupdate<double><<<GV, 256, 0, h->stream>>>(m, d.adj_r, d.adj_invd, d.adj_p, d.cg);
+      LPM_LAUNCHED(h, "k_cg_pupdate");
+    }
+    LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
+    LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->h_cg->done) break;
+    if (batch < 64) batch *= 2;
+  }
+  const CgScalars c = *h->h_cg;
+  if (iters) *iters = c.it;
+  const double err = c.rhs_norm2 > 0 ? sqrt(c.rr / c.rhs_norm2) : 0.0;
+  if (relres) *relres = err;
+  if (c.done == 3) {
+    h->err = "adjoint: non-finite value in the CG iteration";
+    return LPM_ERR_NONFINITE;
+  }
+  // parameter gradients
+  k_adj_mu<<<grid_for(m, TV), TV, 0, h->stream>>>(m, c_dev, d.adj_lam, d.adj_mu);
+  LPM_LAUNCHED(h, "k_adj_mu");
+  k_param_grad<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, dim, d.bptr, d.bp2, d.blayer, d.cs, d.dLe,
+                                                           d.dle_tot, d.bdamage, d.adj_mu, accumulate, gKn_dev,
+                                                           gTv_dev);
+  LPM_LAUNCHED(h, "k_param_grad");
+  return err <= tol ? LPM_OK : LPM_NOT_CONVERGED;
+}
+
+// ---------------------------------------------------------------- checkpoints
+namespace {
+struct CkField {
+  void* dev;
+  size_t bytes;
+};
+// the arrays that define a step's state; everything else is recomputed by
+// the force pass after a restore
+std::vector<CkField> checkpoint_fields(lpm_handle* h) {
+  Dev& d = h->d;
+  const size_t N = (size_t)h->n, B = (size_t)h->nb, S = (size_t)h->nstate * N;
+  std::vector<CkField> f = {{d.x, 3 * N * 8},       {d.xlast, 3 * N * 8},     {d.pex, 3 * N * 8},
+                            {d.mask, 3 * N * 4},    {d.damage, N * 8},        {d.damage_last, N * 8},
+                            {d.dLp, B * 8},         {d.dLp_last, B * 8},      {d.bdamage, B * 8},
+                            {d.bdamage_last, B * 8}, {d.dis_last, B * 8},     {d.bforce_last, B * 8}};
+  if (d.state) f.push_back({d.state, S * 8});
+  if (d.state_last) f.push_back({d.state_last, S * 8});
+  if (d.ddot_local) f.push_back({d.ddot_local, N * 8});
+  if (d.ddot_nl) f.push_back({d.ddot_nl, N * 8});
+  std::vector<CkField> out;
+  for (const CkField& c : f)
+    if (c.dev && c.bytes) out.push_back(c);
+  return out;
+}
+}  // namespace
+
+int checkpoint_save(lpm_handle* h, int* id) {
+  std::vector<CkField> f = checkpoint_fields(h);
+  size_t total = 0;
+  for (const CkField& c : f) total += (c.bytes + 255) / 256 * 256;
+  void* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, std::max<size_t>(total, 256));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    h->err = "checkpoint: out of device memory";
+    return LPM_ERR_NOMEM;
+  }
+  size_t off = 0;
+  for (const CkField& c : f) {
+    e = cudaMemcpyAsync((char*)buf + off, c.dev, c.bytes, cudaMemcpyDeviceToDevice, h->stream);
+    if (e != cudaSuccess) {
+      cudaFree(buf);
+      return cuda_fail(h, e, "checkpoint copy");
+    }
+    off += (c.bytes + 255) / 256 * 256;
+  }
+  int slot = -1;
+  for (size_t k = 0; k < h->checkpoints.size(); ++k)
+    if (!h->checkpoints[k].buf) {
+      slot = (int)k;
+      break;
+    }
+  if (slot < 0) {
+    slot = (int)h->checkpoints.size();
+    h->checkpoints.push_back({});
+  }
+  h->checkpoints[(size_t)slot] = {buf, total};
+  *id = slot;
+  return LPM_OK;
+}
+
+int checkpoint_restore(lpm_handle* h, int id) {
+  if (id < 0 || (size_t)id >= h->checkpoints.size() || !h->checkpoints[(size_t)id].buf) {
+    h->err = "checkpoint: unknown id";
+    return LPM_ERR_ARG;
+  }
+  const Checkpoint& ck = h->checkpoints[(size_t)id];
+  std::vector<CkField> f = checkpoint_fields(h);
+  size_t off = 0;
+  for (const CkField& c : f) {
+    LPM_CUDA(h, cudaMemcpyAsync(c.dev, (const char*)ck.buf + off, c.bytes, cudaMemcpyDeviceToDevice, h->stream));
+    off += (c.bytes + 255) / 256 * 256;
+  }
+  h->a32_valid = false;
+  return launch_geometry_force(h);
+}
+
+int checkpoint_drop(lpm_handle* h, int id) {
+  if (id < 0 || (size_t)id >= h->checkpoints.size() || !h->checkpoints[(size_t)id].buf) {
+    h->err = "checkpoint: unknown id";
+    return LPM_ERR_ARG;
+  }
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  cudaFree(h->checkpoints[(size_t)id].buf);
+  h->checkpoints[(size_t)id] = {};
+  return LPM_OK;
+}
+
+}  // namespace lpm

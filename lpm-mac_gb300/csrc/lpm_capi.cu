@@ -33,6 +33,15 @@ void* dev_alloc(lpm_handle* h, size_t bytes) {
   return p;
 }
 
+void* zeros_dev(lpm_handle* h, size_t bytes) {
+  void* p = dev_alloc(h, bytes);
+  if (p && cudaMemset(p, 0, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+    cuda_fail(h, cudaErrorUnknown, "cudaMemset");
+    return nullptr;
+  }
+  return p;
+}
+
 }  // namespace lpm
 
 using namespace lpm;
@@ -249,6 +258,7 @@ int lpm_destroy(lpm_handle* h) {
   if (!h) return LPM_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (void* p : h->allocations) cudaFree(p);
+  for (auto& c : h->checkpoints) cudaFree(c.buf);
   for (auto& g : h->groups) cudaFree(g.ids);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->h_cg) cudaFreeHost(h->h_cg);
@@ -694,6 +704,63 @@ int lpm_synchronize(lpm_handle* h) {
   if (!h) return LPM_ERR_ARG;
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   return LPM_OK;
+}
+
+
+int lpm_backward_step(lpm_handle* h, const double* dJdx, const double* dJdpin, double cg_tol, int64_t cg_maxit,
+                      int accumulate, double* dJdKn, double* dJdTv, lpm_adjoint_result* res) {
+  if (!h) return arg_error(h, "NULL handle");
+  if (!(cg_tol > 0.0)) return arg_error(h, "cg_tol must be positive");
+  int st = adjoint_buffers(h);
+  if (st) return st;
+  Dev& d = h->d;
+  const size_t m = (size_t)h->n * h->dim;
+  if (dJdx) LPM_CUDA(h, cudaMemcpyAsync(d.adj_a, dJdx, sizeof(double) * m, cudaMemcpyHostToDevice, h->stream));
+  if (dJdpin) LPM_CUDA(h, cudaMemcpyAsync(d.adj_c, dJdpin, sizeof(double) * m, cudaMemcpyHostToDevice, h->stream));
+  long long it = 0;
+  double rel = 0.0;
+  st = adjoint_step(h, dJdx ? d.adj_a : nullptr, dJdpin ? d.adj_c : nullptr, cg_tol, (long long)cg_maxit,
+                    accumulate ? 1 : 0, d.adj_gkn, d.adj_gtv, &it, &rel);
+  if (st < 0) return st;
+  const size_t B = (size_t)h->nb;
+  if (dJdKn) LPM_CUDA(h, cudaMemcpyAsync(dJdKn, d.adj_gkn, sizeof(double) * B, cudaMemcpyDeviceToHost, h->stream));
+  if (dJdTv) LPM_CUDA(h, cudaMemcpyAsync(dJdTv, d.adj_gtv, sizeof(double) * B, cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (res) {
+    res->cg_iters = it;
+    res->relres = rel;
+  }
+  h->stats.cg_iters_total += it;
+  return st;
+}
+
+int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y) {
+  if (!h || !v || !y) return arg_error(h, "NULL handle or buffer");
+  int st = adjoint_buffers(h);
+  if (st) return st;
+  Dev& d = h->d;
+  const size_t m = (size_t)h->n * h->dim;
+  LPM_CUDA(h, cudaMemcpyAsync(d.adj_p, v, sizeof(double) * m, cudaMemcpyHostToDevice, h->stream));
+  st = adjoint_apply(h, d.adj_p, d.adj_q);
+  if (st) return st;
+  LPM_CUDA(h, cudaMemcpyAsync(y, d.adj_q, sizeof(double) * m, cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_checkpoint_save(lpm_handle* h, int* id) {
+  if (!h || !id) return arg_error(h, "NULL handle or id");
+  return checkpoint_save(h, id);
+}
+
+int lpm_checkpoint_restore(lpm_handle* h, int id) {
+  if (!h) return arg_error(h, "NULL handle");
+  return checkpoint_restore(h, id);
+}
+
+int lpm_checkpoint_drop(lpm_handle* h, int id) {
+  if (!h) return arg_error(h, "NULL handle");
+  return checkpoint_drop(h, id);
 }
 
 }  // extern "C"

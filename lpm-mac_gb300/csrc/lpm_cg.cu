@@ -20,9 +20,12 @@
 // block row sum of A (exact algebra).  The stiffness rows nearly sum to zero
 // (rigid translations cost no force), so for the smooth directions that CG
 // resolves last the plain sum cancels to a small fraction of its terms and
-// FP32 rounding swamps it; the differences keep those terms small.  On the
-// simple cubic test lattices this brings the FP32 iteration count to within
-// a few per cent of FP64.  The recurrence runs with reliable updates (residual
+// FP32 rounding swamps it; the differences keep those terms small, and a
+// compensated accumulation (dot2_acc) removes the rounding of the sum.
+// Without both, the FP32 iterate carries errors along the smooth directions
+// that its residual barely shows, and the next Newton solve pays for them
+// (about 50% more iterations at 101^3).  With both, every solve of a load
+// step takes within a few per cent of the FP64 iteration count.  The recurrence runs with reliable updates (residual
 // replacement): when the iterated residual has fallen by kDelta since the
 // last update, the FP32 solution increment is folded into the FP64 solution,
 // the residual is recomputed in FP64 as b - A64 x and replaces the iterated
@@ -31,6 +34,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "lpm_cgvec.cuh"
 #include "lpm_device.cuh"
 
 namespace lpm {
@@ -53,14 +57,33 @@ __device__ __forceinline__ float comp(const float4& v, int t) {
   return t == 0 ? v.x : t == 1 ? v.y : t == 2 ? v.z : v.w;
 }
 
-// y = row `row` of A times p.  The row is walked in groups of four blocks:
-// one 16-byte load brings a block element for four blocks (FP32), two for
-// FP64.  Padding blocks are zero and point at the row itself.
+// s + c += a*b with the rounding errors of the product and of the sum kept
+// in c (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26 (2005): TwoProduct by FMA, TwoSum).  The _rn intrinsics keep the
+// compiler from contracting the steps into other FMAs.
+__device__ __forceinline__ void dot2_acc(float& s, float& c, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float pe = fmaf(a, b, -p);
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  const float se = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(pe, se));
+}
+
+// y = row `row` of A times p (FP32), in difference form with compensated
+// accumulation: the sum comes out as if accumulated in twice the precision
+// and then rounded, so the only FP32 errors left are in the differences
+// (exact for neighbouring values within a factor of two) and the operator's
+// own rounding.  The row is walked in groups of four blocks: one 16-byte load
+// brings a block element for four blocks.  Padding blocks are zero and point
+// at the row itself.
 template <int DIM>
 __device__ __forceinline__ void row_product(const SellView& v, const float* __restrict__ A,
                                             const float* __restrict__ p, int row, float (&y)[DIM]) {
+  float sc[DIM], cc[DIM];
 #pragma unroll
-  for (int r = 0; r < DIM; ++r) y[r] = 0.f;
+  for (int r = 0; r < DIM; ++r) sc[r] = cc[r] = 0.f;
   float pi[DIM];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) pi[k] = __ldg(&p[(int64_t)row * DIM + k]);
@@ -81,14 +104,16 @@ __device__ __forceinline__ void row_product(const SellView& v, const float* __re
 #pragma unroll
       for (int r = 0; r < DIM; ++r)
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) y[r] = fmaf(comp(a[r * DIM + k], t), pc[k], y[r]);
+        for (int k = 0; k < DIM; ++k) dot2_acc(sc[r], cc[r], comp(a[r * DIM + k], t), pc[k]);
     }
   }
   const float* Si = v.S + (int64_t)row * DIM * DIM;
 #pragma unroll
-  for (int r = 0; r < DIM; ++r)
+  for (int r = 0; r < DIM; ++r) {
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) y[r] = fmaf(__ldg(&Si[r * DIM + k]), pi[k], y[r]);
+    for (int k = 0; k < DIM; ++k) dot2_acc(sc[r], cc[r], __ldg(&Si[r * DIM + k]), pi[k]);
+    y[r] = __fadd_rn(sc[r], cc[r]);
+  }
 }
 
 // FP64: the partner values of the four blocks are gathered first; then each
@@ -143,83 +168,6 @@ __global__ void __launch_bounds__(256) k_cg_spmv(SellView v, const T* __restrict
   }
   double w[1] = {acc}, tot[1];
   if (grid_sum<1>(w, partials, ticket, tot) && threadIdx.x == 0) cg->alpha = cg->abs_new / tot[0];
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_cg_update(int64_t ndof, T* __restrict__ x, T* __restrict__ r,
-                                                   const T* __restrict__ p, const T* __restrict__ q,
-                                                   const T* __restrict__ invd, CgScalars* cg, double* partials,
-                                                   unsigned int* ticket) {
-  if (cg->done) return;
-  const T alpha = (T)cg->alpha;
-  double v[2] = {0.0, 0.0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
-    const T ri = r[i] - alpha * q[i];
-    x[i] = x[i] + alpha * p[i];
-    r[i] = ri;
-    const T zi = invd[i] * ri;
-    v[0] += (double)ri * (double)ri;
-    v[1] += (double)ri * (double)zi;
-  }
-  double tot[2];
-  if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
-    cg->rr = tot[0];
-    if (!isfinite(tot[0]) || !isfinite(tot[1])) {
-      cg->done = 3;
-    } else if (tot[0] < cg->threshold) {
-      cg->done = 1;
-    } else {
-      const double old = cg->abs_new;
-      cg->abs_new = tot[1];
-      cg->beta = tot[1] / old;
-      cg->it += 1;
-      if (cg->it >= cg->maxit) cg->done = 2;
-    }
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_cg_pupdate(int64_t ndof, const T* __restrict__ r, const T* __restrict__ invd,
-                                                    T* __restrict__ p, const CgScalars* cg) {
-  if (cg->done) return;
-  const T beta = (T)cg->beta;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = invd[i] * r[i] + beta * p[i];
-}
-
-template <typename T>
-__global__ void k_cg_init(int64_t ndof, const T* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
-                          T* __restrict__ p, const T* __restrict__ invd, CgScalars* cg, double tol, long long maxit,
-                          double* partials, unsigned int* ticket) {
-  double v[2] = {0.0, 0.0};
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
-    const T bi = b[i];
-    const T pi = invd[i] * bi;
-    x[i] = T(0);
-    r[i] = bi;
-    p[i] = pi;
-    v[0] += (double)bi * (double)bi;
-    v[1] += (double)bi * (double)pi;
-  }
-  double tot[2];
-  if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
-    cg->rhs_norm2 = tot[0];
-    cg->rr = tot[0];
-    cg->threshold = fmax(tol * tol * tot[0], DBL_MIN);
-    cg->abs_new = tot[1];
-    cg->alpha = 0.0;
-    cg->beta = 0.0;
-    cg->it = 0;
-    cg->maxit = maxit;
-    if (!isfinite(tot[0]) || !isfinite(tot[1]))
-      cg->done = 3;
-    else if (tot[0] == 0.0 || tot[0] < cg->threshold)
-      cg->done = 1;
-    else if (maxit <= 0)
-      cg->done = 2;
-    else
-      cg->done = 0;
-  }
 }
 
 // Jacobi preconditioner from the diagonal blocks of A (= diagonal of K).
@@ -476,6 +424,9 @@ int run_cg(lpm_handle* h, const T* A, const T* b, T* x, T* r, T* p, T* q, const 
   return LPM_OK;
 }
 
+}  // namespace
+
+// Jacobi preconditioner of the assembled operator (FP64, and FP32 on request).
 int prepare_invd(lpm_handle* h, bool want32) {
   Dev& d = h->d;
   if (h->dim == 3)
@@ -488,7 +439,6 @@ int prepare_invd(lpm_handle* h, bool want32) {
   return LPM_OK;
 }
 
-}  // namespace
 
 int solve_fp64(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres) {
   Dev& d = h->d;

@@ -112,6 +112,17 @@ struct Dev {
   double *pp, *state, *state_last, *ddot_local, *ddot_nl, *nonlocal_L;
   int64_t* nl_ptr;  // nonlocal neighbours (CSR, ascending ids)
   int* nl_idx;
+  // adjoint: response weights a, c; CG vectors; mu = c - lambda; d f per
+  // bond; parameter gradients per bond; a device flag
+  double *adj_a, *adj_c, *adj_g, *adj_lam, *adj_r, *adj_p, *adj_q, *adj_invd, *adj_mu;
+  double *adj_dfb, *adj_gkn, *adj_gtv;
+  int* adj_flag;
+};
+
+// One device-resident copy of a step's state (lpm_checkpoint_save).
+struct Checkpoint {
+  void* buf = nullptr;
+  size_t bytes = 0;
 };
 
 }  // namespace lpm
@@ -143,6 +154,7 @@ struct lpm_handle {
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   std::vector<void*> allocations;
+  std::vector<lpm::Checkpoint> checkpoints;
 };
 
 namespace lpm {
@@ -165,11 +177,21 @@ int convert_A32(lpm_handle* h);
 // solvers (lpm_cg.cu)
 int solve_fp64(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);
 int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);
+int prepare_invd(lpm_handle* h, bool want32);
+// adjoint and checkpoints (lpm_adjoint.cu); vectors are device pointers
+int adjoint_buffers(lpm_handle* h);
+int adjoint_apply(lpm_handle* h, const double* v, double* y);
+int adjoint_step(lpm_handle* h, const double* a, const double* c, double tol, long long maxit, int accumulate,
+                 double* gKn, double* gTv, long long* iters, double* relres);
+int checkpoint_save(lpm_handle* h, int* id);
+int checkpoint_restore(lpm_handle* h, int id);
+int checkpoint_drop(lpm_handle* h, int id);
 
 // helpers (lpm_capi.cu)
 int cuda_fail(lpm_handle* h, cudaError_t e, const char* what);
 void set_global_error(const std::string& msg);  // text of lpm_last_error(NULL)
 void* dev_alloc(lpm_handle* h, size_t bytes);
+void* zeros_dev(lpm_handle* h, size_t bytes);  // dev_alloc + zero fill
 inline int grid_for(long long work, int threads, int cap = 1 << 20) {
   long long g = (work + threads - 1) / threads;
   if (g < 1) g = 1;

@@ -87,6 +87,24 @@ class UnitCell:
         return float(k[0]), float(k[1]), float(k[2])
 
 
+    def elastic_constants_grad(self, E, nu, plane_stress=False, layout="reference"):
+        """Derivatives of elastic_constants(E, nu) = (Kn0, Kn1, Tv) with
+        respect to E and nu: a (2, 3) array, rows d/dE and d/dnu."""
+        if not plane_stress:
+            D = (1.0 + nu) * (1.0 - 2.0 * nu)
+            dC_dE = np.array([(1.0 - nu) / D, nu / D, 0.5 / (1.0 + nu)])
+            dC_dnu = np.array([2.0 * E * nu * (2.0 - nu) / D ** 2, E * (1.0 + 2.0 * nu * nu) / D ** 2,
+                               -0.5 * E / (1.0 + nu) ** 2])
+        else:
+            q = 1.0 - nu * nu
+            dC_dE = np.array([1.0 / q, nu / q, 0.5 / (1.0 + nu)])
+            dC_dnu = np.array([2.0 * E * nu / q ** 2, E * (1.0 + nu * nu) / q ** 2, -0.5 * E / (1.0 + nu) ** 2])
+        out = np.zeros((2, 3))
+        for r, dC in enumerate((dC_dE, dC_dnu)):
+            out[r] = self.elastic_constants(C=tuple(dC), layout=layout)  # the map is linear in C
+        return out
+
+
 def hex_plate(ncol, nrow, a):
     """Hexagonal plate: even rows hold ncol points, odd rows ncol-1 points
     shifted by a/2 (the createPlateHEX2D row rule); row pitch a*sqrt(3)/2."""

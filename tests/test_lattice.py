@@ -75,3 +75,16 @@ def test_nonlocal_neighbours_match_reference():
     xyz = d["xyz0"].reshape(-1, 3)
     ptr, idx = lat.nonlocal_neighbors(xyz, 1.5 * 0.6)
     assert np.array_equal(ptr, d["nl_ptr"]) and np.array_equal(idx, d["nl_idx"])
+
+
+def test_elastic_constants_grad_matches_central_differences():
+    for kind in (lat.HEXAGON2D, lat.SIMPLECUBIC3D, lat.FCC3D):
+        c = lat.UnitCell(kind, 0.25)
+        for ps in (False, True):
+            E, nu, h = 69e3, 0.3, 1e-6
+            g = c.elastic_constants_grad(E, nu, ps, "row")
+            f = lambda E_, nu_: np.array(c.elastic_constants(E_, nu_, ps, layout="row"))  # noqa: E731
+            fE = (f(E * (1 + h), nu) - f(E * (1 - h), nu)) / (2 * h * E)
+            fn = (f(E, nu + h) - f(E, nu - h)) / (2 * h)
+            assert np.abs(g[0] - fE).max() <= 1e-8 * np.abs(fE).max()
+            assert np.abs(g[1] - fn).max() <= 1e-8 * np.abs(fn).max()
