@@ -65,6 +65,8 @@ typedef struct lpm_handle lpm_handle;
 #define LPM_B_TV 107
 #define LPM_B_DIS0 108
 #define LPM_B_DLP 109
+#define LPM_B_SCRIT 110 /* critical stretch of the softening law (LPM_LAW_SOFTENING) */
+#define LPM_B_KAPPA 111 /* largest stretch reached, softening law history             */
 
 /* tangent variants for lpm_assemble */
 #define LPM_TANGENT_AS_WRITTEN 0 /* derivative.h as written: K_ii[1][0] stays 0 (derivative.h:38) */
@@ -127,6 +129,19 @@ int lpm_get_mask(const lpm_handle* h, int* mask);
 #define LPM_LAW_DAMAGE 1
 #define LPM_LAW_J2 2
 #define LPM_LAW_FATIGUE_HCF 3
+/* Continuous softening bond law, an extension with no reference class
+ * (the brittle rule of particle_elastic.h:52-68 made gradual).  Each bond
+ * keeps the largest stretch s = (dis - dis0)/dis0 it has reached, kappa, and
+ *   d = 0                                                 kappa <= s_c
+ *   d = 1 - (s_c/kappa) (alpha s_c - kappa)/((alpha - 1) s_c)   s_c < kappa < alpha s_c
+ *   d = 1                                                 kappa >= alpha s_c
+ * so that a bond's force falls linearly from its peak at s_c to zero at
+ * alpha s_c.  bdamage = max(bdamage, d) after each converged solve; an
+ * increase above 1e-3 on some bond asks for another solve, as the static
+ * damage update does.  params {alpha, s_c}; s_c is the default critical
+ * stretch of the particle's bonds, which LPM_B_SCRIT overrides per bond
+ * (e.g. Weibull draws shared by the two directed copies of a bond). */
+#define LPM_LAW_SOFTENING 4
 int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams, int per_particle);
 /* Particle::type of every particle and the solver's undamaged_pt_type
  * (particles of that type skip the damage updates, solver_static.h:37,57). */
@@ -207,6 +222,9 @@ typedef struct {
 
 /* Load-step driver. */
 #define LPM_SOLVER_STATIC 0 /* SolverStatic::solveProblemStep (solver_static.h:97-149) */
+#define LPM_SOLVER_STATIC_ELIMINATE 2 /* SolverStatic::solveProblemStep with the displacement-BC
+                                         elimination it leaves commented out (solver_static.h:113)
+                                         applied, so that damage rounds run on a constrained tangent */
 #define LPM_SOLVER_FATIGUE_STATIC 1 /* SolverFatigue::solveProblemStep + the storing of
                                        solveProblemStatic (solver_fatigue.h:243-298) */
 typedef struct {

@@ -17,14 +17,14 @@ ERR_ARG, ERR_TOPOLOGY, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_NONFINITE = -1, -2, -
 F_XYZ, F_XYZ0, F_PIN, F_PEX, F_STRESS, F_DVIS, F_DLE_TOT, F_TDLE_TOT, F_CS_SUM, F_DAMAGE, F_XYZ_LAST, F_DISP, \
     F_RESIDUAL, F_STATE, F_DDOT_LOCAL, F_DDOT_NONLOCAL, F_DAMAGE_LAST = range(17)
 # bond fields
-B_BFORCE, B_BDAMAGE, B_DLE, B_DIS, B_BSTRAIN, B_CS, B_KN, B_TV, B_DIS0, B_DLP = range(100, 110)
+B_BFORCE, B_BDAMAGE, B_DLE, B_DIS, B_BSTRAIN, B_CS, B_KN, B_TV, B_DIS0, B_DLP, B_SCRIT, B_KAPPA = range(100, 112)
 TANGENT_AS_WRITTEN, TANGENT_SYMMETRIC = 0, 1
 BC_NONE, BC_ELIMINATE = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 BC_DISP, BC_FORCE = 0, 1
-SOLVER_STATIC, SOLVER_FATIGUE_STATIC = 0, 1
-LAW_ELASTIC, LAW_DAMAGE, LAW_J2, LAW_FATIGUE_HCF = 0, 1, 2, 3
-_NSTATE = {LAW_ELASTIC: 1, LAW_DAMAGE: 1, LAW_J2: 7, LAW_FATIGUE_HCF: 3}
+SOLVER_STATIC, SOLVER_FATIGUE_STATIC, SOLVER_STATIC_ELIMINATE = 0, 1, 2
+LAW_ELASTIC, LAW_DAMAGE, LAW_J2, LAW_FATIGUE_HCF, LAW_SOFTENING = 0, 1, 2, 3, 4
+_NSTATE = {LAW_ELASTIC: 1, LAW_DAMAGE: 1, LAW_J2: 7, LAW_FATIGUE_HCF: 3, LAW_SOFTENING: 1}
 
 
 class LpmError(RuntimeError):
@@ -172,7 +172,7 @@ def _l(a):
 _PWIDTH = {F_XYZ: 3, F_XYZ0: 3, F_PIN: 3, F_PEX: 3, F_STRESS: 6, F_DVIS: 1, F_DLE_TOT: 2, F_TDLE_TOT: 2,
            F_CS_SUM: 6, F_DAMAGE: 1, F_XYZ_LAST: 3, F_DDOT_LOCAL: 1, F_DDOT_NONLOCAL: 1, F_DAMAGE_LAST: 1}
 _BWIDTH = {B_BFORCE: 1, B_BDAMAGE: 1, B_DLE: 1, B_DIS: 1, B_BSTRAIN: 1, B_CS: 3, B_KN: 1, B_TV: 1, B_DIS0: 1,
-           B_DLP: 1}
+           B_DLP: 1, B_SCRIT: 1, B_KAPPA: 1}
 
 
 class Lattice:

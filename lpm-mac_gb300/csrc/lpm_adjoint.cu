@@ -340,6 +340,8 @@ std::vector<CkField> checkpoint_fields(lpm_handle* h) {
   if (d.state_last) f.push_back({d.state_last, S * 8});
   if (d.ddot_local) f.push_back({d.ddot_local, N * 8});
   if (d.ddot_nl) f.push_back({d.ddot_nl, N * 8});
+  if (d.bkappa) f.push_back({d.bkappa, B * 8});
+  if (d.bkappa_last) f.push_back({d.bkappa_last, B * 8});
   std::vector<CkField> out;
   for (const CkField& c : f)
     if (c.dev && c.bytes) out.push_back(c);

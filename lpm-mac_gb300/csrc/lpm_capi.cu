@@ -106,6 +106,8 @@ FieldRef field_ref(lpm_handle* h, int f) {
     case LPM_B_TV: return {d.Tv, B};
     case LPM_B_DIS0: return {d.dis0, B};
     case LPM_B_DLP: return {d.dLp, B};
+    case LPM_B_SCRIT: return {d.bcrit, d.bcrit ? B : 0};
+    case LPM_B_KAPPA: return {d.bkappa, d.bkappa ? B : 0};
   }
   return {nullptr, 0};
 }
@@ -361,8 +363,8 @@ int lpm_update_state(lpm_handle* h) {
 
 int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams, int per_particle) {
   if (!h) return LPM_ERR_ARG;
-  static const int need[4] = {1, 3, 7, 4};
-  if (law < LPM_LAW_ELASTIC || law > LPM_LAW_FATIGUE_HCF) return arg_error(h, "unknown material law");
+  static const int need[5] = {1, 3, 7, 4, 2};
+  if (law < LPM_LAW_ELASTIC || law > LPM_LAW_SOFTENING) return arg_error(h, "unknown material law");
   if (nparams < need[law] || !params) return arg_error(h, "too few material parameters for the law");
   const size_t N = (size_t)h->n;
   std::vector<double> pp(N * (size_t)nparams);
@@ -384,6 +386,22 @@ int lpm_set_law(lpm_handle* h, int law, const double* params, int nparams, int p
     std::vector<double> c(N);
     for (size_t i = 0; i < N; ++i) c[i] = pp[i * nparams];
     LPM_CUDA(h, cudaMemcpy(d.crit, c.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  }
+  if (law == LPM_LAW_SOFTENING) {
+    // per-bond critical stretch from the owner's default; history cleared
+    const size_t B = (size_t)h->nb;
+    std::vector<int64_t> bptr(N + 1);
+    LPM_CUDA(h, cudaMemcpy(bptr.data(), d.bptr, sizeof(int64_t) * (N + 1), cudaMemcpyDeviceToHost));
+    std::vector<double> sc(B), zero(B, 0.0);
+    for (size_t i = 0; i < N; ++i)
+      for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) sc[(size_t)b] = pp[i * nparams + 1];
+    if (!d.bcrit) d.bcrit = (double*)dev_alloc(h, sizeof(double) * std::max<size_t>(B, 1));
+    if (!d.bkappa) d.bkappa = (double*)dev_alloc(h, sizeof(double) * std::max<size_t>(B, 1));
+    if (!d.bkappa_last) d.bkappa_last = (double*)dev_alloc(h, sizeof(double) * std::max<size_t>(B, 1));
+    if (!d.bcrit || !d.bkappa || !d.bkappa_last) return LPM_ERR_NOMEM;
+    LPM_CUDA(h, cudaMemcpy(d.bcrit, sc.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
+    LPM_CUDA(h, cudaMemcpy(d.bkappa, zero.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
+    LPM_CUDA(h, cudaMemcpy(d.bkappa_last, zero.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
   }
   h->law = law;
   h->law_np = nparams;
@@ -563,7 +581,8 @@ int lpm_newton(lpm_handle* h, int max_iter, double tol, int precision, double cg
 
 int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts* o, lpm_step_result* res) {
   if (!h || !o || nbc < 0 || (nbc > 0 && !bcs)) return arg_error(h, "bad load step");
-  if (o->solver != LPM_SOLVER_STATIC && o->solver != LPM_SOLVER_FATIGUE_STATIC)
+  if (o->solver != LPM_SOLVER_STATIC && o->solver != LPM_SOLVER_FATIGUE_STATIC &&
+      o->solver != LPM_SOLVER_STATIC_ELIMINATE)
     return arg_error(h, "bad solver kind");
   for (int k = 0; k < nbc; ++k)
     if (bcs[k].group < 0 || bcs[k].group >= (int)h->groups.size() || (bcs[k].kind != LPM_BC_DISP &&
@@ -602,7 +621,7 @@ int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts
     } else {
       int damaged = 0;
       do {
-        st = lpm_assemble(h, o->tangent, LPM_BC_NONE);
+        st = lpm_assemble(h, o->tangent, o->solver == LPM_SOLVER_STATIC_ELIMINATE ? LPM_BC_ELIMINATE : LPM_BC_NONE);
         if (st) return st;
         st = lpm_newton(h, o->max_iter, o->tol, o->precision, o->cg_tol, o->cg_maxit, &ni);
         if (st < 0) return st;
@@ -656,6 +675,7 @@ int lpm_store_state(lpm_handle* h) {
   LPM_CUDA(h, cudaMemcpyAsync(d.bforce_last, d.bforce, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.dLp_last, d.dLp, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.state_last, d.state, sizeof(double) * N * h->nstate, k, h->stream));
+  if (d.bkappa) LPM_CUDA(h, cudaMemcpyAsync(d.bkappa_last, d.bkappa, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   return LPM_OK;
 }
@@ -672,6 +692,7 @@ int lpm_reset_state(lpm_handle* h, int reset_xyz) {
   LPM_CUDA(h, cudaMemcpyAsync(d.bforce, d.bforce_last, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.dLp, d.dLp_last, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.state, d.state_last, sizeof(double) * N * h->nstate, k, h->stream));
+  if (d.bkappa) LPM_CUDA(h, cudaMemcpyAsync(d.bkappa, d.bkappa_last, sizeof(double) * B, k, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   return LPM_OK;
 }

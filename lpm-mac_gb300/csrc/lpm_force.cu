@@ -216,7 +216,7 @@ int launch_geometry_force(lpm_handle* h) {
   k_geometry_force<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.x, d.bptr, d.bp2, d.blayer, d.dis0, d.dLp,
                                                            d.bdamage, d.Kn, d.Tv, d.dis, d.bstrain, d.dLe, d.cs,
                                                            d.bforce, d.dle_tot, d.tdle_tot, d.cs_sum, d.damage,
-                                                           h->law != 0 ? 1 : 0, d.tsum, d.msum);
+                                                           (h->law >= 1 && h->law <= 3) ? 1 : 0, d.tsum, d.msum);
   LPM_LAUNCHED(h, "k_geometry_force");
   k_particle_force<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.bptr, d.opp, d.bforce, d.cs, d.dis, d.bdamage,
                                                            d.nbonds, h->particle_volume, h->nneighbors, d.pin,

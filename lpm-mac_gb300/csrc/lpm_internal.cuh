@@ -112,6 +112,8 @@ struct Dev {
   double *pp, *state, *state_last, *ddot_local, *ddot_nl, *nonlocal_L;
   int64_t* nl_ptr;  // nonlocal neighbours (CSR, ascending ids)
   int* nl_idx;
+  // softening law: critical stretch and largest stretch reached, per bond
+  double *bcrit, *bkappa, *bkappa_last;
   // adjoint: response weights a, c; CG vectors; mu = c - lambda; d f per
   // bond; parameter gradients per bond; a device flag
   double *adj_a, *adj_c, *adj_g, *adj_lam, *adj_r, *adj_p, *adj_q, *adj_invd, *adj_mu;

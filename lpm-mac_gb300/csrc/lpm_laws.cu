@@ -7,6 +7,7 @@
 //   law 1 ParticleElasticDamage  params {k0, k1, damage_threshold}
 //   law 2 ParticleJ2Plasticity   params {E, mu, sigmay, xi, H, A, damage_threshold}
 //   law 3 ParticleFatigueHCF     params {A, B, d, damage_threshold}
+//   law 4 softening bond law     params {alpha, s_c} (per-bond s_c in bcrit)
 #include <climits>
 
 #include "lpm_device.cuh"
@@ -146,6 +147,37 @@ __global__ void k_static_damage(LawView v, int* any) {
   if (hit) atomicOr(any, 1);
 }
 
+// Softening bond law: kappa = max(kappa, stretch), d(kappa) linear softening
+// between s_c and alpha s_c; bdamage never decreases.  Thread per particle,
+// its own bonds (both directed copies of a bond see the same stretch).
+__global__ void k_softening_damage(int n, const int64_t* __restrict__ bptr, const int* __restrict__ ptype,
+                                   int undamaged, const double* __restrict__ pp, int np,
+                                   const double* __restrict__ dis, const double* __restrict__ dis0,
+                                   const double* __restrict__ bcrit, double* __restrict__ bkappa,
+                                   double* __restrict__ bdamage, int* any) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || ptype[i] == undamaged) return;
+  const double alpha = pp[(int64_t)i * np];
+  bool hit = false;
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    const double s = (dis[b] - dis0[b]) / dis0[b];
+    const double k = fmax(bkappa[b], s);
+    bkappa[b] = k;
+    const double sc = bcrit[b];
+    double d = 0.0;
+    if (k >= alpha * sc)
+      d = 1.0;
+    else if (k > sc)
+      d = 1.0 - (sc / k) * (alpha * sc - k) / ((alpha - 1.0) * sc);
+    const double old = bdamage[b];
+    if (d > old) {
+      bdamage[b] = d;
+      if (d - old > 1e-3) hit = true;
+    }
+  }
+  if (hit) atomicOr(any, 1);
+}
+
 // ParticleFatigueHCF::updateParticleFatigueDamage (particle_fatigue_hcf.h:147-160).
 __global__ void k_fatigue_damage(LawView v, double dt, int* any) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -234,6 +266,12 @@ int launch_static_damage(lpm_handle* h, int* any_new) {
   if (h->law <= 2) {
     k_static_damage<<<grid_for(h->n, T), T, 0, h->stream>>>(v, flag);
     LPM_LAUNCHED(h, "k_static_damage");
+  }
+  if (h->law == LPM_LAW_SOFTENING) {
+    const Dev& d = h->d;
+    k_softening_damage<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.bptr, d.ptype, h->undamaged, d.pp, h->law_np,
+                                                               d.dis, d.dis0, d.bcrit, d.bkappa, d.bdamage, flag);
+    LPM_LAUNCHED(h, "k_softening_damage");
   }
   return read_flag(h, flag, any_new);
 }

@@ -193,3 +193,129 @@ def nonlocal_neighbors(xyz, cutoff):
     ptr = np.zeros(n + 1, np.int64)
     np.add.at(ptr, i + 1, 1)
     return np.cumsum(ptr), j.astype(np.int32)
+
+
+def weibull_draws(p1, p2, shape, scale, seed):
+    """One draw per undirected bond, shared by its two directed copies:
+    scale * (-ln(1 - U))^(1/shape) with U uniform from a seeded generator,
+    the pairs {i, j} taken in ascending (min, max) order."""
+    p1 = np.asarray(p1, dtype=np.int64)
+    p2 = np.asarray(p2, dtype=np.int64)
+    n = int(max(p1.max(initial=0), p2.max(initial=0))) + 1
+    key = np.minimum(p1, p2) * n + np.maximum(p1, p2)
+    uniq, inv = np.unique(key, return_inverse=True)
+    u = np.random.default_rng(seed).random(len(uniq))
+    return (scale * (-np.log1p(-u)) ** (1.0 / shape))[inv]
+
+
+def precrack(xyz, p1, p2, layer, y0, x_tip):
+    """Deletes the bonds whose segment crosses the line y = y0 left of x_tip
+    (a straight edge crack; geometry/geo1_CT_configuration.cpp:79-134 filters
+    its bond list against a notch region the same way); both directed copies
+    of a bond go together.  Returns the kept (p1, p2, layer)."""
+    xyz = np.asarray(xyz, dtype=np.float64)
+    y1, y2 = xyz[p1, 1], xyz[p2, 1]
+    cross = (y1 - y0) * (y2 - y0) < 0
+    t = np.where(cross, (y0 - y1) / np.where(cross, y2 - y1, 1.0), 0.0)
+    xc = xyz[p1, 0] + t * (xyz[p2, 0] - xyz[p1, 0])
+    keep = ~(cross & (xc < x_tip))
+    return p1[keep], p2[keep], layer[keep]
+
+
+def sent_plate(ncol, nrow, a, crack_ratio=0.3):
+    """Single-edge-notched plate: hexagonal lattice (hex_plate rows) with a
+    crack from the left edge along the mid-height line between two rows,
+    of length crack_ratio * W.  Returns (xyz, p1, p2, layer, cell)."""
+    cell = UnitCell(HEXAGON2D, a / 2)
+    xyz = hex_plate(ncol, nrow, a)
+    p1, p2, layer = find_bonds(xyz, cell)
+    h = a * math.sqrt(3.0) / 2.0
+    y0 = (nrow // 2 - 0.5) * h
+    W = xyz[:, 0].max() - xyz[:, 0].min()
+    p1, p2, layer = precrack(xyz, p1, p2, layer, y0, xyz[:, 0].min() + crack_ratio * W)
+    return xyz, p1, p2, layer, cell
+
+
+def random_rotations(n, rng):
+    """n rotation matrices uniform on SO(3), from uniform unit quaternions
+    (Shoemake's subgroup algorithm)."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    q = np.stack([np.sqrt(1 - u1) * np.sin(2 * np.pi * u2), np.sqrt(1 - u1) * np.cos(2 * np.pi * u2),
+                  np.sqrt(u1) * np.sin(2 * np.pi * u3), np.sqrt(u1) * np.cos(2 * np.pi * u3)], axis=1)
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - z * w)
+    R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w)
+    R[:, 2, 1] = 2 * (y * z + x * w)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def bcc_polycrystal(ncell, a, ngrain, seed, overlap=0.5):
+    """Voronoi polycrystal of BCC grains in the cube [0, ncell*a]^3, built the
+    way the reference's Fortran Mbuilder does (benchmark/BCC_Hailong/
+    create_BCC_configuration.F90:169-333): for every grain, a BCC lattice of
+    cubic cell a rotated by the grain's orientation about its seed, the sites
+    inside the grain's Voronoi cell and the box kept, and sites closer than
+    overlap * (nearest-neighbour distance) to an earlier grain's particle
+    dropped.  Seeds are uniform in the box and orientations uniform on SO(3),
+    from one seeded generator.  Returns (xyz, grain id per particle)."""
+    from scipy.spatial import cKDTree
+
+    rng = np.random.default_rng(seed)
+    L = ncell * a
+    seeds = rng.random((ngrain, 3)) * L
+    R = random_rotations(ngrain, rng)
+    # bounding box of each Voronoi cell inside the box, from a sampling grid
+    m = 48
+    g = (np.arange(m) + 0.5) / m * L
+    G = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    owner = cKDTree(seeds).query(G)[1]
+    pad = L / m
+    parts, gid = [], []
+    tree = None
+    thr = overlap * a * math.sqrt(3.0) / 2.0
+    for k in range(ngrain):
+        P = G[owner == k]
+        if len(P) == 0:
+            continue
+        lo, hi = P.min(0) - pad, P.max(0) + pad
+        corners = np.array([[x, y, z] for x in (lo[0], hi[0]) for y in (lo[1], hi[1]) for z in (lo[2], hi[2])])
+        local = (corners - seeds[k]) @ R[k]  # grain frame: x_local = R^T (x - seed)
+        i0 = np.floor(local.min(0) / a).astype(int) - 1
+        i1 = np.ceil(local.max(0) / a).astype(int) + 1
+        ax = [np.arange(i0[d], i1[d] + 1) for d in range(3)]
+        C = np.stack(np.meshgrid(*ax, indexing="ij"), -1).reshape(-1, 3).astype(np.float64) * a
+        sites = np.concatenate([C, C + 0.5 * a])
+        X = sites @ R[k].T + seeds[k]
+        inbox = np.all((X >= 0.0) & (X <= L), axis=1)
+        X = X[inbox]
+        X = X[cKDTree(seeds).query(X)[1] == k]
+        if tree is not None and len(X):
+            near = tree.query(X, distance_upper_bound=thr)[0]
+            X = X[~np.isfinite(near) | (near >= thr)]
+        parts.append(X)
+        gid.append(np.full(len(X), k, np.int32))
+        tree = cKDTree(np.concatenate(parts))
+    return np.concatenate(parts), np.concatenate(gid)
+
+
+def prune_weak(xyz, cell, min_bonds):
+    """Indices of the particles kept after repeatedly dropping those with
+    fewer than min_bonds bonds (createBonds rule).  Grain-boundary and
+    surface particles of a polycrystal can end up with two or three bonds,
+    too few to hold them in 3-D: their stiffness has a null direction and
+    the Newton system becomes singular."""
+    keep = np.arange(len(xyz))
+    while True:
+        p1, _, _ = find_bonds(xyz[keep], cell)
+        nb = np.bincount(p1, minlength=len(keep))
+        ok = nb >= min_bonds
+        if ok.all():
+            return keep
+        keep = keep[ok]

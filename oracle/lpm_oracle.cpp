@@ -48,8 +48,10 @@ struct lo_sys {
   std::vector<long> cptr, tpos;
   std::vector<int> cidx;
   std::vector<double> K;
-  // law: 0 elastic, 1 elastic damage, 2 J2 plasticity, 3 HCF fatigue
+  // law: 0 elastic, 1 elastic damage, 2 J2 plasticity, 3 HCF fatigue,
+  // 4 softening bond law (no reference class; restated from its definition)
   int law = 0;
+  std::vector<double> bcrit, bkappa, bkappa_last;  // softening law, per bond
   int np = 0;                // parameters per particle
   std::vector<double> pp;    // [n * np] per-particle law parameters
   std::vector<double> crit;  // per-particle critical bond strain (elastic law)
@@ -104,7 +106,7 @@ void update_geometry(lo_sys* s) {
 // damage to the larger particle damage (particle_elastic_damage.h:74-87,
 // particle_j2plasticity.h:63-76, particle_fatigue_hcf.h:65-80).
 void update_bond_force(lo_sys* s) {
-  const bool dmg = s->law != 0;
+  const bool dmg = s->law >= 1 && s->law <= 3;
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < s->n; ++i) {
     for (long b = s->bptr[i]; b < s->bptr[i + 1]; ++b) {
@@ -420,6 +422,27 @@ bool static_damage(lo_sys* s) {
       s->damage[i] += s->ddot_nl[i];
       if (s->damage[i] >= thr) s->damage[i] = 1;
       any = (std::abs(s->damage[i] - s->damage_last[i]) > 1e-3) || any;
+    } else if (s->law == 4) {
+      // softening bond law: kappa = max(kappa, (dis - dis0)/dis0);
+      // d = 1 - (s_c/kappa)(alpha s_c - kappa)/((alpha - 1) s_c) between s_c
+      // and alpha s_c, 0 below, 1 above; bdamage never decreases
+      const double alpha = s->pp[(size_t)i * s->np];
+      for (long b = s->bptr[i]; b < s->bptr[i + 1]; ++b) {
+        const double st = (s->dis[b] - s->dis0[b]) / s->dis0[b];
+        const double k = std::max(s->bkappa[b], st);
+        s->bkappa[b] = k;
+        const double sc = s->bcrit[b];
+        double d = 0.0;
+        if (k >= alpha * sc)
+          d = 1.0;
+        else if (k > sc)
+          d = 1.0 - (sc / k) * (alpha * sc - k) / ((alpha - 1.0) * sc);
+        const double old = s->bdamage[b];
+        if (d > old) {
+          s->bdamage[b] = d;
+          if (d - old > 1e-3) any = true;
+        }
+      }
     }
   }
   return any;
@@ -625,6 +648,8 @@ static std::vector<double>* bfield(lo_sys* s, int f) {
     case LO_TV: return &s->Tv;
     case LO_DIS0: return &s->dis0;
     case LO_DLP: return &s->dLp;
+    case LO_SCRIT: return &s->bcrit;
+    case LO_KAPPA: return &s->bkappa;
   }
   return nullptr;
 }
@@ -656,6 +681,14 @@ void lo_set_law(lo_sys* s, int law, const double* params, int nparams, int per_p
     for (int k = 0; k < nparams; ++k) s->pp[i * nparams + k] = per_particle ? params[i * nparams + k] : params[k];
   if (law == 0 && nparams >= 1)
     for (size_t i = 0; i < N; ++i) s->crit[i] = s->pp[i * nparams];
+  if (law == 4) {
+    const size_t B = s->bp2.size();
+    s->bcrit.assign(B, 0.0);
+    for (size_t i = 0; i < N; ++i)
+      for (long b = s->bptr[i]; b < s->bptr[i + 1]; ++b) s->bcrit[(size_t)b] = s->pp[i * nparams + 1];
+    s->bkappa.assign(B, 0.0);
+    s->bkappa_last.assign(B, 0.0);
+  }
   // state variables (constructors of the particle classes)
   s->nstate = law == 2 ? 7 : (law == 3 ? 3 : 1);
   s->state.assign(N * s->nstate, 0.0);
@@ -814,6 +847,7 @@ void lo_store_state(lo_sys* s) {
   s->bdamage_last = s->bdamage;
   s->bforce_last = s->bforce;
   s->dLp_last = s->dLp;
+  s->bkappa_last = s->bkappa;
 }
 void lo_reset_state(lo_sys* s, int reset_xyz) {
   if (reset_xyz) s->x = s->xlast;
@@ -823,6 +857,7 @@ void lo_reset_state(lo_sys* s, int reset_xyz) {
   s->bdamage = s->bdamage_last;
   s->bforce = s->bforce_last;
   s->dLp = s->dLp_last;
+  s->bkappa = s->bkappa_last;
 }
 
 int lo_load_step(lo_sys* s, const int* apply, const double* d, const double* f, int sym, int bc_elim, int max_iter,
@@ -845,12 +880,12 @@ int lo_load_step(lo_sys* s, const int* apply, const double* d, const double* f, 
     int nn = 0;
     bool damaged = false;
     do {
-      lo_assemble(s, sym, bc_elim);
+      lo_assemble(s, sym, bc_elim != 0 ? 1 : 0);
       nn = lo_newton(s, max_iter, tol, cg_tol, cg_maxit);
       if (nn >= max_iter) break;
       damaged = false;
       update_state(s);  // Assembly::updateStateVar
-      if (!bc_elim) damaged = static_damage(s);
+      if (bc_elim != 1) damaged = static_damage(s);
       lo_store_state(s);
       if (damaged) lo_update_geometry_force(s);
     } while (damaged);

@@ -38,7 +38,9 @@ enum lo_pfield {
 enum lo_bfield {
   LO_BFORCE = 0, LO_BDAMAGE = 1, LO_DLE = 2, LO_DIS = 3, LO_BSTRAIN = 4,
   LO_CS = 5, /* Nb*3 */
-  LO_KN = 6, LO_TV = 7, LO_DIS0 = 8, LO_DLP = 9
+  LO_KN = 6, LO_TV = 7, LO_DIS0 = 8, LO_DLP = 9,
+  LO_SCRIT = 10, /* softening law: critical stretch per bond      */
+  LO_KAPPA = 11  /* softening law: largest stretch reached        */
 };
 
 /* Creates a system.  Bonds are directed (p1 -> p2) with layer 0 or 1; the
@@ -70,6 +72,9 @@ void lo_set_mask(lo_sys* s, const int* mask); /* N*3 disp_constraint */
  *   1 ParticleElasticDamage  {k0, k1, damage_threshold}
  *   2 ParticleJ2Plasticity   {E, mu, sigmay, xi, H, A, damage_threshold}
  *   3 ParticleFatigueHCF     {A, B, d, damage_threshold}
+ *   4 softening bond law     {alpha, s_c}: no reference class; d(kappa)
+ *     falls from 0 at kappa = s_c to 1 at alpha*s_c with a linearly
+ *     softening bond force, kappa the largest stretch (dis-dis0)/dis0
  * Resets the state variables to the constructors' values. */
 void lo_set_law(lo_sys* s, int law, const double* params, int nparams, int per_particle);
 void lo_set_types(lo_sys* s, const int* types, int undamaged_type);
@@ -116,7 +121,8 @@ void lo_add_pex(lo_sys* s, const double* f);
 
 /* One static load step with the step cut-back of solver_static.h:64-95 and
  * solver_fatigue.h:243-275.  bc_elim selects the tangent BC treatment
- * (0: SolverStatic, 1: SolverFatigue).  Returns the number of Newton
+ * (0: SolverStatic, 1: SolverFatigue, 2: SolverStatic's damage rounds on
+ * the BC-eliminated tangent).  Returns the number of Newton
  * iterations of the accepted step, or -1 after max_cuts cut-backs. */
 int lo_load_step(lo_sys* s, const int* apply, const double* d, const double* f, int sym, int bc_elim, int max_iter,
                  double tol, double cg_tol, long cg_maxit, int max_cuts);

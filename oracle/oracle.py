@@ -17,11 +17,12 @@ _lib = None
 
 # particle / bond field ids (lpm_oracle.h)
 XYZ, XYZ0, PIN, PEX, STRESS, DVIS, DLE_TOT, TDLE_TOT, CS_SUM, DAMAGE, XYZ_LAST, STATE, DDOT_LOCAL = range(13)
-BFORCE, BDAMAGE, DLE, DIS, BSTRAIN, CS, KN, TV, DIS0, DLP = range(10)
+BFORCE, BDAMAGE, DLE, DIS, BSTRAIN, CS, KN, TV, DIS0, DLP, SCRIT, KAPPA = range(12)
 
 _PWIDTH = {XYZ: 3, XYZ0: 3, PIN: 3, PEX: 3, STRESS: 6, DVIS: 1, DLE_TOT: 2, TDLE_TOT: 2, CS_SUM: 6,
            DAMAGE: 1, XYZ_LAST: 3, DDOT_LOCAL: 1}
-_BWIDTH = {BFORCE: 1, BDAMAGE: 1, DLE: 1, DIS: 1, BSTRAIN: 1, CS: 3, KN: 1, TV: 1, DIS0: 1, DLP: 1}
+_BWIDTH = {BFORCE: 1, BDAMAGE: 1, DLE: 1, DIS: 1, BSTRAIN: 1, CS: 3, KN: 1, TV: 1, DIS0: 1, DLP: 1, SCRIT: 1,
+           KAPPA: 1}
 
 
 def build(force=False):
