@@ -279,6 +279,29 @@ int lpm_get_stream(const lpm_handle* h, void** stream);
 /* Blocks until the handle's stream is idle. */
 int lpm_synchronize(lpm_handle* h);
 
+/* One fatigue cycle: SolverFatigue::solveProblemOneCycle (solver_fatigue.h:
+ * 212-233) on the load steps generateLoadCycle builds (solver_fatigue.h:
+ * 128-172).  bcs_unit are the boundary conditions of a unit load increment
+ * (the LoadUniaxialDisp / LoadUniaxialForce / LoadDogBoneDisp / LoadCTForce
+ * templates of load_step_fatigue.h with their load set to 1); the cycle
+ * applies them scaled by (f1 - f0)/n_interval in n_interval steps, then by
+ * (f2 - f1)/n_interval in n_interval steps.  Each step assembles the
+ * BC-eliminated tangent, runs Newton (opts: tangent, precision, max_iter,
+ * tol, cg_tol, cg_maxit; no cut-back, as in the reference) and updates the
+ * state variables; then the nonlocal fatigue damage rate and damage are
+ * updated with dNdt, the state is stored and the force state refreshed.
+ * res (may be NULL) sums the Newton and CG iterations of the cycle and
+ * reports whether new damage appeared. */
+typedef struct {
+  int newton_iters;      /* Newton iterations, all steps of the cycle    */
+  int unconverged_steps; /* steps that hit max_iter (kept, as the reference does) */
+  int new_damage;        /* updateFatigueDamage found a damage change   */
+  int pad;
+  int64_t cg_iters;      /* CG iterations of the cycle                  */
+} lpm_cycle_result;
+int lpm_fatigue_cycle(lpm_handle* h, const lpm_bc* bcs_unit, int nbc, double f0, double f1, double f2,
+                      int n_interval, double dNdt, const lpm_step_opts* opts, lpm_cycle_result* res);
+
 /* ---- Adjoint (backward) of a converged load step ----
  * No counterpart in the reference, whose only derivative of the internal
  * force is the forward-difference tangent (Stiffness::localStiffnessFD,

@@ -52,6 +52,11 @@ class StepOpts(ctypes.Structure):
                 ("cg_maxit", ctypes.c_int64), ("max_cuts", ctypes.c_int)]
 
 
+class CycleResult(ctypes.Structure):
+    _fields_ = [("newton_iters", ctypes.c_int), ("unconverged_steps", ctypes.c_int), ("new_damage", ctypes.c_int),
+                ("pad", ctypes.c_int), ("cg_iters", ctypes.c_int64)]
+
+
 class AdjointResult(ctypes.Structure):
     _fields_ = [("cg_iters", ctypes.c_int64), ("relres", ctypes.c_double)]
 
@@ -120,6 +125,8 @@ def load(build_if_needed=True):
         "lpm_set_kernel_timing": [H, ctypes.c_int],
         "lpm_get_stream": [H, ctypes.POINTER(ctypes.c_void_p)],
         "lpm_synchronize": [H],
+        "lpm_fatigue_cycle": [H, ctypes.POINTER(BC), ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                              ctypes.c_int, ctypes.c_double, ctypes.POINTER(StepOpts), ctypes.POINTER(CycleResult)],
         "lpm_backward_step": [H, dp, dp, ctypes.c_double, i64, ctypes.c_int, dp, dp, ctypes.POINTER(AdjointResult)],
         "lpm_apply_jacobian": [H, dp, dp],
         "lpm_checkpoint_save": [H, ip],
@@ -145,7 +152,7 @@ def exported_symbols():
             "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
             "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
-            "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
+            "lpm_fatigue_cycle", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
             "lpm_checkpoint_drop"]
 
 
@@ -345,6 +352,30 @@ class Lattice:
 
     def apply_force_bc(self, group, fx, fy, fz, mode=0):
         self._check(self._L.lpm_apply_force_bc(self.h, int(group), int(mode), float(fx), float(fy), float(fz)))
+
+    @staticmethod
+    def _bc_array(bcs):
+        arr = (BC * max(len(bcs), 1))()
+        for k, b in enumerate(bcs):
+            if b[0] == "disp":
+                arr[k] = BC(BC_DISP, int(b[1]), int(b[4]) if len(b) > 4 else 0, int(b[2]), float(b[3]), 0, 0, 0)
+            else:
+                arr[k] = BC(BC_FORCE, int(b[1]), int(b[5]) if len(b) > 5 else 0, 0, 0.0, float(b[2]), float(b[3]),
+                            float(b[4]))
+        return arr
+
+    def fatigue_cycle(self, bcs_unit, f0, f1, f2, n_interval, dNdt, tangent=TANGENT_SYMMETRIC, precision=PREC_FP64,
+                      max_iter=30, tol=1e-5, cg_tol=1e-10, cg_maxit=-1):
+        """One cycle of lpm_fatigue_cycle; bcs_unit in load_step's form, for a
+        unit load increment."""
+        o = StepOpts(SOLVER_FATIGUE_STATIC, int(tangent), int(precision), int(max_iter), float(tol), float(cg_tol),
+                     int(cg_maxit), 0)
+        r = CycleResult()
+        st = self._check(self._L.lpm_fatigue_cycle(self.h, self._bc_array(bcs_unit), len(bcs_unit), float(f0),
+                                                   float(f1), float(f2), int(n_interval), float(dNdt),
+                                                   ctypes.byref(o), ctypes.byref(r)), allow=(OK, NOT_CONVERGED))
+        return dict(status=st, newton_iters=r.newton_iters, unconverged_steps=r.unconverged_steps,
+                    new_damage=bool(r.new_damage), cg_iters=r.cg_iters)
 
     def load_step(self, bcs, solver=SOLVER_FATIGUE_STATIC, tangent=TANGENT_SYMMETRIC, precision=PREC_FP64,
                   max_iter=30, tol=1e-5, cg_tol=1e-10, cg_maxit=-1, max_cuts=8):

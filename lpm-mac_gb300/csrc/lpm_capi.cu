@@ -728,6 +728,54 @@ int lpm_synchronize(lpm_handle* h) {
 }
 
 
+int lpm_fatigue_cycle(lpm_handle* h, const lpm_bc* bcs, int nbc, double f0, double f1, double f2, int n_interval,
+                      double dNdt, const lpm_step_opts* o, lpm_cycle_result* res) {
+  if (!h || !o || nbc < 0 || (nbc > 0 && !bcs) || n_interval < 1) return arg_error(h, "bad fatigue cycle");
+  for (int k = 0; k < nbc; ++k)
+    if (bcs[k].group < 0 || bcs[k].group >= (int)h->groups.size() || (bcs[k].kind != LPM_BC_DISP &&
+                                                                     bcs[k].kind != LPM_BC_FORCE))
+      return arg_error(h, "bad boundary condition");
+  lpm_cycle_result r{};
+  const int64_t it0 = h->stats.cg_iters_total;
+  int st = LPM_OK;
+  for (int half = 0; half < 2; ++half) {
+    const double inc = (half == 0 ? f1 - f0 : f2 - f1) / n_interval;
+    for (int step = 0; step < n_interval; ++step) {
+      // SolverFatigue::solveProblemStep (solver_fatigue.h:272-296)
+      for (int k = 0; k < nbc; ++k)
+        if (bcs[k].kind == LPM_BC_FORCE) {
+          st = lpm_apply_force_bc(h, bcs[k].group, bcs[k].mode, bcs[k].fx * inc, bcs[k].fy * inc, bcs[k].fz * inc);
+          if (st) return st;
+        }
+      for (int k = 0; k < nbc; ++k)
+        if (bcs[k].kind == LPM_BC_DISP) {
+          st = lpm_apply_disp_bc(h, bcs[k].group, bcs[k].axis, bcs[k].mode, bcs[k].value * inc);
+          if (st) return st;
+        }
+      st = lpm_assemble(h, o->tangent, LPM_BC_ELIMINATE);
+      if (st) return st;
+      int ni = 0;
+      st = lpm_newton(h, o->max_iter, o->tol, o->precision, o->cg_tol, o->cg_maxit, &ni);
+      if (st < 0) return st;
+      r.newton_iters += ni;
+      if (ni >= o->max_iter) ++r.unconverged_steps;
+      st = launch_update_state(h);  // solver_fatigue.h:222
+      if (st) return st;
+    }
+  }
+  int any = 0;
+  st = launch_fatigue_damage(h, dNdt, &any);  // solver_fatigue.h:229-232
+  if (st) return st;
+  st = lpm_store_state(h);
+  if (st) return st;
+  st = launch_geometry_force(h);
+  if (st) return st;
+  r.new_damage = any;
+  r.cg_iters = h->stats.cg_iters_total - it0;
+  if (res) *res = r;
+  return r.unconverged_steps ? LPM_NOT_CONVERGED : LPM_OK;
+}
+
 int lpm_backward_step(lpm_handle* h, const double* dJdx, const double* dJdpin, double cg_tol, int64_t cg_maxit,
                       int accumulate, double* dJdKn, double* dJdTv, lpm_adjoint_result* res) {
   if (!h) return arg_error(h, "NULL handle");

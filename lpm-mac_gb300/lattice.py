@@ -319,3 +319,66 @@ def prune_weak(xyz, cell, min_bonds):
         if ok.all():
             return keep
         keep = keep[ok]
+
+
+def _in_notch(x, y, tip, half_width):
+    """The wedge notch of geometry/geo1_CT_configuration.cpp:54-64: within
+    half_width of the notch line and inside the 30-degree wedge that opens
+    from the tip towards +x."""
+    dy = y - tip[1]
+    return (np.abs(dy) <= half_width) & (dy >= (tip[0] - x) / math.sqrt(3.0)) & (dy <= (x - tip[0]) / math.sqrt(3.0))
+
+
+def ct_specimen(W, a0_ratio, a, notch_half_width=None):
+    """Compact-tension plate on a hexagonal lattice of spacing a, ASTM E647
+    proportions in the layout of the reference's CT builder
+    (geometry/geo1_CT_configuration.cpp:120-160): back edge at x = 0, load
+    line at x = W, plate 1.25 W wide and 1.2 W high, pin holes of diameter
+    0.25 W centred on the load line at 0.275 W above and below the crack
+    line y = 0.6 W, and a wedge notch from the right edge to the tip at
+    x = W - a0_ratio*W.  Particles inside the holes or the notch are dropped,
+    and so is every bond that passes through them (tested at ten points
+    along the bond, as the builder does).  Returns
+    (xyz, p1, p2, layer, cell, info) with the hole centres, radius and tip."""
+    cell = UnitCell(HEXAGON2D, a / 2)
+    Lx, Ly = 1.25 * W, 1.2 * W
+    ncol = int(math.floor(Lx / a)) + 1
+    nrow = int(math.floor(Ly / (a * math.sqrt(3.0) / 2.0))) + 1
+    xyz = hex_plate(ncol, nrow, a)
+    yc, r = 0.6 * W, 0.125 * W
+    holes = [(W, yc - 0.275 * W), (W, yc + 0.275 * W)]
+    tip = (W - a0_ratio * W, yc)
+    hw = notch_half_width if notch_half_width is not None else 0.026 * W
+
+    def invalid(x, y):
+        bad = _in_notch(x, y, tip, hw)
+        for cx, cy in holes:
+            bad |= (x - cx) ** 2 + (y - cy) ** 2 <= r * r
+        return bad
+
+    xyz = xyz[~invalid(xyz[:, 0], xyz[:, 1])]
+    p1, p2, layer = find_bonds(xyz, cell)
+    keep = np.ones(len(p1), dtype=bool)
+    for k in range(10):
+        t = (k + 0.5) / 10.0
+        mx = xyz[p1, 0] + t * (xyz[p2, 0] - xyz[p1, 0])
+        my = xyz[p1, 1] + t * (xyz[p2, 1] - xyz[p1, 1])
+        keep &= ~invalid(mx, my)
+    info = dict(holes=holes, radius=r, tip=tip, crack_y=yc, W=W)
+    return xyz, p1[keep], p2[keep], layer[keep], cell, info
+
+
+def ct_groups(xyz, info, a):
+    """Load groups of LoadCTForce (load_step_fatigue.h:69-84): the particles
+    on the upper face of the top hole and the lower face of the bottom hole
+    within 30 degrees of the load line (pin contact), and the back-edge
+    particles on the crack line (held in y)."""
+    (cx, cy_b), (_, cy_t) = info["holes"]
+    r = info["radius"]
+    d_t = np.hypot(xyz[:, 0] - cx, xyz[:, 1] - cy_t)
+    d_b = np.hypot(xyz[:, 0] - cx, xyz[:, 1] - cy_b)
+    ring = 1.5 * a
+    top = np.where((d_t < r + ring) & (xyz[:, 1] - cy_t > np.cos(np.pi / 6) * d_t))[0]
+    bottom = np.where((d_b < r + ring) & (cy_b - xyz[:, 1] > np.cos(np.pi / 6) * d_b))[0]
+    mid = np.where((xyz[:, 0] < 0.6 * a) & (np.abs(xyz[:, 1] - info["crack_y"]) < a))[0]
+    return dict(top=top, bottom=bottom, mid=mid)

@@ -257,6 +257,17 @@ class OracleSystem:
         return lib().lo_load_step(self.h, _i(a), _d(dd), _d(ff), int(sym), int(bc_elim), int(max_iter), float(tol),
                                   float(cg_tol), int(cg_maxit), int(max_cuts))
 
+    def apply_disp_bc(self, apply, d):
+        """Relative DispBC: x += d where apply is set; sets the mask there."""
+        a = np.ascontiguousarray(apply, dtype=np.int32).reshape(self.n, 3)
+        dd = np.ascontiguousarray(d, dtype=np.float64).reshape(self.n, 3)
+        lib().lo_apply_disp_bc(self.h, _i(a), _d(dd))
+
+    def add_pex(self, f):
+        """Relative ForceBC: Pex += f."""
+        ff = np.ascontiguousarray(f, dtype=np.float64).reshape(self.n, 3)
+        lib().lo_add_pex(self.h, _d(ff))
+
     def store_state(self):
         lib().lo_store_state(self.h)
 
