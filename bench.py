@@ -251,6 +251,28 @@ def force_assembly_rate(g, capi, reps, local):
     return out
 
 
+def adjoint_cost(g, capi, w, cg_tol, local):
+    """Device time of one lpm_backward_step at the converged state: the
+    gradient of the top face's z reaction with respect to every bond's Kn and
+    Tv (adjoint CG on the exact Jacobian, FP64)."""
+    import numpy as np
+    import torch
+    c = np.zeros((g.n, 3))
+    c[w["top"], 2] = 1.0
+    stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
+    g.backward_step(dJdpin=c, cg_tol=cg_tol)  # buffers, warm
+    g.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    gk, gt, iters, relres = g.backward_step(dJdpin=c, cg_tol=cg_tol)
+    e1.record(stream)
+    e1.synchronize()
+    return {"ms": e0.elapsed_time(e1), "cg_iters": int(iters), "relres": relres, "cg_tol": cg_tol,
+            "response": "reaction of the top face along z", "parameters": "Kn and Tv of every directed bond",
+            "precision": "FP64 (exact Jacobian, matrix-free)"}
+
+
 def force_bytes(nb, n):
     """Algorithmic bytes of one force pass: per directed bond the partner
     index, dis0, dLp, bdamage, Kn, Tv and the bond force written; per
@@ -438,6 +460,8 @@ def run_gb300(args):
                         "spmv_fp64_gflops": 2 * nblk * 9 / (avg64 * 1e-3) / 1e9,
                         "mixed_speedup": value / fv}
         f["handle"].close()
+    adj = adjoint_cost(g, capi, w, args.cg_tol, local)
+    line["adjoint"] = dict(adj, relative_to_forward_step=adj["ms"] / (t_mixed * 1e3 / args.steps))
     fa = force_assembly_rate(g, capi, 5, local)
     fb = force_bytes(nb, n)
     line["bonds_per_s"] = {"force": world * nb / (fa["force"] * 1e-3),

@@ -267,6 +267,8 @@ typedef struct {
   int64_t spmv32_launches;
   double spmv32_ms;
   int64_t kernel_launches;
+  int64_t mixed_fallbacks; /* mixed solves that broke down (non-finite FP32 recurrence,
+                              e.g. an indefinite softened tangent) and were re-solved in FP64 */
 } lpm_stats;
 int lpm_get_stats(const lpm_handle* h, lpm_stats* st);
 int lpm_reset_stats(lpm_handle* h);
@@ -342,6 +344,24 @@ int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y);
 int lpm_checkpoint_save(lpm_handle* h, int* id);
 int lpm_checkpoint_restore(lpm_handle* h, int id);
 int lpm_checkpoint_drop(lpm_handle* h, int id);
+
+/* ---- Neighbour search on the device (set-up) ----
+ * Assembly::createBonds (assembly.h:212-234): directed bonds i -> j for
+ * every j != i with distance < 1.01*cutoff1, layer 0 when also below
+ * 1.01*cutoff0, sorted by (i, j), the order createBonds pushes them.  The
+ * distance arithmetic is the reference's, so the result is bit-for-bit its
+ * O(N^2) search, found through a uniform cell grid.  xyz: N*3 host array.
+ * With p2 == NULL only *nb is returned; otherwise p1/p2/layer must hold
+ * capacity entries (LPM_ERR_ARG with *nb set when they do not).  p1 may be
+ * NULL.  Runs on the calling thread's current device. */
+int lpm_find_bonds(int n, const double* xyz, double cutoff0, double cutoff1, int64_t capacity, int* p1, int* p2,
+                   int* layer, int64_t* nb);
+/* Assembly::searchNonlocalNeighbors (assembly.h:117-130): for every
+ * particle i the ids j (ascending, i itself included) with distance <
+ * radius[i] (= cutoff_ratio * nonlocal_L of particle i), as CSR ptr[N+1] /
+ * idx[total].  With idx == NULL only *total is returned. */
+int lpm_find_neighbors(int n, const double* xyz, const double* radius, int64_t capacity, int64_t* ptr, int* idx,
+                       int64_t* total);
 
 /* Allocation-free Jacobi-CG solve.  No counterpart in the reference: it is
  * for callers that cannot allocate device memory while they solve (a stream

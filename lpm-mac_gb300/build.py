@@ -13,7 +13,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liblpmgpu.so")
-SOURCES = ["lpm_capi.cu", "lpm_force.cu", "lpm_tangent.cu", "lpm_cg.cu", "lpm_laws.cu", "lpm_noalloc.cu", "lpm_adjoint.cu"]
+SOURCES = ["lpm_capi.cu", "lpm_force.cu", "lpm_tangent.cu", "lpm_cg.cu", "lpm_laws.cu", "lpm_noalloc.cu", "lpm_adjoint.cu", "lpm_search.cu"]
 HEADERS = ["lpm_internal.cuh", "lpm_device.cuh", "lpm_cgvec.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

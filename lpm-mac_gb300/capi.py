@@ -37,7 +37,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("cg_iters_total", ctypes.c_int64), ("refine_sweeps", ctypes.c_int64),
                 ("spmv_launches", ctypes.c_int64), ("spmv_ms", ctypes.c_double),
                 ("spmv32_launches", ctypes.c_int64), ("spmv32_ms", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64)]
+                ("kernel_launches", ctypes.c_int64), ("mixed_fallbacks", ctypes.c_int64)]
 
 
 class BC(ctypes.Structure):
@@ -125,6 +125,8 @@ def load(build_if_needed=True):
         "lpm_set_kernel_timing": [H, ctypes.c_int],
         "lpm_get_stream": [H, ctypes.POINTER(ctypes.c_void_p)],
         "lpm_synchronize": [H],
+        "lpm_find_bonds": [ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, i64, ip, ip, ip, i64p],
+        "lpm_find_neighbors": [ctypes.c_int, dp, dp, i64, i64p, ip, i64p],
         "lpm_fatigue_cycle": [H, ctypes.POINTER(BC), ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                               ctypes.c_int, ctypes.c_double, ctypes.POINTER(StepOpts), ctypes.POINTER(CycleResult)],
         "lpm_backward_step": [H, dp, dp, ctypes.c_double, i64, ctypes.c_int, dp, dp, ctypes.POINTER(AdjointResult)],
@@ -152,7 +154,7 @@ def exported_symbols():
             "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
             "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
-            "lpm_fatigue_cycle", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
+            "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
             "lpm_checkpoint_drop"]
 
 
@@ -162,6 +164,48 @@ def set_device(device):
     st = L.lpm_set_device(int(device))
     if st != OK:
         raise LpmError(st, L.lpm_last_error(None).decode())
+
+
+def find_bonds(xyz, cell):
+    """Directed bonds (p1, p2, layer) of the createBonds rule, searched on
+    the GPU (lpm_find_bonds); the same arrays as lattice.find_bonds."""
+    L = load()
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    nb = ctypes.c_int64()
+    null = ctypes.POINTER(ctypes.c_int)()
+    st = L.lpm_find_bonds(n, _d(x), float(cell.neighbor_cutoff[0]), float(cell.neighbor_cutoff[1]), 0, null, null,
+                          null, ctypes.byref(nb))
+    if st != OK:
+        raise LpmError(st, L.lpm_last_error(None).decode())
+    p1 = np.zeros(nb.value, np.int32)
+    p2 = np.zeros(nb.value, np.int32)
+    layer = np.zeros(nb.value, np.int32)
+    st = L.lpm_find_bonds(n, _d(x), float(cell.neighbor_cutoff[0]), float(cell.neighbor_cutoff[1]), nb.value, _i(p1),
+                          _i(p2), _i(layer), ctypes.byref(nb))
+    if st != OK:
+        raise LpmError(st, L.lpm_last_error(None).decode())
+    return p1, p2, layer
+
+
+def find_neighbors(xyz, radius):
+    """Nonlocal neighbour lists (searchNonlocalNeighbors) on the GPU: CSR
+    (ptr, idx) of the ids closer than radius (scalar or per particle)."""
+    L = load()
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    r = np.ascontiguousarray(np.broadcast_to(np.asarray(radius, dtype=np.float64), (n,)))
+    tot = ctypes.c_int64()
+    ptr = np.zeros(n + 1, np.int64)
+    null = ctypes.POINTER(ctypes.c_int)()
+    st = L.lpm_find_neighbors(n, _d(x), _d(r), 0, _l(ptr), null, ctypes.byref(tot))
+    if st != OK:
+        raise LpmError(st, L.lpm_last_error(None).decode())
+    idx = np.zeros(tot.value, np.int32)
+    st = L.lpm_find_neighbors(n, _d(x), _d(r), tot.value, _l(ptr), _i(idx), ctypes.byref(tot))
+    if st != OK:
+        raise LpmError(st, L.lpm_last_error(None).decode())
+    return ptr, idx
 
 
 def _d(a):

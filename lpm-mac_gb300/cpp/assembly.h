@@ -48,28 +48,31 @@ class Assembly {
     for (auto x : p_xyz) pt_sys.push_back(newParticle(x[0], x[1], x[2], cell, -1));
   }
 
-  // Assembly::createBonds (assembly.h:212-234) with a cell list in place of
-  // the all-pairs loop: the same distance arithmetic and cut-offs, bonds in
-  // ascending partner id per particle.
+  // Assembly::createBonds (assembly.h:212-234), searched on the device
+  // (lpm_find_bonds: a cell grid with the reference's distance arithmetic,
+  // bonds in ascending partner id per particle)
   void createBonds() {
     const int n = (int)pt_sys.size();
     if (!n) return;
     const UnitCell& c = pt_sys[0]->cell;
-    const double r1 = 1.01 * c.neighbor_cutoff[1], r0 = 1.01 * c.neighbor_cutoff[0];
-    std::vector<std::vector<int>> near = neighbourLists(r1);
-    for (int i = 0; i < n; ++i) {
-      Particle<nlayer>* p1 = pt_sys[(size_t)i];
-      for (int j : near[(size_t)i]) {
-        Particle<nlayer>* p2 = pt_sys[(size_t)j];
-        double distance = p1->distanceTo(p2);
-        if (distance < r1 && p1->id != p2->id) {
-          int layer = distance < r0 ? 0 : 1;
-          p1->bond_layers[layer].push_back(new Bond<nlayer>(p1, p2, layer, distance));
-          p1->neighbors.push_back(p2);
-        }
-      }
-      p1->nb = (int)p1->neighbors.size();
+    std::vector<double> x(3 * (size_t)n);
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) x[3 * (size_t)i + k] = pt_sys[(size_t)i]->xyz[(size_t)k];
+    int64_t nb = 0;
+    lpm_check(lpm_find_bonds(n, x.data(), c.neighbor_cutoff[0], c.neighbor_cutoff[1], 0, nullptr, nullptr, nullptr,
+                             &nb),
+              "lpm_find_bonds");
+    std::vector<int> p1((size_t)nb), p2((size_t)nb), layer((size_t)nb);
+    lpm_check(lpm_find_bonds(n, x.data(), c.neighbor_cutoff[0], c.neighbor_cutoff[1], nb, p1.data(), p2.data(),
+                             layer.data(), &nb),
+              "lpm_find_bonds");
+    for (int64_t b = 0; b < nb; ++b) {
+      Particle<nlayer>* a = pt_sys[(size_t)p1[(size_t)b]];
+      Particle<nlayer>* q = pt_sys[(size_t)p2[(size_t)b]];
+      a->bond_layers[layer[(size_t)b]].push_back(new Bond<nlayer>(a, q, layer[(size_t)b], a->distanceTo(q)));
+      a->neighbors.push_back(q);
     }
+    for (Particle<nlayer>* p : pt_sys) p->nb = (int)p->neighbors.size();
   }
 
   // Assembly::updateConnections (assembly.h:236-266), on the host.  The
@@ -92,17 +95,23 @@ class Assembly {
     }
   }
 
-  // Assembly::searchNonlocalNeighbors (assembly.h:117-130), cell list
+  // Assembly::searchNonlocalNeighbors (assembly.h:117-130) on the device
   void searchNonlocalNeighbors(double cutoff_ratio) {
-    double rmax = 0;
-    for (Particle<nlayer>* p : pt_sys) rmax = std::max(rmax, cutoff_ratio * p->nonlocal_L);
-    std::vector<std::vector<int>> near = neighbourLists(rmax);
-    for (size_t i = 0; i < pt_sys.size(); ++i) {
-      Particle<nlayer>* p1 = pt_sys[i];
-      for (int j : near[i])
-        if (p1->distanceTo(pt_sys[(size_t)j]) < cutoff_ratio * (p1->nonlocal_L))
-          p1->neighbors_nonlocal.push_back(pt_sys[(size_t)j]);
+    const int n = (int)pt_sys.size();
+    if (!n) return;
+    std::vector<double> x(3 * (size_t)n), r((size_t)n);
+    for (int i = 0; i < n; ++i) {
+      for (int k = 0; k < 3; ++k) x[3 * (size_t)i + k] = pt_sys[(size_t)i]->xyz[(size_t)k];
+      r[(size_t)i] = cutoff_ratio * (pt_sys[(size_t)i]->nonlocal_L);
     }
+    std::vector<int64_t> ptr((size_t)n + 1);
+    int64_t total = 0;
+    lpm_check(lpm_find_neighbors(n, x.data(), r.data(), 0, ptr.data(), nullptr, &total), "lpm_find_neighbors");
+    std::vector<int> idx((size_t)total);
+    lpm_check(lpm_find_neighbors(n, x.data(), r.data(), total, ptr.data(), idx.data(), &total), "lpm_find_neighbors");
+    for (int i = 0; i < n; ++i)
+      for (int64_t q = ptr[(size_t)i]; q < ptr[(size_t)i + 1]; ++q)
+        pt_sys[(size_t)i]->neighbors_nonlocal.push_back(pt_sys[(size_t)idx[(size_t)q]]);
     g_->nonlocal_dirty = true;
   }
 
@@ -319,47 +328,6 @@ class Assembly {
   void header(FILE* f, int step) {
     fprintf(f, "ITEM: TIMESTEP\n%d\nITEM: NUMBER OF ATOMS\n%d\nITEM: BOX BOUNDS pp pp pp\n", step, nparticle);
     fprintf(f, "%8.8f %8.8f\n%8.8f %8.8f\n%8.8f %8.8f\n", box[0], box[1], box[2], box[3], box[4], box[5]);
-  }
-
-  // candidate partners within r of each particle (ascending ids), from a
-  // uniform cell list; exact distances are tested by the callers
-  std::vector<std::vector<int>> neighbourLists(double r) {
-    const int n = (int)pt_sys.size();
-    std::vector<std::vector<int>> out((size_t)n);
-    if (!n || r <= 0) return out;
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (Particle<nlayer>* p : pt_sys)
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = std::min(lo[k], p->xyz[(size_t)k]);
-        hi[k] = std::max(hi[k], p->xyz[(size_t)k]);
-      }
-    const double h = r * 1.0000001;
-    long long dims[3];
-    for (int k = 0; k < 3; ++k) dims[k] = std::max(1LL, (long long)((hi[k] - lo[k]) / h) + 1);
-    auto cell_of = [&](const std::array<double, NDIM>& x, long long* c) {
-      for (int k = 0; k < 3; ++k) c[k] = std::min(dims[k] - 1, (long long)((x[(size_t)k] - lo[k]) / h));
-    };
-    std::map<long long, std::vector<int>> cells;
-    for (int i = 0; i < n; ++i) {
-      long long c[3];
-      cell_of(pt_sys[(size_t)i]->xyz, c);
-      cells[(c[2] * dims[1] + c[1]) * dims[0] + c[0]].push_back(i);
-    }
-    for (int i = 0; i < n; ++i) {
-      long long c[3];
-      cell_of(pt_sys[(size_t)i]->xyz, c);
-      std::vector<int>& o = out[(size_t)i];
-      for (long long dz = -1; dz <= 1; ++dz)
-        for (long long dy = -1; dy <= 1; ++dy)
-          for (long long dx = -1; dx <= 1; ++dx) {
-            long long x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
-            if (x < 0 || y < 0 || z < 0 || x >= dims[0] || y >= dims[1] || z >= dims[2]) continue;
-            auto it = cells.find((z * dims[1] + y) * dims[0] + x);
-            if (it != cells.end()) o.insert(o.end(), it->second.begin(), it->second.end());
-          }
-      std::sort(o.begin(), o.end());
-    }
-    return out;
   }
 
   void attach() {

@@ -41,75 +41,135 @@ __device__ __forceinline__ void load_v(const double* __restrict__ v, int dim, in
   o[2] = dim == 3 ? v[(int64_t)dim * i + 2] : 0.0;
 }
 
-// Pass 1 of H v: per particle, the per-layer sums of d dLe over its bonds,
-// then d f of each of its bonds.
-__global__ void k_jvp_bonds(int n, int dim, const int64_t* __restrict__ bptr, const int* __restrict__ bp2,
-                            const int* __restrict__ blayer, const double* __restrict__ cs,
-                            const double* __restrict__ bdamage, const double* __restrict__ Kn,
-                            const double* __restrict__ Tv, const double* __restrict__ v, double* __restrict__ dfb,
-                            const CgScalars* cg) {
+// H v runs over a sliced copy of the bond data made once per adjoint
+// (k_jac_slots, k_jac_prep): slices of 32 consecutive particles, bond k of
+// particle i at slot jbase[i/32] + 32 k + i%32, so that one thread per
+// particle reads its bonds with the 32 threads of a warp on consecutive
+// slots.  Each slot holds what the product needs at the fixed state: the
+// partner, the slot of the opposite bond, the layer, the direction cosines
+// and the folded constants 2 w Kn, 2 w Tv and F/dis (F the mean bond force).
+// Broken bonds and padding slots hold zeros (padding points at the particle
+// itself), so every slot is processed without a branch.
+__global__ void k_jac_slots(int n, const int64_t* __restrict__ bptr, const int64_t* __restrict__ jbase,
+                            int* __restrict__ slot_of) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t s0 = jbase[i / 32] + (i % 32);
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) slot_of[b] = (int)(s0 + 32 * (b - bptr[i]));
+}
+
+__global__ void k_jac_prep(int n, const int64_t* __restrict__ bptr, const int64_t* __restrict__ jbase,
+                           const int* __restrict__ slot_of, const int* __restrict__ bp2,
+                           const int* __restrict__ blayer, const int* __restrict__ opp, const double* __restrict__ cs,
+                           const double* __restrict__ dis, const double* __restrict__ bdamage,
+                           const double* __restrict__ bforce, const double* __restrict__ Kn,
+                           const double* __restrict__ Tv, int* __restrict__ jp2, int* __restrict__ jopp,
+                           int* __restrict__ jlayer, double* __restrict__ jc, double* __restrict__ jk,
+                           double* __restrict__ jt, double* __restrict__ jf, int64_t nslot) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sl = i / 32;
+  const int len = (int)((jbase[sl + 1] - jbase[sl]) / 32);
+  const int64_t s0 = jbase[sl] + (i % 32);
+  const int nb = (int)(bptr[i + 1] - bptr[i]);
+  for (int k = 0; k < len; ++k) {
+    const int64_t s = s0 + 32 * (int64_t)k;
+    if (k < nb && !is_broken(bdamage[bptr[i] + k])) {
+      const int64_t b = bptr[i] + k;
+      const double w = 1.0 - bdamage[b];
+      jp2[s] = bp2[b];
+      jopp[s] = slot_of[opp[b]];
+      jlayer[s] = blayer[b];
+      jc[s] = cs[3 * b];
+      jc[nslot + s] = cs[3 * b + 1];
+      jc[2 * nslot + s] = cs[3 * b + 2];
+      jk[s] = 2.0 * w * Kn[b];
+      jt[s] = 2.0 * w * Tv[b];
+      jf[s] = 0.5 * (bforce[b] + bforce[opp[b]]) / dis[b];
+    } else {
+      jp2[s] = i;
+      jopp[s] = (int)s;
+      jlayer[s] = 0;
+      jc[s] = jc[nslot + s] = jc[2 * nslot + s] = 0.0;
+      jk[s] = jt[s] = jf[s] = 0.0;
+    }
+  }
+}
+
+struct JacView {
+  const int64_t* __restrict__ jbase;
+  const int* __restrict__ jp2;
+  const int* __restrict__ jopp;
+  const int* __restrict__ jlayer;
+  const double* __restrict__ jc;
+  const double* __restrict__ jk;
+  const double* __restrict__ jt;
+  const double* __restrict__ jf;
+  double* __restrict__ jd;  // d dLe, then d f, per slot
+  int64_t nslot;
+};
+
+// Pass 1 of H v: d dLe per slot and the per-layer sums d D_i^l, then d f.
+__global__ void k_jvp_bonds(int n, int dim, JacView J, const double* __restrict__ v, const CgScalars* cg) {
   if (cg && cg->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const int sl = i / 32;
+  const int len = (int)((J.jbase[sl + 1] - J.jbase[sl]) / 32);
+  const int64_t s0 = J.jbase[sl] + (i % 32);
   double vi[3];
   load_v(v, dim, i, vi);
-  const int64_t b0 = bptr[i], b1 = bptr[i + 1];
   double dD0 = 0.0, dD1 = 0.0;
-  for (int64_t b = b0; b < b1; ++b) {
-    if (is_broken(bdamage[b])) continue;
+  for (int k = 0; k < len; ++k) {
+    const int64_t s = s0 + 32 * (int64_t)k;
     double vj[3];
-    load_v(v, dim, bp2[b], vj);
-    const double dd = cs[3 * b] * (vi[0] - vj[0]) + cs[3 * b + 1] * (vi[1] - vj[1]) + cs[3 * b + 2] * (vi[2] - vj[2]);
-    if (blayer[b] == 0)
+    load_v(v, dim, J.jp2[s], vj);
+    const double dd = J.jc[s] * (vi[0] - vj[0]) + J.jc[J.nslot + s] * (vi[1] - vj[1]) +
+                      J.jc[2 * J.nslot + s] * (vi[2] - vj[2]);
+    J.jd[s] = dd;
+    if (J.jlayer[s] == 0)
       dD0 += dd;
     else
       dD1 += dd;
   }
-  for (int64_t b = b0; b < b1; ++b) {
-    if (is_broken(bdamage[b])) {
-      dfb[b] = 0.0;
-      continue;
-    }
-    double vj[3];
-    load_v(v, dim, bp2[b], vj);
-    const double dd = cs[3 * b] * (vi[0] - vj[0]) + cs[3 * b + 1] * (vi[1] - vj[1]) + cs[3 * b + 2] * (vi[2] - vj[2]);
-    dfb[b] = (1.0 - bdamage[b]) * (2.0 * Kn[b] * dd + 2.0 * Tv[b] * (blayer[b] == 0 ? dD0 : dD1));
+  for (int k = 0; k < len; ++k) {
+    const int64_t s = s0 + 32 * (int64_t)k;
+    J.jd[s] = J.jk[s] * J.jd[s] + J.jt[s] * (J.jlayer[s] == 0 ? dD0 : dD1);
   }
 }
 
 // Pass 2 of H v: y_i = d Pin_i (zero on constrained DOFs when `mask` is
 // given).  With `cg` set it also forms p.q over the grid and, in the last
 // block, alpha = (r.z) / (p.q) for the CG update.
-__global__ void __launch_bounds__(256) k_jvp_particles(int n, int dim, const int64_t* __restrict__ bptr,
-                                                       const int* __restrict__ bp2, const int* __restrict__ opp,
-                                                       const double* __restrict__ cs, const double* __restrict__ dis,
-                                                       const double* __restrict__ bdamage,
-                                                       const double* __restrict__ bforce,
-                                                       const double* __restrict__ dfb, const double* __restrict__ v,
+__global__ void __launch_bounds__(256) k_jvp_particles(int n, int dim, JacView J, const double* __restrict__ v,
                                                        const int* __restrict__ mask, double* __restrict__ y,
                                                        CgScalars* cg, double* partials, unsigned int* ticket) {
   if (cg && cg->done) return;
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int sl = i / 32;
+    const int len = (int)((J.jbase[sl + 1] - J.jbase[sl]) / 32);
+    const int64_t s0 = J.jbase[sl] + (i % 32);
     double vi[3];
     load_v(v, dim, i, vi);
-    double P[3] = {0.0, 0.0, 0.0};
-    for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
-      if (is_broken(bdamage[b])) continue;
+    double P0 = 0.0, P1 = 0.0, P2 = 0.0;
+    for (int k = 0; k < len; ++k) {
+      const int64_t s = s0 + 32 * (int64_t)k;
       double vj[3];
-      load_v(v, dim, bp2[b], vj);
-      const double c0 = cs[3 * b], c1 = cs[3 * b + 1], c2 = cs[3 * b + 2];
+      load_v(v, dim, J.jp2[s], vj);
+      const double c0 = J.jc[s], c1 = J.jc[J.nslot + s], c2 = J.jc[2 * J.nslot + s];
       const double u0 = vi[0] - vj[0], u1 = vi[1] - vj[1], u2 = vi[2] - vj[2];
       const double dd = c0 * u0 + c1 * u1 + c2 * u2;
-      const double rd = 1.0 / dis[b];
-      const int o = opp[b];
-      const double F = 0.5 * (bforce[b] + bforce[o]);
-      const double dF = 0.5 * (dfb[b] + dfb[o]);
-      P[0] += (u0 - c0 * dd) * rd * F + c0 * dF;
-      P[1] += (u1 - c1 * dd) * rd * F + c1 * dF;
-      P[2] += (u2 - c2 * dd) * rd * F + c2 * dF;
+      const double rf = J.jf[s];
+      const double dF = 0.5 * (J.jd[s] + J.jd[J.jopp[s]]);
+      P0 += (u0 - c0 * dd) * rf + c0 * dF;
+      P1 += (u1 - c1 * dd) * rf + c1 * dF;
+      P2 += (u2 - c2 * dd) * rf + c2 * dF;
     }
-    for (int k = 0; k < dim; ++k) {
+    const double P[3] = {P0, P1, P2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (k >= dim) break;
       const double yk = (mask && mask[3 * i + k]) ? 0.0 : P[k];
       y[(int64_t)dim * i + k] = yk;
       acc += vi[k] * yk;
@@ -219,7 +279,7 @@ int adjoint_buffers(lpm_handle* h) {
       *v = (double*)dev_alloc(h, sizeof(double) * std::max<size_t>(m, 1));
       if (!*v) return LPM_ERR_NOMEM;
     }
-  double** bvecs[3] = {&d.adj_dfb, &d.adj_gkn, &d.adj_gtv};
+  double** bvecs[2] = {&d.adj_gkn, &d.adj_gtv};
   for (double** v : bvecs)
     if (!*v) {
       *v = (double*)zeros_dev(h, sizeof(double) * std::max<size_t>((size_t)h->nb, 1));
@@ -232,22 +292,66 @@ int adjoint_buffers(lpm_handle* h) {
   return LPM_OK;
 }
 
+// Sliced bond data of the Jacobian at the current state (layout once per
+// handle, values on every call).
+static int jacobian_prepare(lpm_handle* h) {
+  Dev& d = h->d;
+  const int n = h->n;
+  if (!d.jbase) {
+    std::vector<int64_t> bptr((size_t)n + 1);
+    LPM_CUDA(h, cudaMemcpy(bptr.data(), d.bptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost));
+    const int nsl = (n + 31) / 32;
+    std::vector<int64_t> jb((size_t)nsl + 1, 0);
+    for (int sl = 0; sl < nsl; ++sl) {
+      int64_t mx = 0;
+      for (int i = sl * 32; i < std::min(n, sl * 32 + 32); ++i) mx = std::max(mx, bptr[(size_t)i + 1] - bptr[(size_t)i]);
+      jb[(size_t)sl + 1] = jb[(size_t)sl] + 32 * mx;
+    }
+    h->jslots = jb[(size_t)nsl];
+    if (h->jslots >= ((int64_t)1 << 31)) {
+      h->err = "adjoint: 2^31 or more bond slots";
+      return LPM_ERR_ARG;
+    }
+    d.jbase = (int64_t*)dev_alloc(h, sizeof(int64_t) * jb.size());
+    d.jslot_of = (int*)dev_alloc(h, sizeof(int) * std::max<size_t>((size_t)h->nb, 1));
+    const size_t S = (size_t)std::max<int64_t>(h->jslots, 1);
+    d.jp2 = (int*)dev_alloc(h, sizeof(int) * S);
+    d.jopp = (int*)dev_alloc(h, sizeof(int) * S);
+    d.jlayer = (int*)dev_alloc(h, sizeof(int) * S);
+    d.jc = (double*)dev_alloc(h, sizeof(double) * 3 * S);
+    d.jk = (double*)dev_alloc(h, sizeof(double) * S);
+    d.jt = (double*)dev_alloc(h, sizeof(double) * S);
+    d.jf = (double*)dev_alloc(h, sizeof(double) * S);
+    d.jd = (double*)dev_alloc(h, sizeof(double) * S);
+    if (!d.jbase || !d.jslot_of || !d.jp2 || !d.jopp || !d.jlayer || !d.jc || !d.jk || !d.jt || !d.jf || !d.jd)
+      return LPM_ERR_NOMEM;
+    LPM_CUDA(h, cudaMemcpy(d.jbase, jb.data(), sizeof(int64_t) * jb.size(), cudaMemcpyHostToDevice));
+    k_jac_slots<<<grid_for(n, 128), 128, 0, h->stream>>>(n, d.bptr, d.jbase, d.jslot_of);
+    LPM_LAUNCHED(h, "k_jac_slots");
+  }
+  k_jac_prep<<<grid_for(n, 128), 128, 0, h->stream>>>(n, d.bptr, d.jbase, d.jslot_of, d.bp2, d.blayer, d.opp, d.cs,
+                                                      d.dis, d.bdamage, d.bforce, d.Kn, d.Tv, d.jp2, d.jopp,
+                                                      d.jlayer, d.jc, d.jk, d.jt, d.jf, h->jslots);
+  LPM_LAUNCHED(h, "k_jac_prep");
+  return LPM_OK;
+}
+
 // y = H v (mask: zero the constrained rows); with cg, p.q and alpha too.
 static int apply_jacobian(lpm_handle* h, const double* v, double* y, bool masked, CgScalars* cg) {
   Dev& d = h->d;
-  const int T = 128;
-  k_jvp_bonds<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, h->dim, d.bptr, d.bp2, d.blayer, d.cs, d.bdamage, d.Kn,
-                                                       d.Tv, v, d.adj_dfb, cg);
+  const JacView J{d.jbase, d.jp2, d.jopp, d.jlayer, d.jc, d.jk, d.jt, d.jf, d.jd, h->jslots};
+  k_jvp_bonds<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, h->dim, J, v, cg);
   LPM_LAUNCHED(h, "k_jvp_bonds");
   k_jvp_particles<<<grid_for(h->n, 256, kMaxRedBlocks), 256, 0, h->stream>>>(
-      h->n, h->dim, d.bptr, d.bp2, d.opp, d.cs, d.dis, d.bdamage, d.bforce, d.adj_dfb, v, masked ? d.mask : nullptr, y,
-      cg, d.red.partials, d.red.ticket + 8);
+      h->n, h->dim, J, v, masked ? d.mask : nullptr, y, cg, d.red.partials, d.red.ticket + 8);
   LPM_LAUNCHED(h, "k_jvp_particles");
   return LPM_OK;
 }
 
 int adjoint_apply(lpm_handle* h, const double* v_dev, double* y_dev) {
   int st = adjoint_buffers(h);
+  if (st) return st;
+  st = jacobian_prepare(h);
   if (st) return st;
   return apply_jacobian(h, v_dev, y_dev, false, nullptr);
 }
@@ -270,6 +374,8 @@ int adjoint_step(lpm_handle* h, const double* a_dev, const double* c_dev, double
     h->err = "adjoint: partially or one-sidedly damaged bonds make the Jacobian non-symmetric";
     return LPM_ERR_STATE;
   }
+  st = jacobian_prepare(h);
+  if (st) return st;
   // g = a + H c on the free DOFs
   const int TV = 256;
   if (c_dev) {

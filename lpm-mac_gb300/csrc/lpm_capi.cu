@@ -530,8 +530,13 @@ int lpm_solve(lpm_handle* h, int precision, double tol, int64_t maxit, int64_t* 
   int st;
   if (precision == LPM_PREC_FP64)
     st = solve_fp64(h, tol, maxit, &it, &rr);
-  else if (precision == LPM_PREC_MIXED)
+  else if (precision == LPM_PREC_MIXED) {
     st = solve_mixed(h, tol, maxit, &it, &rr);
+    if (st == LPM_ERR_NONFINITE) {  // FP32 recurrence broke down: the FP64 iteration decides
+      h->stats.mixed_fallbacks++;
+      st = solve_fp64(h, tol, maxit, &it, &rr);
+    }
+  }
   else
     return arg_error(h, "bad precision");
   if (iters) *iters = it;

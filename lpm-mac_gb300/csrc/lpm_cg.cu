@@ -89,12 +89,26 @@ __device__ __forceinline__ void row_product(const SellView& v, const float* __re
   for (int k = 0; k < DIM; ++k) pi[k] = __ldg(&p[(int64_t)row * DIM + k]);
   const int ng = (v.rowlen[row] + kVec - 1) / kVec;
   const int64_t base = sell_row_base(v.sell_ptr, row);
+  // software pipeline: the next group's column indices and values are in
+  // flight while the current group is multiplied
+  int4 c4n = make_int4(0, 0, 0, 0);
+  float4 an[DIM * DIM];
+  if (ng > 0) {
+    c4n = __ldg(reinterpret_cast<const int4*>(v.scol + base));
+#pragma unroll
+    for (int e = 0; e < DIM * DIM; ++e) an[e] = __ldcs(reinterpret_cast<const float4*>(A + e * v.nslots + base));
+  }
   for (int g = 0; g < ng; ++g) {
-    const int64_t s0 = base + (int64_t)g * (kSlice * kVec);
-    const int4 c4 = __ldg(reinterpret_cast<const int4*>(v.scol + s0));
+    const int4 c4 = c4n;
     float4 a[DIM * DIM];
 #pragma unroll
-    for (int e = 0; e < DIM * DIM; ++e) a[e] = __ldcs(reinterpret_cast<const float4*>(A + e * v.nslots + s0));
+    for (int e = 0; e < DIM * DIM; ++e) a[e] = an[e];
+    if (g + 1 < ng) {
+      const int64_t s1 = base + (int64_t)(g + 1) * (kSlice * kVec);
+      c4n = __ldg(reinterpret_cast<const int4*>(v.scol + s1));
+#pragma unroll
+      for (int e = 0; e < DIM * DIM; ++e) an[e] = __ldcs(reinterpret_cast<const float4*>(A + e * v.nslots + s1));
+    }
 #pragma unroll
     for (int t = 0; t < kVec; ++t) {
       const int64_t c = (int64_t)comp(c4, t) * DIM;
@@ -188,13 +202,34 @@ __global__ void k_invd(int n, const int* __restrict__ diag_slot, const double* _
 
 constexpr double kDelta = 0.1;  // reliable-update trigger: |r| < kDelta * max |r| since the last update
 
-// Mixed solve set-up: r32 = r64 = b, x32 = 0, p32 = M r32, |b|^2, r.z.
+// max |b| for the scaling of the mixed solve
+__global__ void k_absmax(int64_t m, const double* __restrict__ b, CgScalars* cg) {
+  unsigned long long mx = 0ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const double a = fabs(b[i]);
+    if (isfinite(a)) mx = max(mx, (unsigned long long)__double_as_longlong(a));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(&cg->bmax_bits, mx);
+}
+
+// Power of two s with s max|b| in [1, 2): the FP32 recurrence then works on
+// values of order one whatever the load magnitude (no FP32 underflow or
+// overflow), and the scaling is exact in FP64.
+__device__ __forceinline__ double rhs_scale(const CgScalars* cg) {
+  const double m = __longlong_as_double((long long)cg->bmax_bits);
+  return m > 0.0 ? ldexp(1.0, -ilogb(m)) : 1.0;
+}
+
+// Mixed solve set-up: r32 = s b, x32 = 0, p32 = M r32, |s b|^2, r.z.
 __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __restrict__ x32,
                           float* __restrict__ r32, float* __restrict__ p32, const float* __restrict__ invd,
                           CgScalars* cg, double tol, long long maxit, double* partials, unsigned int* ticket) {
   double v[2] = {0.0, 0.0};
+  const double sc = rhs_scale(cg);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
-    const double bi = b[i];
+    const double bi = b[i] * sc;
     const float r = (float)bi;
     const float z = invd[i] * r;
     x32[i] = 0.f;
@@ -215,6 +250,7 @@ __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __r
     cg->ru = 0;
     cg->ru_count = 0;
     cg->zcoef = 1.0;
+    cg->bscale = sc;
     cg->rmax = sqrt(tot[0]);
     if (!isfinite(tot[0]) || !isfinite(tot[1]))
       cg->done = 3;
@@ -269,12 +305,14 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
   }
 }
 
-// Reliable update, part 1: x64 += x32, x32 = 0.
+// Reliable update, part 1: x64 += x32, x32 = 0.  The final fold (force)
+// also undoes the right-hand-side scaling.
 __global__ void k_mx_fold(int64_t ndof, float* __restrict__ x32, double* __restrict__ x64, const CgScalars* cg,
                           int force) {
   if (!force && (cg->done || !cg->ru)) return;
+  const double unscale = force ? 1.0 / cg->bscale : 1.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
-    x64[i] += (double)x32[i];
+    x64[i] = (x64[i] + (double)x32[i]) * unscale;
     x32[i] = 0.f;
   }
 }
@@ -288,12 +326,13 @@ __global__ void __launch_bounds__(256) k_mx_residual(SellView v, const double* _
                                                      unsigned int* ticket) {
   if (cg->done || !cg->ru) return;
   double acc = 0.0;
+  const double sc = cg->bscale;
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < v.n; row += gridDim.x * blockDim.x) {
     double y[DIM];
     row_product<DIM>(v, A, x, row, y);
 #pragma unroll
     for (int c = 0; c < DIM; ++c) {
-      const double ri = b[(int64_t)row * DIM + c] - y[c];
+      const double ri = b[(int64_t)row * DIM + c] * sc - y[c];
       r[(int64_t)row * DIM + c] = ri;
       acc += ri * ri;
     }
@@ -488,6 +527,9 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   int st = prepare_invd(h, true);
   if (st) return st;
   LPM_CUDA(h, cudaMemsetAsync(d.x64, 0, sizeof(double) * ndof, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(&d.cg->bmax_bits, 0, sizeof(unsigned long long), h->stream));
+  k_absmax<<<GV, 256, 0, h->stream>>>(ndof, d.rhs, d.cg);
+  LPM_LAUNCHED(h, "k_absmax");
   k_mx_init<<<GV, 256, 0, h->stream>>>(ndof, d.rhs, d.x32, d.r32, d.p32, d.invd32, d.cg, tol, maxit, d.red.partials,
                                        d.red.ticket + 2);
   LPM_LAUNCHED(h, "k_mx_init");

@@ -48,6 +48,8 @@ struct CgScalars {
   double rmax;        // mixed solve: largest |r| since the last reliable update
   long long ru_count; // mixed solve: reliable updates taken
   double zcoef;       // mixed solve: p = zcoef z + beta p (1 except right after an update)
+  unsigned long long bmax_bits;  // mixed solve: bits of max |b| (non-negative doubles order as integers)
+  double bscale;      // mixed solve: power of two that brings max |b| to [1, 2)
 };
 
 // Deterministic grid reductions: each block writes a partial, the last block
@@ -117,8 +119,12 @@ struct Dev {
   // adjoint: response weights a, c; CG vectors; mu = c - lambda; d f per
   // bond; parameter gradients per bond; a device flag
   double *adj_a, *adj_c, *adj_g, *adj_lam, *adj_r, *adj_p, *adj_q, *adj_invd, *adj_mu;
-  double *adj_dfb, *adj_gkn, *adj_gtv;
+  double *adj_gkn, *adj_gtv;
   int* adj_flag;
+  // adjoint: sliced bond data of the exact Jacobian (32 particles per slice)
+  int64_t* jbase;
+  int *jslot_of, *jp2, *jopp, *jlayer;
+  double *jc, *jk, *jt, *jf, *jd;
 };
 
 // One device-resident copy of a step's state (lpm_checkpoint_save).
@@ -157,6 +163,7 @@ struct lpm_handle {
   size_t ev_used = 0;
   std::vector<void*> allocations;
   std::vector<lpm::Checkpoint> checkpoints;
+  int64_t jslots = 0;  // adjoint: slots of the sliced bond data
 };
 
 namespace lpm {

@@ -34,7 +34,7 @@ def test_sent_softening_steps_match_oracle(precision):
     g.update()
     c = xyz[:, 1]
     bottom, top = np.where(c < c.min() + 1e-9)[0], np.where(c > c.max() - 1e-9)[0]
-    du = 5.0e-4
+    du = 2.5e-4  # damage grows from step 3; the ligament bursts at step 7
     apply = np.zeros((n, 3), np.int32)
     dd = np.zeros((n, 3))
     apply[bottom, 1] = 1
@@ -47,7 +47,7 @@ def test_sent_softening_steps_match_oracle(precision):
     # same equilibrium within the Newton tolerance
     tol_u, tol_d = (1e-8, 1e-7) if precision == capi.PREC_FP64 else (1e-5, 1e-4)
     damaged_steps = 0
-    for step in range(8):
+    for step in range(7):
         ro = o.load_step(apply, dd, sym=1, bc_elim=2, max_iter=60, tol=1e-9, cg_tol=1e-12)
         rg = g.load_step(bcs, solver=capi.SOLVER_STATIC_ELIMINATE, tangent=capi.TANGENT_SYMMETRIC,
                          precision=precision, max_iter=60, tol=1e-9, cg_tol=1e-12)
