@@ -47,10 +47,22 @@ struct SellView {
   const int64_t* __restrict__ sell_ptr;
   const int* __restrict__ scol;
   const int* __restrict__ rowlen;
-  const float* __restrict__ S;  // block row sums (FP32 difference-form product only)
+  const float* __restrict__ S;     // block row sums (FP32 difference-form product only)
+  const short* __restrict__ soff;  // column - row per slot when every offset fits 16 bits (FP32 product)
   int64_t nslots;
   int n;
 };
+
+// Four column indices of a group of slots: 16-bit offsets from the row
+// (8 bytes a group) when they fit, else the 32-bit columns (16 bytes).
+template <bool OFF16>
+__device__ __forceinline__ int4 group_cols(const SellView& v, int row, int64_t s) {
+  if (OFF16) {
+    const short4 o = __ldg(reinterpret_cast<const short4*>(v.soff + s));
+    return make_int4(row + o.x, row + o.y, row + o.z, row + o.w);
+  }
+  return __ldg(reinterpret_cast<const int4*>(v.scol + s));
+}
 
 __device__ __forceinline__ int comp(const int4& v, int t) { return t == 0 ? v.x : t == 1 ? v.y : t == 2 ? v.z : v.w; }
 __device__ __forceinline__ float comp(const float4& v, int t) {
@@ -71,6 +83,45 @@ __device__ __forceinline__ void dot2_acc(float& s, float& c, float a, float b) {
   c = __fadd_rn(c, __fadd_rn(pe, se));
 }
 
+// (s, c) += (x, xc) for double-float pairs: TwoSum of the leading parts,
+// the rounding error and the trailing parts kept in c.
+__device__ __forceinline__ void df_add(float& s, float& c, float x, float xc) {
+  const float t = __fadd_rn(s, x);
+  const float z = __fsub_rn(t, s);
+  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(xc, e));
+}
+
+// Block sum of per-thread double-float partials, result in thread 0 as
+// FP64.  The warp stage stays in FP32 pairs (GB300 runs FP32 at many times
+// its FP64 rate, and a butterfly of FP64 adds over every thread of a large
+// grid costs microseconds); only one value per warp is converted.
+template <int K>
+__device__ __forceinline__ void block_df_sum(float (&s)[K], float (&c)[K], double (&out)[K]) {
+  __shared__ double sm[K][32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const float so = __shfl_xor_sync(0xffffffffu, s[k], o), co = __shfl_xor_sync(0xffffffffu, c[k], o);
+      df_add(s[k], c[k], so, co);
+    }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) sm[k][warp] = (double)s[k] + (double)c[k];
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double a = 0.0;
+      for (int w = 0; w < nw; ++w) a += sm[k][w];
+      out[k] = a;
+    }
+}
+
 // y = row `row` of A times p (FP32), in difference form with compensated
 // accumulation: the sum comes out as if accumulated in twice the precision
 // and then rounded, so the only FP32 errors left are in the differences
@@ -78,9 +129,9 @@ __device__ __forceinline__ void dot2_acc(float& s, float& c, float a, float b) {
 // own rounding.  The row is walked in groups of four blocks: one 16-byte load
 // brings a block element for four blocks.  Padding blocks are zero and point
 // at the row itself.
-template <int DIM>
-__device__ __forceinline__ void row_product(const SellView& v, const float* __restrict__ A,
-                                            const float* __restrict__ p, int row, float (&y)[DIM]) {
+template <int DIM, bool OFF16>
+__device__ __forceinline__ void row_product32(const SellView& v, const float* __restrict__ A,
+                                              const float* __restrict__ p, int row, float (&y)[DIM]) {
   float sc[DIM], cc[DIM];
 #pragma unroll
   for (int r = 0; r < DIM; ++r) sc[r] = cc[r] = 0.f;
@@ -94,7 +145,7 @@ __device__ __forceinline__ void row_product(const SellView& v, const float* __re
   int4 c4n = make_int4(0, 0, 0, 0);
   float4 an[DIM * DIM];
   if (ng > 0) {
-    c4n = __ldg(reinterpret_cast<const int4*>(v.scol + base));
+    c4n = group_cols<OFF16>(v, row, base);
 #pragma unroll
     for (int e = 0; e < DIM * DIM; ++e) an[e] = __ldcs(reinterpret_cast<const float4*>(A + e * v.nslots + base));
   }
@@ -105,7 +156,7 @@ __device__ __forceinline__ void row_product(const SellView& v, const float* __re
     for (int e = 0; e < DIM * DIM; ++e) a[e] = an[e];
     if (g + 1 < ng) {
       const int64_t s1 = base + (int64_t)(g + 1) * (kSlice * kVec);
-      c4n = __ldg(reinterpret_cast<const int4*>(v.scol + s1));
+      c4n = group_cols<OFF16>(v, row, s1);
 #pragma unroll
       for (int e = 0; e < DIM * DIM; ++e) an[e] = __ldcs(reinterpret_cast<const float4*>(A + e * v.nslots + s1));
     }
@@ -133,9 +184,12 @@ __device__ __forceinline__ void row_product(const SellView& v, const float* __re
 // FP64: the partner values of the four blocks are gathered first; then each
 // element's 32-byte run (four blocks) is read as two back-to-back 16-byte
 // loads, so both halves of a sector are used by the same instruction pair.
-template <int DIM>
+// With ADD32 the product is taken of p + p32 (an FP64 vector plus an FP32
+// increment not yet folded into it).
+template <int DIM, bool ADD32 = false>
 __device__ __forceinline__ void row_product(const SellView& v, const double* __restrict__ A,
-                                            const double* __restrict__ p, int row, double (&y)[DIM]) {
+                                            const double* __restrict__ p, int row, double (&y)[DIM],
+                                            const float* __restrict__ p32 = nullptr) {
 #pragma unroll
   for (int r = 0; r < DIM; ++r) y[r] = 0.0;
   const int ng = (v.rowlen[row] + kVec - 1) / kVec;
@@ -148,7 +202,7 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
     for (int t = 0; t < kVec; ++t) {
       const int64_t c = (int64_t)comp(c4, t) * DIM;
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) pc[t][k] = __ldg(&p[c + k]);
+      for (int k = 0; k < DIM; ++k) pc[t][k] = ADD32 ? __ldg(&p[c + k]) + (double)__ldg(&p32[c + k]) : __ldg(&p[c + k]);
     }
 #pragma unroll
     for (int r = 0; r < DIM; ++r)
@@ -165,23 +219,39 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
   }
 }
 
-template <typename T, int DIM>
+template <typename T, int DIM, bool OFF16 = false>
 __global__ void __launch_bounds__(256) k_cg_spmv(SellView v, const T* __restrict__ A, const T* __restrict__ p,
                                                  T* __restrict__ q, CgScalars* cg, double* partials,
                                                  unsigned int* ticket) {
   if (cg->done) return;
   double acc = 0.0;
+  float ps = 0.f, pc = 0.f;  // FP32: p.q as a compensated double-float sum
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < v.n; row += gridDim.x * blockDim.x) {
     T y[DIM];
-    row_product<DIM>(v, A, p, row, y);
+    if constexpr (sizeof(T) == 4)
+      row_product32<DIM, OFF16>(v, A, p, row, y);
+    else
+      row_product<DIM>(v, A, p, row, y);
 #pragma unroll
     for (int r = 0; r < DIM; ++r) {
       q[(int64_t)row * DIM + r] = y[r];
-      acc += (double)p[(int64_t)row * DIM + r] * (double)y[r];
+      if constexpr (sizeof(T) == 4)
+        dot2_acc(ps, pc, (float)p[(int64_t)row * DIM + r], (float)y[r]);
+      else
+        acc += (double)p[(int64_t)row * DIM + r] * (double)y[r];
     }
   }
-  double w[1] = {acc}, tot[1];
-  if (grid_sum<1>(w, partials, ticket, tot) && threadIdx.x == 0) cg->alpha = cg->abs_new / tot[0];
+  double w[1], tot[1];
+  bool last;
+  if constexpr (sizeof(T) == 4) {
+    float s1[1] = {ps}, c1[1] = {pc};
+    block_df_sum<1>(s1, c1, w);
+    last = grid_fold<1>(w, partials, ticket, tot);
+  } else {
+    w[0] = acc;
+    last = grid_sum<1>(w, partials, ticket, tot);
+  }
+  if (last && threadIdx.x == 0) cg->alpha = cg->abs_new / tot[0];
 }
 
 // Jacobi preconditioner from the diagonal blocks of A (= diagonal of K).
@@ -272,19 +342,20 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
                                                    unsigned int* ticket) {
   if (cg->done) return;
   const float alpha = (float)cg->alpha;
-  // per-thread partials in FP32 (a handful of terms each), folded in FP64
-  float f0 = 0.f, f1 = 0.f;
+  // |r|^2 and r.z as compensated double-float sums, FP64 only per warp
+  float s[2] = {0.f, 0.f}, c[2] = {0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
     const float ri = r[i] - alpha * q[i];
     x[i] = x[i] + alpha * p[i];
     r[i] = ri;
     const float zi = invd[i] * ri;
-    f0 = fmaf(ri, ri, f0);
-    f1 = fmaf(ri, zi, f1);
+    dot2_acc(s[0], c[0], ri, ri);
+    dot2_acc(s[1], c[1], ri, zi);
   }
-  double v[2] = {(double)f0, (double)f1};
+  double v[2];
+  block_df_sum<2>(s, c, v);
   double tot[2];
-  if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
+  if (grid_fold<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
     cg->rr = tot[0];
     cg->it += 1;
     if (!isfinite(tot[0]) || !isfinite(tot[1])) {
@@ -305,31 +376,29 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
   }
 }
 
-// Reliable update, part 1: x64 += x32, x32 = 0.  The final fold (force)
-// also undoes the right-hand-side scaling.
-__global__ void k_mx_fold(int64_t ndof, float* __restrict__ x32, double* __restrict__ x64, const CgScalars* cg,
-                          int force) {
-  if (!force && (cg->done || !cg->ru)) return;
-  const double unscale = force ? 1.0 / cg->bscale : 1.0;
+// End of the solve: x64 += x32 (what the last iterations added), x32 = 0,
+// and the right-hand-side scaling undone.
+__global__ void k_mx_fold(int64_t ndof, float* __restrict__ x32, double* __restrict__ x64, const CgScalars* cg) {
+  const double unscale = 1.0 / cg->bscale;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
     x64[i] = (x64[i] + (double)x32[i]) * unscale;
     x32[i] = 0.f;
   }
 }
 
-// Reliable update, part 2: r64 = b - A64 x64 and |r64|^2; converged when it
-// is below the threshold.
+// Reliable update, part 1: r64 = s b - A64 (x64 + x32) and |r64|^2;
+// converged when it is below the threshold.
 template <int DIM>
 __global__ void __launch_bounds__(256) k_mx_residual(SellView v, const double* __restrict__ A,
-                                                     const double* __restrict__ x, const double* __restrict__ b,
-                                                     double* __restrict__ r, CgScalars* cg, double* partials,
-                                                     unsigned int* ticket) {
+                                                     const double* __restrict__ x, const float* __restrict__ x32,
+                                                     const double* __restrict__ b, double* __restrict__ r,
+                                                     CgScalars* cg, double* partials, unsigned int* ticket) {
   if (cg->done || !cg->ru) return;
   double acc = 0.0;
   const double sc = cg->bscale;
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < v.n; row += gridDim.x * blockDim.x) {
     double y[DIM];
-    row_product<DIM>(v, A, x, row, y);
+    row_product<DIM, true>(v, A, x, row, y, x32);
 #pragma unroll
     for (int c = 0; c < DIM; ++c) {
       const double ri = b[(int64_t)row * DIM + c] * sc - y[c];
@@ -348,16 +417,18 @@ __global__ void __launch_bounds__(256) k_mx_residual(SellView v, const double* _
   }
 }
 
-// Reliable update, part 3: r32 = r64, new r.z and beta, reset the maximum.
-// The replaced residual is no longer orthogonal to the last search
-// direction; the next direction is formed from p - (r.p / r.z) z, which
-// restores r.p = 0, i.e. p_new = (1 - beta gamma) z + beta p.
+// Reliable update, part 2: x64 += x32, x32 = 0, r32 = r64, new r.z and
+// beta, reset the maximum.  The replaced residual is no longer orthogonal to
+// the last search direction; the next direction is formed from
+// p - (r.p / r.z) z, which restores r.p = 0, i.e. p_new = (1 - beta gamma) z + beta p.
 __global__ void k_mx_replace(int64_t ndof, const double* __restrict__ r64, float* __restrict__ r32,
-                             const float* __restrict__ p32, const float* __restrict__ invd, CgScalars* cg,
-                             double* partials, unsigned int* ticket) {
+                             float* __restrict__ x32, double* __restrict__ x64, const float* __restrict__ p32,
+                             const float* __restrict__ invd, CgScalars* cg, double* partials, unsigned int* ticket) {
   if (cg->done || !cg->ru) return;
   double v[2] = {0.0, 0.0};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
+    x64[i] += (double)x32[i];
+    x32[i] = 0.f;
     const float r = (float)r64[i];
     r32[i] = r;
     v[0] += (double)r * (double)(invd[i] * r);
@@ -389,7 +460,8 @@ __global__ void __launch_bounds__(256) k_mx_pupdate(int64_t ndof, const float* _
 // reduction partials (and the result bits) do not depend on the row count.
 int row_grid(lpm_handle* h) { return grid_for((long long)h->n, 256, kMaxRedBlocks); }
 SellView sell_view(lpm_handle* h) {
-  return SellView{h->d.sell_ptr, h->d.scol, h->d.rowlen, h->d.S32, h->nslots, h->n};
+  return SellView{h->d.sell_ptr, h->d.scol, h->d.rowlen, h->d.S32, h->soff16_ok ? h->d.soff16 : nullptr, h->nslots,
+                  h->n};
 }
 int vec_grid(long long m) { return grid_for(m, 256, kMaxRedBlocks); }
 
@@ -544,9 +616,15 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
         e1 = next_event(h);
         if (e0) cudaEventRecord(e0, h->stream);
       }
-      if (dim == 3)
+      if (dim == 3 && sv.soff)
+        k_cg_spmv<float, 3, true><<<GR, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials,
+                                                             d.red.ticket + 3);
+      else if (dim == 3)
         k_cg_spmv<float, 3><<<GR, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials,
                                                        d.red.ticket + 3);
+      else if (sv.soff)
+        k_cg_spmv<float, 2, true><<<GR, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials,
+                                                             d.red.ticket + 3);
       else
         k_cg_spmv<float, 2><<<GR, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials,
                                                        d.red.ticket + 3);
@@ -555,16 +633,14 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
       k_mx_update<<<GV, 256, 0, h->stream>>>(ndof, d.x32, d.r32, d.p32, d.q32, d.invd32, d.cg, d.red.partials,
                                              d.red.ticket + 4);
       LPM_LAUNCHED(h, "k_mx_update");
-      k_mx_fold<<<GV, 256, 0, h->stream>>>(ndof, d.x32, d.x64, d.cg, 0);
-      LPM_LAUNCHED(h, "k_mx_fold");
       if (dim == 3)
-        k_mx_residual<3><<<GR, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.rhs, d.r64, d.cg, d.red.partials,
+        k_mx_residual<3><<<GR, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.rhs, d.r64, d.cg, d.red.partials,
                                                     d.red.ticket + 6);
       else
-        k_mx_residual<2><<<GR, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.rhs, d.r64, d.cg, d.red.partials,
+        k_mx_residual<2><<<GR, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.rhs, d.r64, d.cg, d.red.partials,
                                                     d.red.ticket + 6);
       LPM_LAUNCHED(h, "k_mx_residual");
-      k_mx_replace<<<GV, 256, 0, h->stream>>>(ndof, d.r64, d.r32, d.p32, d.invd32, d.cg, d.red.partials,
+      k_mx_replace<<<GV, 256, 0, h->stream>>>(ndof, d.r64, d.r32, d.x32, d.x64, d.p32, d.invd32, d.cg, d.red.partials,
                                               d.red.ticket + 7);
       LPM_LAUNCHED(h, "k_mx_replace");
       k_mx_pupdate<<<GV, 256, 0, h->stream>>>(ndof, d.r32, d.invd32, d.p32, d.cg);
@@ -575,8 +651,8 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
     if (h->h_cg->done) break;
     if (batch < 64) batch *= 2;
   }
-  // fold what the last iterations added (a no-op after a converged update)
-  k_mx_fold<<<GV, 256, 0, h->stream>>>(ndof, d.x32, d.x64, d.cg, 1);
+  // fold what the iterations since the last replacement added
+  k_mx_fold<<<GV, 256, 0, h->stream>>>(ndof, d.x32, d.x64, d.cg);
   LPM_LAUNCHED(h, "k_mx_fold");
   LPM_CUDA(h, cudaMemcpyAsync(d.disp, d.x64, sizeof(double) * ndof, cudaMemcpyDeviceToDevice, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -76,6 +76,41 @@ __device__ __forceinline__ bool grid_sum(double (&v)[K], double* partials, unsig
   return true;
 }
 
+// Grid-wide sum of values already reduced per block (valid in thread 0 of
+// each block): the last-block fold of grid_sum without its block reduction.
+template <int K>
+__device__ __forceinline__ bool grid_fold(const double (&v)[K], double* partials, unsigned int* ticket,
+                                          double (&tot)[K]) {
+  __shared__ bool last;
+  __shared__ double res[K];
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
+    __threadfence();
+    unsigned int t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] += __ldcg(&partials[k * gridDim.x + b]);
+  block_sum<K>(acc);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) res[k] = acc[k];
+    *ticket = 0u;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) tot[k] = res[k];
+  return true;
+}
+
 __device__ __forceinline__ bool is_broken(double bdamage) { return fabs(bdamage - 1.0) < EPS; }
 
 }  // namespace lpm

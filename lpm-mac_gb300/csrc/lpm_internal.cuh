@@ -98,6 +98,7 @@ struct Dev {
   double* A64;
   float* A32;
   float* S32;  // [n * dim * dim] block row sums of A64, rounded (difference-form FP32 product)
+  short* soff16;  // [nslots] column - row of each slot read by the FP32 product, valid when soff16_ok
   // solver vectors (n_dof each)
   double *rhs, *disp, *x64, *r64, *p64, *q64, *invd64;
   float *b32, *x32, *r32, *p32, *q32, *invd32;
@@ -153,6 +154,7 @@ struct lpm_handle {
   int undamaged = -1;  // particle type that skips damage updates
   bool have_K = false;
   bool a32_valid = false;  // FP32 copy of the operator matches A64
+  bool soff16_ok = false;  // every column offset of the pattern fits 16 bits
   int tangent = LPM_TANGENT_AS_WRITTEN;
   // host mirrors
   lpm::CgScalars* h_cg = nullptr;  // pinned

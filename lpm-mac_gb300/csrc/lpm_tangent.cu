@@ -303,6 +303,25 @@ __global__ void k_to_fp32(int64_t m, const double* __restrict__ a, float* __rest
     b[t] = (float)a[t];
 }
 
+// 16-bit column offsets (column - row) of the slots the product reads for
+// row j: its blocks and the padding of its last group of four.  The flag is
+// set when one does not fit; the slots past them are never read.
+__global__ void k_col_offsets(int n, const int64_t* __restrict__ sell_ptr, const int* __restrict__ scol,
+                              const int* __restrict__ rowlen, short* __restrict__ soff, int* flag) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int len = (rowlen[j] + kVec - 1) / kVec * kVec;
+  const int64_t base = sell_row_base(sell_ptr, j);
+  bool bad = false;
+  for (int k = 0; k < len; ++k) {
+    const int64_t s = sell_slot(base, k);
+    const int o = scol[s] - j;
+    bad |= (o < -32768 || o > 32767);
+    soff[s] = (short)o;
+  }
+  if (bad) atomicOr(flag, 1);
+}
+
 // S_i = sum_j A_ij over the blocks of row i, summed in FP64 and rounded once.
 template <int DIM>
 __global__ void k_block_rowsum(int n, const int64_t* __restrict__ sell_ptr, const int* __restrict__ rowlen,
@@ -444,6 +463,19 @@ int convert_A32(lpm_handle* h) {
   if (!d.S32) {
     d.S32 = (float*)dev_alloc(h, sizeof(float) * std::max<size_t>((size_t)h->n * dim * dim, 1));
     if (!d.S32) return LPM_ERR_NOMEM;
+  }
+  if (!d.soff16) {  // the pattern is fixed for the handle: offsets once
+    d.soff16 = (short*)dev_alloc(h, sizeof(short) * std::max<size_t>((size_t)h->nslots, 1));
+    int* flag = (int*)dev_alloc(h, sizeof(int));
+    if (!d.soff16 || !flag) return LPM_ERR_NOMEM;
+    LPM_CUDA(h, cudaMemsetAsync(flag, 0, sizeof(int), h->stream));
+    LPM_CUDA(h, cudaMemsetAsync(d.soff16, 0, sizeof(short) * std::max<size_t>((size_t)h->nslots, 1), h->stream));
+    k_col_offsets<<<(h->n + 127) / 128, 128, 0, h->stream>>>(h->n, d.sell_ptr, d.scol, d.rowlen, d.soff16, flag);
+    LPM_LAUNCHED(h, "k_col_offsets");
+    int bad = 0;
+    LPM_CUDA(h, cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->soff16_ok = bad == 0;
   }
   k_to_fp32<<<grid_for((long long)vals, 256, 152 * 32), 256, 0, h->stream>>>((int64_t)vals, d.A64, d.A32);
   LPM_LAUNCHED(h, "k_to_fp32");
