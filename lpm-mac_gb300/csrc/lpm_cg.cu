@@ -94,12 +94,14 @@ __device__ __forceinline__ void df_add(float& s, float& c, float x, float xc) {
 }
 
 // Block sum of per-thread double-float partials, result in thread 0 as
-// FP64.  The warp stage stays in FP32 pairs (GB300 runs FP32 at many times
-// its FP64 rate, and a butterfly of FP64 adds over every thread of a large
-// grid costs microseconds); only one value per warp is converted.
+// FP64.  Both the warp and the cross-warp stage stay in FP32 pairs: GB300's
+// FP64 pipe takes a whole warp slot even for a one-lane instruction, so an
+// FP64 step per warp over a grid of thousands of warps costs microseconds.
+// One conversion per block remains.
 template <int K>
 __device__ __forceinline__ void block_df_sum(float (&s)[K], float (&c)[K], double (&out)[K]) {
-  __shared__ double sm[K][32];
+  __shared__ float sm[K][2][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -107,19 +109,31 @@ __device__ __forceinline__ void block_df_sum(float (&s)[K], float (&c)[K], doubl
       const float so = __shfl_xor_sync(0xffffffffu, s[k], o), co = __shfl_xor_sync(0xffffffffu, c[k], o);
       df_add(s[k], c[k], so, co);
     }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __syncthreads();
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < K; ++k) sm[k][warp] = (double)s[k] + (double)c[k];
+    for (int k = 0; k < K; ++k) {
+      sm[k][0][warp] = s[k];
+      sm[k][1][warp] = c[k];
+    }
   __syncthreads();
-  if (threadIdx.x == 0)
+  if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      double a = 0.0;
-      for (int w = 0; w < nw; ++w) a += sm[k][w];
-      out[k] = a;
+      s[k] = lane < nw ? sm[k][0][lane] : 0.f;
+      c[k] = lane < nw ? sm[k][1][lane] : 0.f;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const float so = __shfl_xor_sync(0xffffffffu, s[k], o), co = __shfl_xor_sync(0xffffffffu, c[k], o);
+        df_add(s[k], c[k], so, co);
+      }
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < K; ++k) out[k] = (double)s[k] + (double)c[k];
+  }
 }
 
 // y = row `row` of A times p (FP32), in difference form with compensated
@@ -251,7 +265,10 @@ __global__ void __launch_bounds__(256) k_cg_spmv(SellView v, const T* __restrict
     w[0] = acc;
     last = grid_sum<1>(w, partials, ticket, tot);
   }
-  if (last && threadIdx.x == 0) cg->alpha = cg->abs_new / tot[0];
+  if (last && threadIdx.x == 0) {
+    cg->alpha = cg->abs_new / tot[0];
+    cg->alpha32 = (float)cg->alpha;
+  }
 }
 
 // Jacobi preconditioner from the diagonal blocks of A (= diagonal of K).
@@ -320,6 +337,8 @@ __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __r
     cg->ru = 0;
     cg->ru_count = 0;
     cg->zcoef = 1.0;
+    cg->alpha32 = cg->beta32 = 0.f;
+    cg->zcoef32 = 1.f;
     cg->bscale = sc;
     cg->rmax = sqrt(tot[0]);
     if (!isfinite(tot[0]) || !isfinite(tot[1]))
@@ -341,7 +360,7 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
                                                    const float* __restrict__ invd, CgScalars* cg, double* partials,
                                                    unsigned int* ticket) {
   if (cg->done) return;
-  const float alpha = (float)cg->alpha;
+  const float alpha = cg->alpha32;
   // |r|^2 and r.z as compensated double-float sums, FP64 only per warp
   float s[2] = {0.f, 0.f}, c[2] = {0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
@@ -371,6 +390,8 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
       cg->abs_new = tot[1];
       cg->beta = tot[1] / old;
       cg->zcoef = 1.0;
+      cg->beta32 = (float)cg->beta;
+      cg->zcoef32 = 1.f;
     }
     if (cg->it >= cg->maxit) cg->done = 2;
   }
@@ -441,6 +462,8 @@ __global__ void k_mx_replace(int64_t ndof, const double* __restrict__ r64, float
     cg->beta = tot[0] / old;
     const double gamma = tot[0] != 0.0 ? tot[1] / tot[0] : 0.0;
     cg->zcoef = 1.0 - cg->beta * gamma;
+    cg->beta32 = (float)cg->beta;
+    cg->zcoef32 = (float)cg->zcoef;
     cg->rmax = sqrt(cg->rr);
     cg->ru = 0;
   }
@@ -451,7 +474,7 @@ __global__ void __launch_bounds__(256) k_mx_pupdate(int64_t ndof, const float* _
                                                     const float* __restrict__ invd, float* __restrict__ p,
                                                     const CgScalars* cg) {
   if (cg->done) return;
-  const float beta = (float)cg->beta, zc = (float)cg->zcoef;
+  const float beta = cg->beta32, zc = cg->zcoef32;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = zc * (invd[i] * r[i]) + beta * p[i];
 }

@@ -50,6 +50,7 @@ struct CgScalars {
   double zcoef;       // mixed solve: p = zcoef z + beta p (1 except right after an update)
   unsigned long long bmax_bits;  // mixed solve: bits of max |b| (non-negative doubles order as integers)
   double bscale;      // mixed solve: power of two that brings max |b| to [1, 2)
+  float alpha32, beta32, zcoef32;  // mixed solve: FP32 copies, so that the vector kernels convert nothing
 };
 
 // Deterministic grid reductions: each block writes a partial, the last block
