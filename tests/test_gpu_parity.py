@@ -7,7 +7,7 @@ solves and load steps within the tolerances written at each assert.
 import numpy as np
 import pytest
 
-from lpm_cases import (cube, dense_from_bsr, dense_from_csc, golden, golden_meta, gpu_bcs, inputs_from_golden,
+from lpm_cases import (cube, dense_from_bsr, dense_from_csc, golden, golden_meta, gpu_bcs, inputs_from_golden, lat,
                        make_gpu, make_oracle, mask3, oracle, pkg, plate, rel, tension_bcs)
 
 capi = pkg.capi
@@ -237,3 +237,28 @@ def test_isolated_particle():
     assert np.array_equal(cptr, t["cptr"]) and np.array_equal(cidx, t["cidx"])
     assert cptr[-1] == cptr[-2]
     g.close()
+
+
+def test_mixed_solve_with_wide_pattern_uses_32bit_columns():
+    """A particle numbering whose column offsets do not fit 16 bits (a
+    randomly permuted 33^3 cube, 35,937 particles) runs the FP32 product on
+    32-bit column indices; its load step matches the FP64 one within 1e-8."""
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = cube(33)
+    n = len(xyz)
+    xyz = xyz[np.random.default_rng(4).permutation(n)]
+    q1, q2, ql = lat.find_bonds(xyz, cell)
+    Kn, Tv = lat.bond_constants(cell, ql, cell.elastic_constants(200e3, 0.3, layout="row"))
+    groups, _, _ = tension_bcs(xyz, dim, 2e-3)
+    outs = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        g = make_gpu(dim, xyz, q1, q2, ql, Kn, Tv, cell)
+        cptr, cidx = g.pattern()
+        rows = np.repeat(np.arange(n), np.diff(cptr))
+        assert np.abs(cidx - rows).max() > 32767
+        bcs = gpu_bcs(g, groups, dim, 2e-3)
+        g.update()
+        res = g.load_step(bcs, tangent=capi.TANGENT_SYMMETRIC, precision=prec, cg_tol=1e-10)
+        assert res["status"] == 0
+        outs[prec] = g.download(capi.F_XYZ) - xyz
+        g.close()
+    assert rel(outs[capi.PREC_MIXED], outs[capi.PREC_FP64]) <= 1e-8
