@@ -126,6 +126,9 @@ class Assembly {
   // device pass computes both, so either call brings the force state up to
   // date.
   void updateGeometry() { updateForceState(); }
+  // The device force pass without the copy back to the particles, for the
+  // solvers' inner loops; pullParticles() brings the particles up to date.
+  void refreshForceState() { lpm_check(lpm_update_geometry_force(device()), "lpm_update_geometry_force"); }
   void updateForceState() {
     lpm_check(lpm_update_geometry_force(device()), "lpm_update_geometry_force");
     pullParticles();

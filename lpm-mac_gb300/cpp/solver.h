@@ -71,14 +71,19 @@ class Solver {
     }
   }
   // solver.h:108-128: residual on the device; the reaction list from the
-  // particles' internal forces at constrained DOFs
+  // internal forces at constrained DOFs (read from the device, since the
+  // Newton loop does not copy the particles back between iterations)
   void updateRR() {
     lpm_check(lpm_residual(ass.device(), &norm_r_, &norm_R_), "lpm_residual");
     lpm_check(lpm_download(ass.device(), LPM_F_RESIDUAL, stiffness.residual.data()), "lpm_download");
+    pin_.resize(3 * ass.pt_sys.size());
+    lpm_check(lpm_download(ass.device(), LPM_F_PIN, pin_.data()), "lpm_download");
     std::vector<double> temp;
-    for (Particle<nlayer>* pt : ass.pt_sys)
+    for (size_t i = 0; i < ass.pt_sys.size(); ++i) {
+      Particle<nlayer>* pt = ass.pt_sys[i];
       for (int k = 0; k < pt->cell.dim; k++)
-        if (pt->disp_constraint[(size_t)k] == 1) temp.push_back(pt->Pin[(size_t)k]);
+        if (pt->disp_constraint[(size_t)k] == 1) temp.push_back(pin_[3 * i + (size_t)k]);
+    }
     reaction_force.resize((Eigen::Index)temp.size());
     for (size_t i = 0; i < temp.size(); ++i) reaction_force((Eigen::Index)i) = temp[i];
   }
@@ -105,9 +110,20 @@ class Solver {
     if (sol_mode == SolverMode::CG) LPM_CG();
     lpm_check(lpm_move_by_disp(ass.device()), "lpm_move_by_disp");
   }
-  // solver.h:53-89
+  // solver.h:53-89.  The force state stays on the device through the loop;
+  // the particles are brought up to date once, when it returns.
   int NewtonIteration() {
-    ass.updateForceState();  // updateGeometry and updateForceState are one device pass
+    const int ni = newtonLoop();
+    ass.pullParticles();
+    return ni;
+  }
+
+ protected:
+  double norm_r_ = 0, norm_R_ = 0;
+  std::vector<double> pin_;
+
+  int newtonLoop() {
+    ass.refreshForceState();  // updateGeometry and updateForceState are one device pass
     updateRR();
     double norm_residual = norm_r_, norm_reaction_force = norm_R_;
     double tol_multiplier = std::max(norm_residual, norm_reaction_force);
@@ -120,7 +136,7 @@ class Solver {
       if (++ni > max_NR_iter) return max_NR_iter;
       if (v) printf("|  |  Iteration-%d: ", ni);
       solveLinearSystem();
-      ass.updateForceState();
+      ass.refreshForceState();
       updateRR();
       norm_residual = norm_r_;
       if (v)
@@ -129,7 +145,4 @@ class Solver {
     }
     return ni;
   }
-
- protected:
-  double norm_r_ = 0, norm_R_ = 0;
 };
