@@ -178,7 +178,6 @@ def gpu_run(w, args, precision, world, local):
     stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    g.set_kernel_timing(True)
     g.reset_stats()
     newton, cg = [], []
     barrier(world)
@@ -197,8 +196,18 @@ def gpu_run(w, args, precision, world, local):
     barrier(world)
     ms = e0.elapsed_time(e1)
     st = g.stats()
+    # kernel-timing pass: one more step with CUDA events around every
+    # sparse-product launch.  The mixed solve then launches its kernels one by
+    # one from the host instead of as one graph; the product kernel is the same.
+    g.set_kernel_timing(True)
+    g.reset_stats()
+    r = g.load_step(bcs, **opts)
+    g.synchronize()
+    kt = g.stats()
     g.set_kernel_timing(False)
-    out = dict(ms=ms, stats=st, newton=newton, cg=cg, handle=g, bcs=bcs, opts=opts)
+    if r["status"] != 0:
+        raise RuntimeError("kernel-timing step did not converge: %s" % r)
+    out = dict(ms=ms, stats=st, ktime=kt, newton=newton, cg=cg, handle=g, bcs=bcs, opts=opts)
     return out
 
 
@@ -436,8 +445,8 @@ def run_gb300(args):
     e2e_value, _ = aggregate(e2e_s, args.steps, world)
     st = mixed["stats"]
     n, nb, nblk = g.n, g.nb, g.nblk
-    launches = st["spmv32_launches"]
-    avg_ms = st["spmv32_ms"] / max(launches, 1)
+    launches = mixed["ktime"]["spmv32_launches"]
+    avg_ms = mixed["ktime"]["spmv32_ms"] / max(launches, 1)
     byts = spmv_bytes(nblk, n, 3, 4, column_index_bytes(g), row_sums=True)
     peak, peak_kind = measured_peaks()
     achieved = byts / (avg_ms * 1e-3) / 1e9
@@ -456,6 +465,7 @@ def run_gb300(args):
             "roofline": {"kernel": "k_cg_spmv<float,3>", "bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "algorithmic_bytes_per_launch": byts, "avg_launch_ms": avg_ms, "launches": launches,
+                         "launch_timing": "CUDA events around each launch, kernel-timing step after the timed steps",
                          "peak_kind": peak_kind + " (hbm_gbs copy bandwidth)"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}}
     if clk:
@@ -463,7 +473,7 @@ def run_gb300(args):
     if capi.PREC_FP64 in results:
         f = results[capi.PREC_FP64]
         fv, tf = aggregate(f["ms"] / 1e3, args.steps, world)
-        sf = f["stats"]
+        sf = f["ktime"]
         avg64 = sf["spmv_ms"] / max(sf["spmv_launches"], 1)
         b64 = spmv_bytes(nblk, n, 3, 8)
         line["fp64"] = {"value": fv, "ms_per_step": tf * 1e3 / args.steps,

@@ -33,6 +33,7 @@
 // stops on the FP64 residual.  Every update is one FP64 sparse product.
 #include <cfloat>
 #include <cmath>
+#include <tuple>
 
 #include "lpm_cgvec.cuh"
 #include "lpm_device.cuh"
@@ -336,6 +337,7 @@ __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __r
     cg->maxit = maxit;
     cg->ru = 0;
     cg->ru_count = 0;
+    cg->graph_passes = 0;
     cg->zcoef = 1.0;
     cg->alpha32 = cg->beta32 = 0.f;
     cg->zcoef32 = 1.f;
@@ -358,7 +360,7 @@ __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __r
 __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restrict__ x, float* __restrict__ r,
                                                    const float* __restrict__ p, const float* __restrict__ q,
                                                    const float* __restrict__ invd, CgScalars* cg, double* partials,
-                                                   unsigned int* ticket) {
+                                                   unsigned int* ticket, cudaGraphConditionalHandle ru_cond) {
   if (cg->done) return;
   const float alpha = cg->alpha32;
   // |r|^2 and r.z as compensated double-float sums, FP64 only per warp
@@ -379,6 +381,7 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
     cg->it += 1;
     if (!isfinite(tot[0]) || !isfinite(tot[1])) {
       cg->done = 3;
+      if (ru_cond) cudaGraphSetConditional(ru_cond, 0u);
       return;
     }
     const double rn = sqrt(tot[0]);
@@ -394,6 +397,7 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
       cg->zcoef32 = 1.f;
     }
     if (cg->it >= cg->maxit) cg->done = 2;
+    if (ru_cond) cudaGraphSetConditional(ru_cond, cg->ru ? 1u : 0u);
   }
 }
 
@@ -470,9 +474,16 @@ __global__ void k_mx_replace(int64_t ndof, const double* __restrict__ r64, float
 }
 
 // p = zcoef z + beta p with z = M^-1 r (FP32 vectors).
+// Inside the solve graph it is the last kernel of an iteration: block 0
+// sets the loop condition (continue while nothing has ended the solve) and
+// counts the iteration's kernel launches.
 __global__ void __launch_bounds__(256) k_mx_pupdate(int64_t ndof, const float* __restrict__ r,
                                                     const float* __restrict__ invd, float* __restrict__ p,
-                                                    const CgScalars* cg) {
+                                                    CgScalars* cg, cudaGraphConditionalHandle loop_cond) {
+  if (loop_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+    cudaGraphSetConditional(loop_cond, cg->done ? 0u : 1u);
+    cg->graph_passes += 1;
+  }
   if (cg->done) return;
   const float beta = cg->beta32, zc = cg->zcoef32;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x)
@@ -597,6 +608,99 @@ int solve_fp64(lpm_handle* h, double tol, long long maxit, long long* iters, dou
   return err <= tol ? LPM_OK : LPM_NOT_CONVERGED;
 }
 
+namespace {
+
+// A kernel node of a graph: the arguments are converted to the kernel's
+// parameter types and passed by address, as cudaGraphAddKernelNode wants.
+template <typename... P, typename... A>
+cudaError_t add_kernel(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* dep, void (*fn)(P...), int grid,
+                       int block, A... a) {
+  std::tuple<P...> vals(a...);
+  void* params[sizeof...(P) > 0 ? sizeof...(P) : 1];
+  std::apply([&](auto&... x) {
+    int i = 0;
+    ((params[i++] = (void*)&x), ...);
+  }, vals);
+  cudaKernelNodeParams kp = {};
+  kp.func = (void*)fn;
+  kp.gridDim = dim3((unsigned)grid);
+  kp.blockDim = dim3((unsigned)block);
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = params;
+  return cudaGraphAddKernelNode(node, g, dep, dep ? 1 : 0, &kp);
+}
+
+template <int DIM, bool OFF16>
+cudaError_t add_spmv32(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* dep, int GR, const SellView& sv,
+                       const Dev& d) {
+  return add_kernel(node, g, dep, k_cg_spmv<float, DIM, OFF16>, GR, 256, sv, (const float*)d.A32,
+                    (const float*)d.p32, d.q32, d.cg, d.red.partials, d.red.ticket + 3);
+}
+
+// The mixed solve's iteration loop as one graph:
+//   while (loop_cond) { spmv; update; if (ru_cond) { residual; replace } pupdate }
+// update sets ru_cond (a reliable update is due) and pupdate sets
+// loop_cond (the solve goes on), so a whole solve is one graph launch with
+// no host round trip and no launch of an idle reliable-update kernel.
+int build_mixed_graph(lpm_handle* h, const SellView& sv, int GV, int GR) {
+  Dev& d = h->d;
+  const int dim = h->dim;
+  const int64_t ndof = (int64_t)h->n * dim;
+  if (h->mx_exec) cudaGraphExecDestroy(h->mx_exec);
+  if (h->mx_graph) cudaGraphDestroy(h->mx_graph);
+  h->mx_exec = nullptr;
+  h->mx_graph = nullptr;
+  cudaGraph_t g;
+  LPM_CUDA(h, cudaGraphCreate(&g, 0));
+  h->mx_graph = g;
+  cudaGraphConditionalHandle loop_cond, ru_cond;
+  LPM_CUDA(h, cudaGraphConditionalHandleCreate(&loop_cond, g, 1u, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams wp = {};
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = loop_cond;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  cudaGraphNode_t wnode;
+  LPM_CUDA(h, cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
+  LPM_CUDA(h, cudaGraphConditionalHandleCreate(&ru_cond, body, 0u, cudaGraphCondAssignDefault));
+  cudaGraphNode_t n_spmv, n_upd, n_if, n_res, n_rep, n_pup;
+  cudaError_t e;
+  if (dim == 3)
+    e = sv.soff ? add_spmv32<3, true>(&n_spmv, body, nullptr, GR, sv, d)
+                : add_spmv32<3, false>(&n_spmv, body, nullptr, GR, sv, d);
+  else
+    e = sv.soff ? add_spmv32<2, true>(&n_spmv, body, nullptr, GR, sv, d)
+                : add_spmv32<2, false>(&n_spmv, body, nullptr, GR, sv, d);
+  LPM_CUDA(h, e);
+  LPM_CUDA(h, add_kernel(&n_upd, body, &n_spmv, k_mx_update, GV, 256, ndof, d.x32, d.r32, (const float*)d.p32,
+                         (const float*)d.q32, (const float*)d.invd32, d.cg, d.red.partials, d.red.ticket + 4,
+                         ru_cond));
+  cudaGraphNodeParams ip = {};
+  ip.type = cudaGraphNodeTypeConditional;
+  ip.conditional.handle = ru_cond;
+  ip.conditional.type = cudaGraphCondTypeIf;
+  ip.conditional.size = 1;
+  LPM_CUDA(h, cudaGraphAddNode(&n_if, body, &n_upd, nullptr, 1, &ip));
+  cudaGraph_t ifb = ip.conditional.phGraph_out[0];
+  if (dim == 3)
+    e = add_kernel(&n_res, ifb, nullptr, k_mx_residual<3>, GR, 256, sv, (const double*)d.A64, (const double*)d.x64,
+                   (const float*)d.x32, (const double*)d.rhs, d.r64, d.cg, d.red.partials, d.red.ticket + 6);
+  else
+    e = add_kernel(&n_res, ifb, nullptr, k_mx_residual<2>, GR, 256, sv, (const double*)d.A64, (const double*)d.x64,
+                   (const float*)d.x32, (const double*)d.rhs, d.r64, d.cg, d.red.partials, d.red.ticket + 6);
+  LPM_CUDA(h, e);
+  LPM_CUDA(h, add_kernel(&n_rep, ifb, &n_res, k_mx_replace, GV, 256, ndof, (const double*)d.r64, d.r32, d.x32, d.x64,
+                         (const float*)d.p32, (const float*)d.invd32, d.cg, d.red.partials, d.red.ticket + 7));
+  LPM_CUDA(h, add_kernel(&n_pup, body, &n_if, k_mx_pupdate, GV, 256, ndof, (const float*)d.r32,
+                         (const float*)d.invd32, d.p32, d.cg, loop_cond));
+  LPM_CUDA(h, cudaGraphInstantiate(&h->mx_exec, g, 0));
+  h->mx_graph_off16 = sv.soff != nullptr;
+  return LPM_OK;
+}
+
+}  // namespace
+
 int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres) {
   Dev& d = h->d;
   const int dim = h->dim;
@@ -630,8 +734,19 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   LPM_LAUNCHED(h, "k_mx_init");
   const bool timing = h->timing;
   const size_t ev0 = h->ev_used;
+  if (!timing) {
+    // the whole iteration loop as one graph launch
+    if (!h->mx_exec || h->mx_graph_off16 != (sv.soff != nullptr)) {
+      st = build_mixed_graph(h, sv, GV, GR);
+      if (st) return st;
+    }
+    LPM_CUDA(h, cudaGraphLaunch(h->mx_exec, h->stream));
+  }
+  // with kernel timing on, the same kernels launched one by one from the
+  // host, with events around each sparse product; the host reads the device
+  // flag once per batch of iterations
   long long batch = 8;
-  for (;;) {
+  for (; timing;) {
     for (long long k = 0; k < batch; ++k) {
       cudaEvent_t e0 = nullptr, e1 = nullptr;
       if (timing) {
@@ -654,7 +769,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
       LPM_LAUNCHED(h, "k_cg_spmv");
       if (timing && e1) cudaEventRecord(e1, h->stream);
       k_mx_update<<<GV, 256, 0, h->stream>>>(ndof, d.x32, d.r32, d.p32, d.q32, d.invd32, d.cg, d.red.partials,
-                                             d.red.ticket + 4);
+                                             d.red.ticket + 4, 0);
       LPM_LAUNCHED(h, "k_mx_update");
       if (dim == 3)
         k_mx_residual<3><<<GR, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.rhs, d.r64, d.cg, d.red.partials,
@@ -666,7 +781,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
       k_mx_replace<<<GV, 256, 0, h->stream>>>(ndof, d.r64, d.r32, d.x32, d.x64, d.p32, d.invd32, d.cg, d.red.partials,
                                               d.red.ticket + 7);
       LPM_LAUNCHED(h, "k_mx_replace");
-      k_mx_pupdate<<<GV, 256, 0, h->stream>>>(ndof, d.r32, d.invd32, d.p32, d.cg);
+      k_mx_pupdate<<<GV, 256, 0, h->stream>>>(ndof, d.r32, d.invd32, d.p32, d.cg, 0);
       LPM_LAUNCHED(h, "k_mx_pupdate");
     }
     LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
@@ -678,8 +793,10 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   k_mx_fold<<<GV, 256, 0, h->stream>>>(ndof, d.x32, d.x64, d.cg);
   LPM_LAUNCHED(h, "k_mx_fold");
   LPM_CUDA(h, cudaMemcpyAsync(d.disp, d.x64, sizeof(double) * ndof, cudaMemcpyDeviceToDevice, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   const CgScalars& c = *h->h_cg;
+  if (!timing) h->stats.kernel_launches += 3 * c.graph_passes + 2 * c.ru_count;
   if (timing) {
     double ms_sum = 0.0;
     long long used = 0;

@@ -47,6 +47,7 @@ struct CgScalars {
   int ru;             // mixed solve: a reliable update is pending
   double rmax;        // mixed solve: largest |r| since the last reliable update
   long long ru_count; // mixed solve: reliable updates taken
+  long long graph_passes;  // mixed solve: loop passes run by the solve graph
   double zcoef;       // mixed solve: p = zcoef z + beta p (1 except right after an update)
   unsigned long long bmax_bits;  // mixed solve: bits of max |b| (non-negative doubles order as integers)
   double bscale;      // mixed solve: power of two that brings max |b| to [1, 2)
@@ -167,6 +168,10 @@ struct lpm_handle {
   std::vector<void*> allocations;
   std::vector<lpm::Checkpoint> checkpoints;
   int64_t jslots = 0;  // adjoint: slots of the sliced bond data
+  // the mixed solve's iteration loop as a graph with device-side conditions
+  cudaGraph_t mx_graph = nullptr;
+  cudaGraphExec_t mx_exec = nullptr;
+  bool mx_graph_off16 = false;  // which FP32 product the graph launches
 };
 
 namespace lpm {
