@@ -364,9 +364,9 @@ int lpm_find_neighbors(int n, const double* xyz, const double* radius, int64_t c
                        int64_t* total);
 
 /* Allocation-free Jacobi-CG solve.  No counterpart in the reference: it is
- * for callers that cannot allocate device memory while they solve (a stream
- * being captured into a CUDA graph, a real-time loop that reserved its
- * memory up front, a host framework whose allocator owns the device).  The
+ * for callers that cannot allocate device memory while they solve (a
+ * real-time loop that reserved its memory up front, a host framework whose
+ * allocator owns the device).  The
  * caller passes device buffers: the operator in block CSR (ptr[n+1] int64,
  * col[nnz] int32, vals[nnz*dim*dim] row-major blocks, applied as y = A x),
  * the right-hand side b and the solution x (n*dim doubles each).  The
@@ -378,7 +378,9 @@ int lpm_find_neighbors(int n, const double* xyz, const double* radius, int64_t c
  * LPM_ERR_ARG.  The first call on a device looks up that array's address:
  * make it before any stream capture.  All calls share the array, so calls
  * that overlap on the same GPU race.  Runs on `stream` (NULL: the default
- * stream) and returns when the solve is done; iters/relres may be NULL. */
+ * stream) and returns when the solve is done (it synchronises with `stream`
+ * to read the counts back, so the call itself cannot be recorded by stream
+ * capture); iters/relres may be NULL. */
 #define LPM_NOALLOC_MAX_DOF 1048576
 int lpm_cg_solve_noalloc(int dim, int n, const int64_t* ptr, const int* col, const double* vals, const double* b,
                          double* x, double tol, int64_t maxit, void* stream, int64_t* iters, double* relres);

@@ -2,9 +2,11 @@
 // allocate device memory.
 //
 // Who needs it: code that runs inside a region where allocation is not
-// allowed, e.g. a stream being captured into a CUDA graph, a real-time loop
-// that has reserved all its memory up front, or a host framework whose own
-// allocator owns the device and forbids cudaMalloc from libraries.  Such a
+// allowed, e.g. a real-time loop that has reserved all its memory up front,
+// or a host framework whose own allocator owns the device and forbids
+// cudaMalloc from libraries.  The call waits for its stream at the end (it
+// reads the iteration count back), so it cannot itself be recorded by
+// stream capture.  Such a
 // caller allocates its inputs and outputs itself and passes them in; the
 // solver's work vectors and reduction scratch live in one file-scope device
 // array of fixed size (LPM_NOALLOC_MAX_DOF), so no call allocates or frees.

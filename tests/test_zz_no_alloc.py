@@ -1,8 +1,8 @@
 """The allocation-free CG entry point, lpm_cg_solve_noalloc.
 
 It serves callers that cannot allocate device memory while they solve: a
-stream being captured into a CUDA graph, a real-time loop that reserved its
-memory up front, or a host framework whose allocator owns the device.  They
+real-time loop that reserved its memory up front, or a host framework whose
+allocator owns the device.  They
 pass their own device buffers; the solver's scratch is a fixed device array
 inside the library.  This test calls it through the C ABI twice in a row on
 the same device and compares each result with lpm_solve on the same system.
