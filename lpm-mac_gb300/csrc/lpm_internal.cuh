@@ -157,6 +157,7 @@ struct lpm_handle {
   bool have_K = false;
   bool a32_valid = false;  // FP32 copy of the operator matches A64
   bool soff16_ok = false;  // every column offset of the pattern fits 16 bits
+  int sms = 0;             // multiprocessors of the device (looked up on the first mixed solve)
   int tangent = LPM_TANGENT_AS_WRITTEN;
   // host mirrors
   lpm::CgScalars* h_cg = nullptr;  // pinned

@@ -123,6 +123,44 @@ def test_cg_zero_rhs_and_maxit():
     g.close()
 
 
+def test_mixed_solve_graph_matches_host_launched_loop():
+    """The mixed solve's graph (device-set loop and reliable-update
+    conditions) runs the same kernels in the same order as the host-launched
+    loop that kernel timing selects: identical iterates, bit for bit, on a
+    relaunch too; the iteration cap and a zero right-hand side end it."""
+    d = golden("kernels_sc_undamaged")
+    g, dim, n = _gpu_at_golden_state(d)
+    g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_ELIMINATE)
+    g.residual()
+    runs = []
+    for timing in (False, True, False):
+        g.set_kernel_timing(timing)
+        g.reset_stats()
+        it, rr, st = g.solve(capi.PREC_MIXED, 1e-10)
+        s = g.stats()
+        assert st == 0 and rr <= 1e-10 and it > 0
+        runs.append((it, g.download(capi.F_DISP).copy(), s))
+    g.set_kernel_timing(False)
+    for it, x, _ in runs[1:]:
+        assert it == runs[0][0]
+        assert np.array_equal(x, runs[0][1])
+    assert runs[0][2]["refine_sweeps"] == runs[1][2]["refine_sweeps"] > 0
+    # the graph launches the product, the update and the direction update per
+    # iteration, and the two reliable-update kernels only when one is due
+    assert runs[0][2]["kernel_launches"] < runs[1][2]["kernel_launches"]
+    it, rr, st = g.solve(capi.PREC_MIXED, 1e-10, maxit=5)
+    assert st == capi.NOT_CONVERGED and it == 5
+    g.close()
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = cube(4)
+    g = make_gpu(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    g.update()
+    g.residual()  # zero: undeformed, no loads
+    g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_NONE)
+    it, rr, st = g.solve(capi.PREC_MIXED, 1e-10)
+    assert it == 0 and st == 0 and not np.any(g.download(capi.F_DISP))
+    g.close()
+
+
 @pytest.mark.parametrize("name,rtol", [("steps_hex_fatigue", 1e-9), ("steps_sc_fatigue", 1e-6), ("config1_hex", 1e-9)])
 def test_load_steps_as_written_match_reference(name, rtol):
     """SolverFatigue static steps (as-written tangent, BC elimination, FP64
