@@ -401,7 +401,7 @@ int adjoint_step(lpm_handle* h, const double* a_dev, const double* c_dev, double
       k_cg_update<double><<<GV, 256, 0, h->stream>>>(m, d.adj_lam, d.adj_r, d.adj_p, d.adj_q, d.adj_invd, d.cg,
                                                      d.red.partials, d.red.ticket + 4);
       LPM_LAUNCHED(h, "k_cg_update");
-      k_cg_pupdate<double><<<GV, 256, 0, h->stream>>>(m, d.adj_r, d.adj_invd, d.adj_p, d.cg);
+      k_cg_pupdate<double><<<GV, 256, 0, h->stream>>>(m, d.adj_r, d.adj_invd, d.adj_p, d.cg, 0);
       LPM_LAUNCHED(h, "k_cg_pupdate");
     }
     LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));

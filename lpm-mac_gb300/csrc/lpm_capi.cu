@@ -263,6 +263,8 @@ int lpm_destroy(lpm_handle* h) {
   for (auto& c : h->checkpoints) cudaFree(c.buf);
   for (auto& g : h->groups) cudaFree(g.ids);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  if (h->fp_exec) cudaGraphExecDestroy(h->fp_exec);
+  if (h->fp_graph) cudaGraphDestroy(h->fp_graph);
   if (h->mx_exec) cudaGraphExecDestroy(h->mx_exec);
   if (h->mx_graph) cudaGraphDestroy(h->mx_graph);
   if (h->h_cg) cudaFreeHost(h->h_cg);

@@ -11,11 +11,12 @@
 //   k_cg_spmv    q = A p and p.q; the last block sets alpha
 //   k_cg_update  x, r, |r|^2, r.z; the last block tests convergence, sets beta
 //   k_cg_pupdate p = z + beta p
-// Kernels return at once when the device flag `done` is set, so the host
-// enqueues iterations in batches and reads the flag once per batch.  The
-// mixed solve instead runs its whole loop as one CUDA graph whose loop and
-// reliable-update conditions are set on the device (build_mixed_graph),
-// except under kernel timing, where it launches from the host as above.
+// Kernels return at once when the device flag `done` is set.  Each solve
+// runs its whole loop as one CUDA graph whose loop condition (and, for the
+// mixed solve, reliable-update condition) is set on the device
+// (build_fp64_graph, build_mixed_graph); under kernel timing the host
+// enqueues the iterations in batches instead and reads the flag once per
+// batch.
 //
 // Mixed precision: the same recurrence on an FP32 copy of A with FP32
 // vectors and FP64 dot accumulation.  The FP32 product is taken in
@@ -529,6 +530,9 @@ cudaEvent_t next_event(lpm_handle* h) {
   return h->ev_pool[h->ev_used++];
 }
 
+int build_fp64_graph(lpm_handle* h, const double* A, const double* b, double* x, double* r, double* p, double* q,
+                     const double* invd, int GV, int GR, const SellView& sv);
+
 // Runs the CG iteration on the given operator/vectors.  Returns the device
 // `done` code through h->h_cg.
 template <typename T>
@@ -542,6 +546,21 @@ int run_cg(lpm_handle* h, const T* A, const T* b, T* x, T* r, T* p, T* q, const 
                                           d.red.ticket + 2);
   LPM_LAUNCHED(h, "k_cg_init");
   const bool timing = h->timing;
+  if constexpr (sizeof(T) == 8) {
+    if (!timing) {  // the whole iteration loop as one graph launch
+      if (!h->fp_exec || h->fp_graph_x != (const void*)x) {
+        const int st = build_fp64_graph(h, A, b, x, r, p, q, invd, GV, GR, sv);
+        if (st) return st;
+      }
+      LPM_CUDA(h, cudaGraphLaunch(h->fp_exec, h->stream));
+      LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
+      LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+      h->stats.kernel_launches += 3 * h->h_cg->graph_passes;
+      return LPM_OK;
+    }
+  }
+  // host-launched loop (kernel timing on): events around each product; the
+  // host reads the device flag once per batch of iterations
   const size_t ev0 = h->ev_used;
   long long batch = 8;
   for (;;) {
@@ -560,7 +579,7 @@ int run_cg(lpm_handle* h, const T* A, const T* b, T* x, T* r, T* p, T* q, const 
       if (timing && e1) cudaEventRecord(e1, h->stream);
       k_cg_update<T><<<GV, 256, 0, h->stream>>>(ndof, x, r, p, q, invd, d.cg, d.red.partials, d.red.ticket + 4);
       LPM_LAUNCHED(h, "k_cg_update");
-      k_cg_pupdate<T><<<GV, 256, 0, h->stream>>>(ndof, r, invd, p, d.cg);
+      k_cg_pupdate<T><<<GV, 256, 0, h->stream>>>(ndof, r, invd, p, d.cg, 0);
       LPM_LAUNCHED(h, "k_cg_pupdate");
     }
     LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
@@ -737,6 +756,47 @@ int build_mixed_graph(lpm_handle* h, const SellView& sv, const MixedGrids& mg) {
                          (const float*)d.invd32, d.p32, d.cg, loop_cond));
   LPM_CUDA(h, cudaGraphInstantiate(&h->mx_exec, g, 0));
   h->mx_graph_off16 = sv.soff != nullptr;
+  return LPM_OK;
+}
+
+// The FP64 solve's iteration loop as one graph:
+//   while (loop_cond) { spmv; update; pupdate }
+// with pupdate setting loop_cond once update has decided (converged,
+// iteration cap or non-finite).
+int build_fp64_graph(lpm_handle* h, const double* A, const double* b, double* x, double* r, double* p, double* q,
+                     const double* invd, int GV, int GR, const SellView& sv) {
+  Dev& d = h->d;
+  const int64_t ndof = (int64_t)h->n * h->dim;
+  if (h->fp_exec) cudaGraphExecDestroy(h->fp_exec);
+  if (h->fp_graph) cudaGraphDestroy(h->fp_graph);
+  h->fp_exec = nullptr;
+  h->fp_graph = nullptr;
+  h->fp_graph_x = nullptr;
+  cudaGraph_t g;
+  LPM_CUDA(h, cudaGraphCreate(&g, 0));
+  h->fp_graph = g;
+  cudaGraphConditionalHandle loop_cond;
+  LPM_CUDA(h, cudaGraphConditionalHandleCreate(&loop_cond, g, 1u, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams wp = {};
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = loop_cond;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  cudaGraphNode_t wnode, n_spmv, n_upd, n_pup;
+  LPM_CUDA(h, cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
+  if (h->dim == 3)
+    LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, k_cg_spmv<double, 3>, GR, 256, sv, A, (const double*)p, q, d.cg,
+                           d.red.partials, d.red.ticket + 3));
+  else
+    LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, k_cg_spmv<double, 2>, GR, 256, sv, A, (const double*)p, q, d.cg,
+                           d.red.partials, d.red.ticket + 3));
+  LPM_CUDA(h, add_kernel(&n_upd, body, &n_spmv, k_cg_update<double>, GV, 256, ndof, x, r, (const double*)p,
+                         (const double*)q, invd, d.cg, d.red.partials, d.red.ticket + 4));
+  LPM_CUDA(h, add_kernel(&n_pup, body, &n_upd, k_cg_pupdate<double>, GV, 256, ndof, (const double*)r, invd, p, d.cg,
+                         loop_cond));
+  LPM_CUDA(h, cudaGraphInstantiate(&h->fp_exec, g, 0));
+  h->fp_graph_x = x;
   return LPM_OK;
 }
 

@@ -51,7 +51,14 @@ __global__ void __launch_bounds__(256) k_cg_update(int64_t ndof, T* __restrict__
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_cg_pupdate(int64_t ndof, const T* __restrict__ r, const T* __restrict__ invd,
-                                                    T* __restrict__ p, const CgScalars* cg) {
+                                                    T* __restrict__ p, CgScalars* cg,
+                                                    cudaGraphConditionalHandle loop_cond) {
+  // inside a solve graph, the last kernel of an iteration: block 0 sets the
+  // loop condition and counts the pass
+  if (loop_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+    cudaGraphSetConditional(loop_cond, cg->done ? 0u : 1u);
+    cg->graph_passes += 1;
+  }
   if (cg->done) return;
   const T beta = (T)cg->beta;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x)
@@ -82,6 +89,7 @@ __global__ void k_cg_init(int64_t ndof, const T* __restrict__ b, T* __restrict__
     cg->beta = 0.0;
     cg->it = 0;
     cg->maxit = maxit;
+    cg->graph_passes = 0;
     if (!isfinite(tot[0]) || !isfinite(tot[1]))
       cg->done = 3;
     else if (tot[0] == 0.0 || tot[0] < cg->threshold)

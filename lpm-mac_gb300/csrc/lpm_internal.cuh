@@ -169,6 +169,10 @@ struct lpm_handle {
   std::vector<void*> allocations;
   std::vector<lpm::Checkpoint> checkpoints;
   int64_t jslots = 0;  // adjoint: slots of the sliced bond data
+  // the FP64 solve's iteration loop as a graph (for the solution vector fp_graph_x)
+  cudaGraph_t fp_graph = nullptr;
+  cudaGraphExec_t fp_exec = nullptr;
+  const void* fp_graph_x = nullptr;
   // the mixed solve's iteration loop as a graph with device-side conditions
   cudaGraph_t mx_graph = nullptr;
   cudaGraphExec_t mx_exec = nullptr;

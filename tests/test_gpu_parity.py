@@ -161,6 +161,27 @@ def test_mixed_solve_graph_matches_host_launched_loop():
     g.close()
 
 
+def test_fp64_solve_graph_matches_host_launched_loop():
+    """The FP64 solve's graph and its host-launched loop give the same
+    iterates, bit for bit; the iteration cap ends the graph too."""
+    d = golden("kernels_sc_undamaged")
+    g, dim, n = _gpu_at_golden_state(d)
+    g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_ELIMINATE)
+    g.residual()
+    runs = []
+    for timing in (False, True, False):
+        g.set_kernel_timing(timing)
+        it, rr, st = g.solve(capi.PREC_FP64, 1e-10)
+        assert st == 0 and rr <= 1e-10 and it > 0
+        runs.append((it, g.download(capi.F_DISP).copy()))
+    g.set_kernel_timing(False)
+    for it, x in runs[1:]:
+        assert it == runs[0][0] and np.array_equal(x, runs[0][1])
+    it, rr, st = g.solve(capi.PREC_FP64, 1e-10, maxit=7)
+    assert st == capi.NOT_CONVERGED and it == 7
+    g.close()
+
+
 @pytest.mark.parametrize("name,rtol", [("steps_hex_fatigue", 1e-9), ("steps_sc_fatigue", 1e-6), ("config1_hex", 1e-9)])
 def test_load_steps_as_written_match_reference(name, rtol):
     """SolverFatigue static steps (as-written tangent, BC elimination, FP64
