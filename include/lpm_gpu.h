@@ -273,7 +273,9 @@ typedef struct {
 int lpm_get_stats(const lpm_handle* h, lpm_stats* st);
 int lpm_reset_stats(lpm_handle* h);
 /* Records CUDA events around every CG sparse-product launch (on the
- * handle's stream) so that lpm_get_stats reports its device time. */
+ * handle's stream) so that lpm_get_stats reports its device time.  While it
+ * is on, the solves launch their iterations one by one from the host instead
+ * of as one CUDA graph (same kernels, same results). */
 int lpm_set_kernel_timing(lpm_handle* h, int on);
 /* The handle's CUDA stream (cudaStream_t), for callers that time or order
  * work around the library. */
