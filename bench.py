@@ -20,6 +20,12 @@ Reported (one JSON line on rank 0):
                copy bandwidth
   cpu_baseline the CPU oracle (a restatement of the reference algorithm) on
                the host cores, bounded sample extrapolated to a full step
+  adjoint      one backward step (gradient of a reaction with respect to
+               every bond's constants), in ms and relative to a forward step
+  bonds_per_s  the force pass alone and with the tangent assembly
+  setup        the GPU bond search (checked identical to the CPU
+               generator's bonds) and the creation of the device lattice
+  fatigue      compact-tension fatigue cycles at full size (configuration 5)
 
 --impl reference times the CPU oracle alone on the same workload.
 Multi-GPU runs are independent replicas (the path has no exchange step).
@@ -63,12 +69,15 @@ def workload(n, a=0.2, E=200e3, nu=0.3):
     lat = ge.load_package().lattice
     cell = lat.UnitCell(lat.SIMPLECUBIC3D, a / 2)
     xyz = lat.sc_cuboid(n, n, n, a)
+    t0 = time.perf_counter()
     p1, p2, layer = lat.find_bonds(xyz, cell)
+    t_bonds = time.perf_counter() - t0
     Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(E, nu, layout="row"))
     z = xyz[:, 2]
     bottom = np.where(z < z.min() + 1e-9)[0]
     top = np.where(z > z.max() - 1e-9)[0]
-    return dict(cell=cell, xyz=xyz, p1=p1, p2=p2, layer=layer, Kn=Kn, Tv=Tv, bottom=bottom, top=top)
+    return dict(cell=cell, xyz=xyz, p1=p1, p2=p2, layer=layer, Kn=Kn, Tv=Tv, bottom=bottom, top=top,
+                find_bonds_s=t_bonds)
 
 
 def describe(w):
@@ -282,6 +291,88 @@ def adjoint_cost(g, capi, w, cg_tol, local):
             "precision": "FP64 (exact Jacobian, matrix-free)"}
 
 
+def setup_cost(w, capi):
+    """The set-up before the first load step, through the public API with
+    host arrays: the createBonds search on the GPU (lpm_find_bonds) checked
+    against the CPU generator's bonds (identical arrays required), and the
+    creation of the device lattice (upload, opposite bonds, pattern and its
+    sliced layout).  The CPU time is the repository's k-d tree generator;
+    the reference's own search is O(N^2) and is not timed."""
+    xyz, cell = w["xyz"], w["cell"]
+    capi.find_bonds(xyz[:4096], cell)  # first-call costs out of the way
+    t0 = time.perf_counter()
+    p1, p2, layer = capi.find_bonds(xyz, cell)
+    t1 = time.perf_counter()
+    same = bool(np.array_equal(p1, w["p1"]) and np.array_equal(p2, w["p2"]) and np.array_equal(layer, w["layer"]))
+    t2 = time.perf_counter()
+    g = capi.Lattice(3, xyz, w["p1"], w["p2"], w["layer"], w["Kn"], w["Tv"], cell.particle_volume,
+                     cell.nneighbors)
+    g.synchronize()
+    t3 = time.perf_counter()
+    g.close()
+    return {"bond_search_ms": (t1 - t0) * 1e3, "bond_search_bonds_per_s": len(p1) / (t1 - t0),
+            "bonds_identical_to_cpu_generator": same, "cpu_kdtree_generator_ms": w["find_bonds_s"] * 1e3,
+            "lattice_create_ms": (t3 - t2) * 1e3, "timing": "host wall clock, host arrays in and out"}
+
+
+def fatigue_cost(capi, local, cycles=3):
+    """Configuration 5 at full size: the compact-tension plate (hexagonal
+    lattice, W = 40 mm from the load line, 0.15 mm spacing), HCF fatigue law
+    with seeded per-particle A and B, nonlocal damage rate, pin loads
+    cycled between 40 and 400 N (R = 0.1).  A static step to the minimum
+    load, then `cycles` calls of lpm_fatigue_cycle (one load increment up and
+    one down, a cycle jump of 1000), mixed precision.  Device time with CUDA
+    events on the library's stream."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    lat, fat = pkg.lattice, pkg.fatigue
+    xyz, p1, p2, layer, cell, info = lat.ct_specimen(40.0, 0.4, 0.15)
+    n = len(xyz)
+    Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(110e3, 0.34, plane_stress=True, layout="row"))
+    groups = lat.ct_groups(xyz, info, 0.15)
+    rng = np.random.default_rng(20261203)
+    params = np.stack([rng.uniform(1.5e-4, 2.5e-4, n), rng.uniform(0.50, 0.65, n), np.full(n, 1.079),
+                       np.ones(n)], axis=1)
+    L = 0.3
+    nl_ptr, nl_idx = lat.nonlocal_neighbors(xyz, 1.5 * L)
+    g = capi.Lattice(2, xyz, p1, p2, layer, Kn, Tv, cell.particle_volume, cell.nneighbors)
+    g.set_law(capi.LAW_FATIGUE_HCF, params)
+    (cx, cy_b), (_, cy_t) = info["holes"]
+    near_pins = (np.abs(xyz[:, 0] - cx) <= info["radius"]) & ((xyz[:, 1] >= cy_t) | (xyz[:, 1] <= cy_b))
+    g.set_types(np.where(near_pins, 4, 0).astype(np.int32), 4)  # the pin regions do not damage
+    g.set_nonlocal(nl_ptr, nl_idx, L)
+    g.update()
+    gm, gt, gb = g.add_group(groups["mid"]), g.add_group(groups["top"]), g.add_group(groups["bottom"])
+    f_max, R = 400.0, 0.1
+    opts = dict(tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_MIXED, max_iter=30, tol=1e-5, cg_tol=1e-10)
+    fixed = [("disp", gm, 1, 0.0), ("disp", gt, 0, 0.0), ("disp", gb, 0, 0.0)]
+    r = g.load_step(fixed + [("force", gt, 0.0, R * f_max, 0.0), ("force", gb, 0.0, -R * f_max, 0.0)], **opts)
+    if r["status"] != 0:
+        raise RuntimeError("CT static step did not converge: %s" % r)
+    unit = fixed + [("force", gt, 0.0, 1.0, 0.0), ("force", gb, 0.0, -1.0, 0.0)]
+    spectrum = fat.ca_spectrum(f_max, R, 1000 * (cycles + 1))
+    fat.run_cycles(g, unit, spectrum, 1, 0.001, max_calls=1, **opts)  # warm-up cycle
+    stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    g.synchronize()
+    e0.record(stream)
+    recs = fat.run_cycles(g, unit, spectrum, 1, 0.001, max_calls=cycles, **opts)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    g.close()
+    if any(rc["status"] != 0 for rc in recs):
+        raise RuntimeError("CT fatigue cycle did not converge")
+    return {"workload": "CT hex plate W=40 mm, 0.15 mm spacing (%d particles, %d bonds), HCF law, "
+                        "pin load 40-400 N" % (n, len(p1)),
+            "cycles_per_s": len(recs) / (ms * 1e-3), "ms_per_cycle": ms / len(recs), "cycles": len(recs),
+            "newton_iters_per_cycle": statistics.mean(rc["newton_iters"] for rc in recs),
+            "cg_iters_per_cycle": statistics.mean(rc["cg_iters"] for rc in recs),
+            "cycle": "1 increment up, 1 down, cycle jump 1000 (lpm_fatigue_cycle)", "precision": "mixed"}
+
+
 def force_bytes(nb, n):
     """Algorithmic bytes of one force pass: per directed bond the partner
     index, dis0, dLp, bdamage, Kn, Tv and the bond force written; per
@@ -492,6 +583,8 @@ def run_gb300(args):
                            "force_ms": fa["force"], "assembly_ms": fa["assembly"], "directed_bonds": nb,
                            "force_achieved_gbs": fb / (fa["force"] * 1e-3) / 1e9,
                            "force_algorithmic_bytes": fb}
+    line["setup"] = setup_cost(w, capi)
+    line["fatigue"] = fatigue_cost(capi, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         oracle, o = cpu_oracle_system(w, threads)
