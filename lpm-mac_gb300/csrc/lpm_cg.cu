@@ -142,6 +142,16 @@ __device__ __forceinline__ void block_df_sum(float (&s)[K], float (&c)[K], doubl
   }
 }
 
+// Four values of the FP32 operator.  An operator that fits in L2 with room
+// to spare is read with the default policy and stays there from one
+// iteration to the next (KEEP); a larger one streams through with
+// evict-first loads, which leaves L2 to the vectors.
+template <bool KEEP>
+__device__ __forceinline__ float4 op_load(const float* a) {
+  if (KEEP) return __ldg(reinterpret_cast<const float4*>(a));
+  return __ldcs(reinterpret_cast<const float4*>(a));
+}
+
 // y = row `row` of A times p (FP32), in difference form with compensated
 // accumulation: the sum comes out as if accumulated in twice the precision
 // and then rounded, so the only FP32 errors left are in the differences
@@ -149,7 +159,7 @@ __device__ __forceinline__ void block_df_sum(float (&s)[K], float (&c)[K], doubl
 // own rounding.  The row is walked in groups of four blocks: one 16-byte load
 // brings a block element for four blocks.  Padding blocks are zero and point
 // at the row itself.
-template <int DIM, bool OFF16>
+template <int DIM, bool OFF16, bool KEEP>
 __device__ __forceinline__ void row_product32(const SellView& v, const float* __restrict__ A,
                                               const float* __restrict__ p, int row, float (&y)[DIM]) {
   float sc[DIM], cc[DIM];
@@ -167,7 +177,7 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
   if (ng > 0) {
     c4n = group_cols<OFF16>(v, row, base);
 #pragma unroll
-    for (int e = 0; e < DIM * DIM; ++e) an[e] = __ldcs(reinterpret_cast<const float4*>(A + e * v.nslots + base));
+    for (int e = 0; e < DIM * DIM; ++e) an[e] = op_load<KEEP>(A + e * v.nslots + base);
   }
   for (int g = 0; g < ng; ++g) {
     const int4 c4 = c4n;
@@ -178,7 +188,7 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
       const int64_t s1 = base + (int64_t)(g + 1) * (kSlice * kVec);
       c4n = group_cols<OFF16>(v, row, s1);
 #pragma unroll
-      for (int e = 0; e < DIM * DIM; ++e) an[e] = __ldcs(reinterpret_cast<const float4*>(A + e * v.nslots + s1));
+      for (int e = 0; e < DIM * DIM; ++e) an[e] = op_load<KEEP>(A + e * v.nslots + s1);
     }
 #pragma unroll
     for (int t = 0; t < kVec; ++t) {
@@ -239,7 +249,7 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
   }
 }
 
-template <typename T, int DIM, bool OFF16 = false>
+template <typename T, int DIM, bool OFF16 = false, bool KEEP = false>
 __global__ void __launch_bounds__(256) k_cg_spmv(SellView v, const T* __restrict__ A, const T* __restrict__ p,
                                                  T* __restrict__ q, CgScalars* cg, double* partials,
                                                  unsigned int* ticket) {
@@ -249,7 +259,7 @@ __global__ void __launch_bounds__(256) k_cg_spmv(SellView v, const T* __restrict
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < v.n; row += gridDim.x * blockDim.x) {
     T y[DIM];
     if constexpr (sizeof(T) == 4)
-      row_product32<DIM, OFF16>(v, A, p, row, y);
+      row_product32<DIM, OFF16, KEEP>(v, A, p, row, y);
     else
       row_product<DIM>(v, A, p, row, y);
 #pragma unroll
@@ -657,12 +667,23 @@ struct MixedGrids {
   int spmv, update, residual, replace, pupdate;
 };
 
+// The FP32 product of a mixed solve: 16-bit column offsets when they fit;
+// the operator kept in L2 when its FP32 values take at most kKeepBytes.
+using Spmv32Fn = void (*)(SellView, const float*, const float*, float*, CgScalars*, double*, unsigned int*);
+constexpr long long kKeepBytes = 64LL << 20;  // half of GB300's L2
+template <int DIM>
+Spmv32Fn spmv32_fn_dim(bool o16, bool keep) {
+  if (keep) return o16 ? k_cg_spmv<float, DIM, true, true> : k_cg_spmv<float, DIM, false, true>;
+  return o16 ? k_cg_spmv<float, DIM, true> : k_cg_spmv<float, DIM>;
+}
+Spmv32Fn spmv32_fn(const lpm_handle* h, const SellView& sv) {
+  const bool keep = (long long)h->nslots * h->dim * h->dim * 4 <= kKeepBytes;
+  return h->dim == 3 ? spmv32_fn_dim<3>(sv.soff != nullptr, keep) : spmv32_fn_dim<2>(sv.soff != nullptr, keep);
+}
+
 int mixed_grids(lpm_handle* h, const SellView& sv, MixedGrids* mg) {
   const long long n = h->n, ndof = n * h->dim;
-  if (h->dim == 3)
-    mg->spmv = sv.soff ? resident_grid(h, k_cg_spmv<float, 3, true>, n) : resident_grid(h, k_cg_spmv<float, 3>, n);
-  else
-    mg->spmv = sv.soff ? resident_grid(h, k_cg_spmv<float, 2, true>, n) : resident_grid(h, k_cg_spmv<float, 2>, n);
+  mg->spmv = resident_grid(h, spmv32_fn(h, sv), n);
   mg->residual = fp64_row_grid(h);
   mg->update = resident_grid(h, k_mx_update, ndof);
   mg->replace = resident_grid(h, k_mx_replace, ndof);
@@ -690,12 +711,7 @@ cudaError_t add_kernel(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode
   return cudaGraphAddKernelNode(node, g, dep, dep ? 1 : 0, &kp);
 }
 
-template <int DIM, bool OFF16>
-cudaError_t add_spmv32(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* dep, int GR, const SellView& sv,
-                       const Dev& d) {
-  return add_kernel(node, g, dep, k_cg_spmv<float, DIM, OFF16>, GR, 256, sv, (const float*)d.A32,
-                    (const float*)d.p32, d.q32, d.cg, d.red.partials, d.red.ticket + 3);
-}
+
 
 // The mixed solve's iteration loop as one graph:
 //   while (loop_cond) { spmv; update; if (ru_cond) { residual; replace } pupdate }
@@ -726,13 +742,9 @@ int build_mixed_graph(lpm_handle* h, const SellView& sv, const MixedGrids& mg) {
   LPM_CUDA(h, cudaGraphConditionalHandleCreate(&ru_cond, body, 0u, cudaGraphCondAssignDefault));
   cudaGraphNode_t n_spmv, n_upd, n_if, n_res, n_rep, n_pup;
   cudaError_t e;
-  if (dim == 3)
-    e = sv.soff ? add_spmv32<3, true>(&n_spmv, body, nullptr, mg.spmv, sv, d)
-                : add_spmv32<3, false>(&n_spmv, body, nullptr, mg.spmv, sv, d);
-  else
-    e = sv.soff ? add_spmv32<2, true>(&n_spmv, body, nullptr, mg.spmv, sv, d)
-                : add_spmv32<2, false>(&n_spmv, body, nullptr, mg.spmv, sv, d);
-  LPM_CUDA(h, e);
+  const Spmv32Fn spmv = spmv32_fn(h, sv);
+  LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, spmv, mg.spmv, 256, sv, (const float*)d.A32, (const float*)d.p32,
+                         d.q32, d.cg, d.red.partials, d.red.ticket + 3));
   LPM_CUDA(h, add_kernel(&n_upd, body, &n_spmv, k_mx_update, mg.update, 256, ndof, d.x32, d.r32, (const float*)d.p32,
                          (const float*)d.q32, (const float*)d.invd32, d.cg, d.red.partials, d.red.ticket + 4,
                          ru_cond));
@@ -755,7 +767,7 @@ int build_mixed_graph(lpm_handle* h, const SellView& sv, const MixedGrids& mg) {
   LPM_CUDA(h, add_kernel(&n_pup, body, &n_if, k_mx_pupdate, mg.pupdate, 256, ndof, (const float*)d.r32,
                          (const float*)d.invd32, d.p32, d.cg, loop_cond));
   LPM_CUDA(h, cudaGraphInstantiate(&h->mx_exec, g, 0));
-  h->mx_graph_off16 = sv.soff != nullptr;
+  h->mx_graph_spmv = (const void*)spmv;
   return LPM_OK;
 }
 
@@ -840,7 +852,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   const size_t ev0 = h->ev_used;
   if (!timing) {
     // the whole iteration loop as one graph launch
-    if (!h->mx_exec || h->mx_graph_off16 != (sv.soff != nullptr)) {
+    if (!h->mx_exec || h->mx_graph_spmv != (const void*)spmv32_fn(h, sv)) {
       st = build_mixed_graph(h, sv, mg);
       if (st) return st;
     }
@@ -849,6 +861,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   // with kernel timing on, the same kernels launched one by one from the
   // host, with events around each sparse product; the host reads the device
   // flag once per batch of iterations
+  const Spmv32Fn spmv32 = spmv32_fn(h, sv);
   long long batch = 8;
   for (; timing;) {
     for (long long k = 0; k < batch; ++k) {
@@ -858,18 +871,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
         e1 = next_event(h);
         if (e0) cudaEventRecord(e0, h->stream);
       }
-      if (dim == 3 && sv.soff)
-        k_cg_spmv<float, 3, true><<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials,
-                                                             d.red.ticket + 3);
-      else if (dim == 3)
-        k_cg_spmv<float, 3><<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials,
-                                                       d.red.ticket + 3);
-      else if (sv.soff)
-        k_cg_spmv<float, 2, true><<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials,
-                                                             d.red.ticket + 3);
-      else
-        k_cg_spmv<float, 2><<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials,
-                                                       d.red.ticket + 3);
+      spmv32<<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials, d.red.ticket + 3);
       LPM_LAUNCHED(h, "k_cg_spmv");
       if (timing && e1) cudaEventRecord(e1, h->stream);
       k_mx_update<<<mg.update, 256, 0, h->stream>>>(ndof, d.x32, d.r32, d.p32, d.q32, d.invd32, d.cg, d.red.partials,

@@ -176,7 +176,7 @@ struct lpm_handle {
   // the mixed solve's iteration loop as a graph with device-side conditions
   cudaGraph_t mx_graph = nullptr;
   cudaGraphExec_t mx_exec = nullptr;
-  bool mx_graph_off16 = false;  // which FP32 product the graph launches
+  const void* mx_graph_spmv = nullptr;  // the FP32 product kernel the graph launches
 };
 
 namespace lpm {
