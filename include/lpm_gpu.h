@@ -269,6 +269,7 @@ typedef struct {
   int64_t kernel_launches;
   int64_t mixed_fallbacks; /* mixed solves that broke down (non-finite FP32 recurrence,
                               e.g. an indefinite softened tangent) and were re-solved in FP64 */
+  int64_t tangent_cg_iters; /* CG iterations of the tangent solves (lpm_tangent_begin) */
 } lpm_stats;
 int lpm_get_stats(const lpm_handle* h, lpm_stats* st);
 int lpm_reset_stats(lpm_handle* h);
@@ -334,6 +335,29 @@ int lpm_backward_step(lpm_handle* h, const double* dJdx, const double* dJdpin, d
 /* y = H v with H = dPin/dx at the current state (all DOFs, N*dim each):
  * the exact Jacobian-vector product the adjoint uses. */
 int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y);
+
+/* Forward-mode (tangent-linear) sensitivity of a J2 load history with respect
+ * to the law's parameters, for responses of the stress-strain curve.
+ * Between lpm_tangent_begin and lpm_tangent_end every converged load step
+ * (lpm_load_step) also carries ndir tangent states along: dparams
+ * (ndir x n x np, host, np the law's parameters per particle) gives each
+ * direction's change of the parameters, e.g. 1 in the yield-stress column
+ * for d/d(sigma_y).  At each step, after Newton and before the state update
+ * (solver_fatigue.h:266, solver_static.h:122): the change of the
+ * equilibrium, H_ff dx_f = -(dPin/d dLp . d dLp)_f with dx = 0 on
+ * constrained DOFs (CG on the exact Jacobian to `tol`); the change of the
+ * internal forces (LPM_T_PIN) and positions (LPM_T_XYZ) of that equilibrium;
+ * then the radial return (particle_j2plasticity.h:78-140) differentiated,
+ * which advances the tangents of the state variables and of dLp.  A
+ * response R(Pin, x) summed over steps has dR/dtheta = sum over steps of
+ * its partial derivatives times these tangents.  Damage is held fixed
+ * (bonds intact or broken on both sides; LPM_ERR_STATE otherwise); a
+ * load step that cuts back fails with LPM_ERR_STATE. */
+#define LPM_T_PIN 1 /* n x dim: d Pin / d theta at the step's equilibrium */
+#define LPM_T_XYZ 2 /* n x dim: d x / d theta at the step's equilibrium */
+int lpm_tangent_begin(lpm_handle* h, int ndir, const double* dparams, double tol);
+int lpm_tangent_get(const lpm_handle* h, int dir, int field, double* dst);
+int lpm_tangent_end(lpm_handle* h);
 
 /* Device-resident snapshots of a step's state: positions, last converged
  * positions, external loads, constraints, particle damage and state

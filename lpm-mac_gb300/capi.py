@@ -24,6 +24,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 BC_DISP, BC_FORCE = 0, 1
 SOLVER_STATIC, SOLVER_FATIGUE_STATIC, SOLVER_STATIC_ELIMINATE = 0, 1, 2
 LAW_ELASTIC, LAW_DAMAGE, LAW_J2, LAW_FATIGUE_HCF, LAW_SOFTENING = 0, 1, 2, 3, 4
+T_PIN, T_XYZ = 1, 2  # tangent fields (lpm_tangent_get)
 _NSTATE = {LAW_ELASTIC: 1, LAW_DAMAGE: 1, LAW_J2: 7, LAW_FATIGUE_HCF: 3, LAW_SOFTENING: 1}
 
 
@@ -37,7 +38,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("cg_iters_total", ctypes.c_int64), ("refine_sweeps", ctypes.c_int64),
                 ("spmv_launches", ctypes.c_int64), ("spmv_ms", ctypes.c_double),
                 ("spmv32_launches", ctypes.c_int64), ("spmv32_ms", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64), ("mixed_fallbacks", ctypes.c_int64)]
+                ("kernel_launches", ctypes.c_int64), ("mixed_fallbacks", ctypes.c_int64),
+                ("tangent_cg_iters", ctypes.c_int64)]
 
 
 class BC(ctypes.Structure):
@@ -131,6 +133,9 @@ def load(build_if_needed=True):
                               ctypes.c_int, ctypes.c_double, ctypes.POINTER(StepOpts), ctypes.POINTER(CycleResult)],
         "lpm_backward_step": [H, dp, dp, ctypes.c_double, i64, ctypes.c_int, dp, dp, ctypes.POINTER(AdjointResult)],
         "lpm_apply_jacobian": [H, dp, dp],
+        "lpm_tangent_begin": [H, ctypes.c_int, dp, ctypes.c_double],
+        "lpm_tangent_get": [H, ctypes.c_int, ctypes.c_int, dp],
+        "lpm_tangent_end": [H],
         "lpm_checkpoint_save": [H, ip],
         "lpm_checkpoint_restore": [H, ctypes.c_int],
         "lpm_checkpoint_drop": [H, ctypes.c_int],
@@ -155,7 +160,7 @@ def exported_symbols():
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
             "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
             "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
-            "lpm_checkpoint_drop"]
+            "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_get", "lpm_tangent_end"]
 
 
 def set_device(device):
@@ -487,6 +492,26 @@ class Lattice:
         y = np.zeros(self.ndof)
         self._check(self._L.lpm_apply_jacobian(self.h, _d(v), _d(y)))
         return y
+
+    def tangent_begin(self, dparams, tol=1e-12):
+        """Carries len(dparams) tangent directions through the following load
+        steps (J2 law): each direction an (N, np) array, or one row of np
+        values for all particles, of parameter changes."""
+        rows = []
+        for d in dparams:
+            d = np.asarray(d, dtype=np.float64)
+            rows.append(np.broadcast_to(d, (self.n, d.shape[-1])))
+        dp = np.ascontiguousarray(np.stack(rows)) if rows else np.zeros(1)
+        self._check(self._L.lpm_tangent_begin(self.h, len(rows), _d(dp), float(tol)))
+
+    def tangent_get(self, direction, field=T_PIN):
+        """The step's d Pin (T_PIN) or d x (T_XYZ) along one direction, (N, dim)."""
+        y = np.zeros(self.ndof)
+        self._check(self._L.lpm_tangent_get(self.h, int(direction), int(field), _d(y)))
+        return y.reshape(self.n, self.dim)
+
+    def tangent_end(self):
+        self._check(self._L.lpm_tangent_end(self.h))
 
     def checkpoint_save(self):
         i = ctypes.c_int()

@@ -110,7 +110,9 @@ struct JacView {
 };
 
 // Pass 1 of H v: d dLe per slot and the per-layer sums d D_i^l, then d f.
-__global__ void k_jvp_bonds(int n, int dim, JacView J, const double* __restrict__ v, const CgScalars* cg) {
+// With dlp (per slot) the plastic stretches move too: d dLe -= d dLp.
+__global__ void k_jvp_bonds(int n, int dim, JacView J, const double* __restrict__ v, const double* __restrict__ dlp,
+                            const CgScalars* cg) {
   if (cg && cg->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -124,8 +126,9 @@ __global__ void k_jvp_bonds(int n, int dim, JacView J, const double* __restrict_
     const int64_t s = s0 + 32 * (int64_t)k;
     double vj[3];
     load_v(v, dim, J.jp2[s], vj);
-    const double dd = J.jc[s] * (vi[0] - vj[0]) + J.jc[J.nslot + s] * (vi[1] - vj[1]) +
-                      J.jc[2 * J.nslot + s] * (vi[2] - vj[2]);
+    double dd = J.jc[s] * (vi[0] - vj[0]) + J.jc[J.nslot + s] * (vi[1] - vj[1]) +
+                J.jc[2 * J.nslot + s] * (vi[2] - vj[2]);
+    if (dlp) dd -= dlp[s];
     J.jd[s] = dd;
     if (J.jlayer[s] == 0)
       dD0 += dd;
@@ -267,6 +270,142 @@ __global__ void k_partial_damage(int64_t nb, const double* __restrict__ bdamage,
   if ((d > EPS && d < 1.0 - EPS) || is_broken(d) != is_broken(bdamage[opp[b]])) atomicOr(flag, 1);
 }
 
+// ------------------------------------------------ tangent-linear sensitivity
+// d dLp in the sliced bond layout (broken bonds 0; padding slots stay 0).
+__global__ void k_dlp_slots(int n, const int64_t* __restrict__ bptr, const int* __restrict__ slot_of,
+                            const double* __restrict__ bdamage, const double* __restrict__ dlp,
+                            double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) out[slot_of[b]] = is_broken(bdamage[b]) ? 0.0 : dlp[b];
+}
+
+// g = -q on the free DOFs, 0 on the constrained ones.
+__global__ void k_tg_rhs(int n, int dim, const double* __restrict__ q, const int* __restrict__ mask,
+                         double* __restrict__ g) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * dim) return;
+  const int i = t / dim, k = t % dim;
+  g[t] = mask[3 * i + k] ? 0.0 : -q[t];
+}
+
+// The change of the particle stress (particle.h:217-240,
+// sigma_pq = sum_b (1/2 V_m) dis_b F_b c_p c_q with F_b the mean bond force)
+// for a change v of the positions, with d F_b from pass 1 of the Jacobian
+// product (J.jd, which includes any change of dLp):
+//   d dis = c . u,  d c = (u - c d dis) / dis,  u = v_i - v_j.
+__global__ void k_jvp_stress(int n, int dim, JacView J, const double* __restrict__ v, const int64_t* __restrict__ bptr,
+                             const int* __restrict__ bp2, const int* __restrict__ slot_of,
+                             const int* __restrict__ opp, const double* __restrict__ bforce,
+                             const double* __restrict__ cs, const double* __restrict__ dis,
+                             const int* __restrict__ nbonds, double pvol, int nneighbors, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double hv = 0.5 / (pvol * nbonds[i] / nneighbors);
+  double vi[3];
+  load_v(v, dim, i, vi);
+  double ds[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    double vj[3];
+    load_v(v, dim, bp2[b], vj);
+    const double c[3] = {cs[3 * b], cs[3 * b + 1], cs[3 * b + 2]};
+    const double u[3] = {vi[0] - vj[0], vi[1] - vj[1], vi[2] - vj[2]};
+    const double dd = c[0] * u[0] + c[1] * u[1] + c[2] * u[2];
+    const double dc[3] = {(u[0] - c[0] * dd) / dis[b], (u[1] - c[1] * dd) / dis[b], (u[2] - c[2] * dd) / dis[b]};
+    const int s = slot_of[b];
+    const double F = 0.5 * (bforce[b] + bforce[opp[b]]);
+    const double dF = 0.5 * (J.jd[s] + J.jd[J.jopp[s]]);
+    const double sf = hv * dis[b] * F, dsf = hv * (dd * F + dis[b] * dF);
+    const int p[6] = {0, 1, 2, 1, 0, 0}, q[6] = {0, 1, 2, 2, 2, 1};  // xx yy zz yz xz xy
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+      ds[k] += dsf * c[p[k]] * c[q[k]] + sf * (dc[p[k]] * c[q[k]] + c[p[k]] * dc[q[k]]);
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) out[6 * (int64_t)i + k] = ds[k];
+}
+
+// The radial return of ParticleJ2Plasticity (particle_j2plasticity.h:78-140,
+// the primal in lpm_laws.cu) differentiated along one direction: inputs the
+// primal stress, state (before the update) and parameters, and the tangents
+// of stress, state, parameters and positions; advances the tangents of the
+// state (alpha, back stress) and of each bond's dLp.  Elastic particles
+// (no yield) leave their tangents unchanged.
+__global__ void k_j2_tangent(int n, int dim, int np, int ns, const double* __restrict__ pp,
+                             const double* __restrict__ dpp, const double* __restrict__ state,
+                             double* __restrict__ tsv, const double* __restrict__ stress,
+                             const double* __restrict__ dstress, const int64_t* __restrict__ bptr,
+                             const int* __restrict__ bp2, const double* __restrict__ dis,
+                             const double* __restrict__ cs, const double* __restrict__ tx, double* __restrict__ tdlp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* P = pp + (int64_t)i * np;
+  const double* dP = dpp + (int64_t)i * np;
+  const double* sv = state + (int64_t)i * ns;
+  double* t = tsv + (int64_t)i * ns;
+  const double E = P[0], mu = P[1], sigmay = P[2], xi = P[3], H = P[4];
+  const double dE = dP[0], dmu = dP[1], dsigmay = dP[2], dxi = dP[3], dH = dP[4];
+  double st[6], dst[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    st[j] = stress[6 * (int64_t)i + j];
+    dst[j] = dstress[6 * (int64_t)i + j];
+  }
+  const double sm = (st[0] + st[1] + st[2]) / 3.0, dsm = (dst[0] + dst[1] + dst[2]) / 3.0;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    st[j] -= sm;
+    dst[j] -= dsm;
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    st[j] -= sv[j + 1];
+    dst[j] -= t[j + 1];
+  }
+  double s2 = 0.0, ds2 = 0.0;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const double w = j < 3 ? 1.0 : 2.0;
+    s2 += w * st[j] * st[j];
+    ds2 += w * st[j] * dst[j];
+  }
+  const double seq = sqrt(1.5 * s2);
+  const double dseq = seq > 0.0 ? 1.5 * ds2 / seq : 0.0;
+  const double yf = seq - (sigmay + (1.0 - xi) * H * sv[0]);
+  if (!(yf > 0.0)) return;
+  const double G = E / 2 / (1 + mu), dG = dE / 2 / (1 + mu) - E * dmu / (2 * (1 + mu) * (1 + mu));
+  const double den = 3 * G + H;
+  const double dyf = dseq - (dsigmay - dxi * H * sv[0] + (1.0 - xi) * (dH * sv[0] + H * t[0]));
+  const double dl = yf / den, ddl = dyf / den - yf * (3 * dG + dH) / (den * den);
+  t[0] += ddl;
+  double dp[6] = {0, 0, 0, 0, 0, 0}, ddp[6] = {0, 0, 0, 0, 0, 0};
+  if (fabs(seq) > EPS) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      dp[j] = dl * 1.5 * st[j] / seq;
+      ddp[j] = 1.5 * (ddl * st[j] / seq + dl * (dst[j] / seq - st[j] * dseq / (seq * seq)));
+      t[j + 1] += 2. / 3. * (dxi * H * dp[j] + xi * dH * dp[j] + xi * H * ddp[j]);
+    }
+  }
+  double vi[3];
+  load_v(tx, dim, i, vi);
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    double vj[3];
+    load_v(tx, dim, bp2[b], vj);
+    const double c0 = cs[3 * b], c1 = cs[3 * b + 1], c2 = cs[3 * b + 2];
+    const double u0 = vi[0] - vj[0], u1 = vi[1] - vj[1], u2 = vi[2] - vj[2];
+    const double dd = c0 * u0 + c1 * u1 + c2 * u2;
+    const double e0 = (u0 - c0 * dd) / dis[b], e1 = (u1 - c1 * dd) / dis[b], e2 = (u2 - c2 * dd) / dis[b];
+    const double q = dp[0] * c0 * c0 + dp[1] * c1 * c1 + dp[2] * c2 * c2 + 2 * dp[3] * c1 * c2 +
+                     2 * dp[4] * c0 * c2 + 2 * dp[5] * c0 * c1;
+    const double dq = ddp[0] * c0 * c0 + ddp[1] * c1 * c1 + ddp[2] * c2 * c2 + 2 * ddp[3] * c1 * c2 +
+                      2 * ddp[4] * c0 * c2 + 2 * ddp[5] * c0 * c1 + dp[0] * 2 * c0 * e0 + dp[1] * 2 * c1 * e1 +
+                      dp[2] * 2 * c2 * e2 + 2 * dp[3] * (e1 * c2 + c1 * e2) + 2 * dp[4] * (e0 * c2 + c0 * e2) +
+                      2 * dp[5] * (e0 * c1 + c0 * e1);
+    tdlp[b] += dd * q + dis[b] * dq;
+  }
+}
+
 }  // namespace
 
 // Work buffers of the adjoint, allocated on first use (gradients zeroed).
@@ -336,11 +475,13 @@ static int jacobian_prepare(lpm_handle* h) {
   return LPM_OK;
 }
 
-// y = H v (mask: zero the constrained rows); with cg, p.q and alpha too.
-static int apply_jacobian(lpm_handle* h, const double* v, double* y, bool masked, CgScalars* cg) {
+// y = H v (mask: zero the constrained rows); with cg, p.q and alpha too;
+// with dlp (sliced layout) the derivative along a change of dLp as well.
+static int apply_jacobian(lpm_handle* h, const double* v, double* y, bool masked, CgScalars* cg,
+                          const double* dlp = nullptr) {
   Dev& d = h->d;
   const JacView J{d.jbase, d.jp2, d.jopp, d.jlayer, d.jc, d.jk, d.jt, d.jf, d.jd, h->jslots};
-  k_jvp_bonds<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, h->dim, J, v, cg);
+  k_jvp_bonds<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, h->dim, J, v, dlp, cg);
   LPM_LAUNCHED(h, "k_jvp_bonds");
   k_jvp_particles<<<grid_for(h->n, 256, kMaxRedBlocks), 256, 0, h->stream>>>(
       h->n, h->dim, J, v, masked ? d.mask : nullptr, y, cg, d.red.partials, d.red.ticket + 8);
@@ -356,49 +497,28 @@ int adjoint_apply(lpm_handle* h, const double* v_dev, double* y_dev) {
   return apply_jacobian(h, v_dev, y_dev, false, nullptr);
 }
 
-int adjoint_step(lpm_handle* h, const double* a_dev, const double* c_dev, double tol, long long maxit, int accumulate,
-                 double* gKn_dev, double* gTv_dev, long long* iters, double* relres) {
+// H_ff x = g (g zero on the constrained DOFs, x zero there too) by
+// Jacobi-PCG on the exact Jacobian at the prepared state, with its exact
+// diagonal as the preconditioner; the relative residual in *relres.
+static int jacobian_cg(lpm_handle* h, const double* g, double* x, double tol, long long maxit, long long* iters,
+                       double* relres) {
   Dev& d = h->d;
   const int dim = h->dim;
   const int64_t m = (int64_t)h->n * dim;
-  int st = adjoint_buffers(h);
-  if (st) return st;
-  // the symmetric solve needs every bond intact or broken
-  LPM_CUDA(h, cudaMemsetAsync(d.adj_flag, 0, sizeof(int), h->stream));
-  k_partial_damage<<<grid_for(h->nb, 256), 256, 0, h->stream>>>(h->nb, d.bdamage, d.opp, d.adj_flag);
-  LPM_LAUNCHED(h, "k_partial_damage");
-  int flag = 0;
-  LPM_CUDA(h, cudaMemcpyAsync(&flag, d.adj_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
-  if (flag) {
-    h->err = "adjoint: partially or one-sidedly damaged bonds make the Jacobian non-symmetric";
-    return LPM_ERR_STATE;
-  }
-  st = jacobian_prepare(h);
-  if (st) return st;
-  // g = a + H c on the free DOFs
-  const int TV = 256;
-  if (c_dev) {
-    st = apply_jacobian(h, c_dev, d.adj_q, false, nullptr);
-    if (st) return st;
-  }
-  k_adj_rhs<<<grid_for(m, TV), TV, 0, h->stream>>>(h->n, dim, a_dev, c_dev ? d.adj_q : nullptr, d.mask, d.adj_g);
-  LPM_LAUNCHED(h, "k_adj_rhs");
   k_jac_invdiag<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, dim, d.bptr, d.blayer, d.opp, d.cs, d.dis,
                                                             d.bdamage, d.bforce, d.Kn, d.Tv, d.mask, d.adj_invd);
   LPM_LAUNCHED(h, "k_jac_invdiag");
-  // H_ff lambda = g by Jacobi-PCG on the exact Jacobian
   if (maxit < 0) maxit = 2LL * m;
   const int GV = grid_for(m, 256, kMaxRedBlocks);
-  k_cg_init<double><<<GV, 256, 0, h->stream>>>(m, d.adj_g, d.adj_lam, d.adj_r, d.adj_p, d.adj_invd, d.cg, tol, maxit,
+  k_cg_init<double><<<GV, 256, 0, h->stream>>>(m, g, x, d.adj_r, d.adj_p, d.adj_invd, d.cg, tol, maxit,
                                                d.red.partials, d.red.ticket + 2);
   LPM_LAUNCHED(h, "k_cg_init");
   long long batch = 8;
   for (;;) {
     for (long long k = 0; k < batch; ++k) {
-      st = apply_jacobian(h, d.adj_p, d.adj_q, true, d.cg);
+      int st = apply_jacobian(h, d.adj_p, d.adj_q, true, d.cg);
       if (st) return st;
-      k_cg_update<double><<<GV, 256, 0, h->stream>>>(m, d.adj_lam, d.adj_r, d.adj_p, d.adj_q, d.adj_invd, d.cg,
+      k_cg_update<double><<<GV, 256, 0, h->stream>>>(m, x, d.adj_r, d.adj_p, d.adj_q, d.adj_invd, d.cg,
                                                      d.red.partials, d.red.ticket + 4);
       LPM_LAUNCHED(h, "k_cg_update");
       k_cg_pupdate<double><<<GV, 256, 0, h->stream>>>(m, d.adj_r, d.adj_invd, d.adj_p, d.cg, 0);
@@ -411,12 +531,56 @@ int adjoint_step(lpm_handle* h, const double* a_dev, const double* c_dev, double
   }
   const CgScalars c = *h->h_cg;
   if (iters) *iters = c.it;
-  const double err = c.rhs_norm2 > 0 ? sqrt(c.rr / c.rhs_norm2) : 0.0;
-  if (relres) *relres = err;
+  *relres = c.rhs_norm2 > 0 ? sqrt(c.rr / c.rhs_norm2) : 0.0;
   if (c.done == 3) {
     h->err = "adjoint: non-finite value in the CG iteration";
     return LPM_ERR_NONFINITE;
   }
+  return LPM_OK;
+}
+
+// 1 in the adjoint flag (and LPM_ERR_STATE) when some bond is partially or
+// one-sidedly damaged: the Jacobian is then not symmetric.
+static int check_symmetric_damage(lpm_handle* h) {
+  Dev& d = h->d;
+  LPM_CUDA(h, cudaMemsetAsync(d.adj_flag, 0, sizeof(int), h->stream));
+  k_partial_damage<<<grid_for(h->nb, 256), 256, 0, h->stream>>>(h->nb, d.bdamage, d.opp, d.adj_flag);
+  LPM_LAUNCHED(h, "k_partial_damage");
+  int flag = 0;
+  LPM_CUDA(h, cudaMemcpyAsync(&flag, d.adj_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (flag) {
+    h->err = "adjoint: partially or one-sidedly damaged bonds make the Jacobian non-symmetric";
+    return LPM_ERR_STATE;
+  }
+  return LPM_OK;
+}
+
+int adjoint_step(lpm_handle* h, const double* a_dev, const double* c_dev, double tol, long long maxit, int accumulate,
+                 double* gKn_dev, double* gTv_dev, long long* iters, double* relres) {
+  Dev& d = h->d;
+  const int dim = h->dim;
+  const int64_t m = (int64_t)h->n * dim;
+  int st = adjoint_buffers(h);
+  if (st) return st;
+  // the symmetric solve needs every bond intact or broken
+  st = check_symmetric_damage(h);
+  if (st) return st;
+  st = jacobian_prepare(h);
+  if (st) return st;
+  // g = a + H c on the free DOFs
+  const int TV = 256;
+  if (c_dev) {
+    st = apply_jacobian(h, c_dev, d.adj_q, false, nullptr);
+    if (st) return st;
+  }
+  k_adj_rhs<<<grid_for(m, TV), TV, 0, h->stream>>>(h->n, dim, a_dev, c_dev ? d.adj_q : nullptr, d.mask, d.adj_g);
+  LPM_LAUNCHED(h, "k_adj_rhs");
+  // H_ff lambda = g by Jacobi-PCG on the exact Jacobian
+  double err = 0.0;
+  st = jacobian_cg(h, d.adj_g, d.adj_lam, tol, maxit, iters, &err);
+  if (st) return st;
+  if (relres) *relres = err;
   // parameter gradients
   k_adj_mu<<<grid_for(m, TV), TV, 0, h->stream>>>(m, c_dev, d.adj_lam, d.adj_mu);
   LPM_LAUNCHED(h, "k_adj_mu");
@@ -425,6 +589,99 @@ int adjoint_step(lpm_handle* h, const double* a_dev, const double* c_dev, double
                                                            gTv_dev);
   LPM_LAUNCHED(h, "k_param_grad");
   return err <= tol ? LPM_OK : LPM_NOT_CONVERGED;
+}
+
+// ------------------------------------------------ tangent-linear sensitivity
+int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double tol) {
+  Dev& d = h->d;
+  if (ndir < 0 || (ndir > 0 && !dparams_host) || !(tol > 0.0)) {
+    h->err = "tangent: bad arguments";
+    return LPM_ERR_ARG;
+  }
+  if (ndir > 0 && (h->law != 2 || !d.pp || !d.state)) {
+    h->err = "tangent: the J2 law (lpm_set_law 2) is required";
+    return LPM_ERR_STATE;
+  }
+  if (ndir > h->tg_cap) {  // buffers for ndir directions (smaller ones stay owned by the handle)
+    const size_t N = (size_t)h->n, B = (size_t)std::max<int64_t>(h->nb, 1), m = N * h->dim;
+    d.tg_dlp = (double*)dev_alloc(h, sizeof(double) * ndir * B);
+    d.tg_sv = (double*)dev_alloc(h, sizeof(double) * ndir * N * h->nstate);
+    d.tg_x = (double*)dev_alloc(h, sizeof(double) * ndir * m);
+    d.tg_pin = (double*)dev_alloc(h, sizeof(double) * ndir * m);
+    d.tg_dp = (double*)dev_alloc(h, sizeof(double) * ndir * N * h->law_np);
+    d.tg_stress = (double*)dev_alloc(h, sizeof(double) * 6 * N);
+    if (!d.tg_dlp || !d.tg_sv || !d.tg_x || !d.tg_pin || !d.tg_dp || !d.tg_stress) return LPM_ERR_NOMEM;
+    h->tg_cap = ndir;
+  }
+  h->tg_ndir = 0;
+  if (ndir == 0) return LPM_OK;
+  const size_t N = (size_t)h->n, B = (size_t)std::max<int64_t>(h->nb, 1), m = N * h->dim;
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_dlp, 0, sizeof(double) * ndir * B, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_sv, 0, sizeof(double) * ndir * N * h->nstate, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_x, 0, sizeof(double) * ndir * m, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_pin, 0, sizeof(double) * ndir * m, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.tg_dp, dparams_host, sizeof(double) * ndir * N * h->law_np, cudaMemcpyHostToDevice,
+                              h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->tg_ndir = ndir;
+  h->tg_tol = tol;
+  return LPM_OK;
+}
+
+// One converged step's tangents (called after Newton, before the state
+// update): for each direction, the equilibrium's change, the changes of
+// Pin and of the stress there, then the differentiated J2 return.
+int tangent_step(lpm_handle* h) {
+  Dev& d = h->d;
+  const int dim = h->dim, n = h->n;
+  const int64_t m = (int64_t)n * dim;
+  int st = adjoint_buffers(h);
+  if (st) return st;
+  st = check_symmetric_damage(h);
+  if (st) return st;
+  st = jacobian_prepare(h);
+  if (st) return st;
+  if (!d.tg_jdl) {
+    d.tg_jdl = (double*)zeros_dev(h, sizeof(double) * (size_t)std::max<int64_t>(h->jslots, 1));
+    if (!d.tg_jdl) return LPM_ERR_NOMEM;
+  }
+  LPM_CUDA(h, cudaMemsetAsync(d.adj_a, 0, sizeof(double) * m, h->stream));  // a zero position change
+  const JacView J{d.jbase, d.jp2, d.jopp, d.jlayer, d.jc, d.jk, d.jt, d.jf, d.jd, h->jslots};
+  for (int k = 0; k < h->tg_ndir; ++k) {
+    double* tdlp = d.tg_dlp + (size_t)k * std::max<int64_t>(h->nb, 1);
+    double* tsv = d.tg_sv + (size_t)k * n * h->nstate;
+    double* tx = d.tg_x + (size_t)k * m;
+    double* tpin = d.tg_pin + (size_t)k * m;
+    const double* tdp = d.tg_dp + (size_t)k * n * h->law_np;
+    k_dlp_slots<<<grid_for(n, 128), 128, 0, h->stream>>>(n, d.bptr, d.jslot_of, d.bdamage, tdlp, d.tg_jdl);
+    LPM_LAUNCHED(h, "k_dlp_slots");
+    // H_ff dx_f = -(dPin/d dLp . d dLp)_f
+    st = apply_jacobian(h, d.adj_a, d.adj_q, false, nullptr, d.tg_jdl);
+    if (st) return st;
+    k_tg_rhs<<<grid_for(m, 256), 256, 0, h->stream>>>(n, dim, d.adj_q, d.mask, d.adj_g);
+    LPM_LAUNCHED(h, "k_tg_rhs");
+    long long it = 0;
+    double rr = 0.0;
+    st = jacobian_cg(h, d.adj_g, tx, h->tg_tol, -1, &it, &rr);
+    if (st) return st;
+    h->stats.tangent_cg_iters += it;
+    if (!(rr <= h->tg_tol)) {
+      h->err = "tangent: the equilibrium change did not converge";
+      return LPM_NOT_CONVERGED;
+    }
+    // dPin and the stress change at the equilibrium (pass 1 leaves d f in J.jd)
+    st = apply_jacobian(h, tx, tpin, false, nullptr, d.tg_jdl);
+    if (st) return st;
+    k_jvp_stress<<<grid_for(n, 128), 128, 0, h->stream>>>(n, dim, J, tx, d.bptr, d.bp2, d.jslot_of, d.opp, d.bforce,
+                                                         d.cs, d.dis, d.nbonds, h->particle_volume, h->nneighbors,
+                                                         d.tg_stress);
+    LPM_LAUNCHED(h, "k_jvp_stress");
+    k_j2_tangent<<<grid_for(n, 128), 128, 0, h->stream>>>(n, dim, h->law_np, h->nstate, d.pp, tdp, d.state, tsv,
+                                                         d.stress, d.tg_stress, d.bptr, d.bp2, d.dis, d.cs, tx,
+                                                         tdlp);
+    LPM_LAUNCHED(h, "k_j2_tangent");
+  }
+  return LPM_OK;
 }
 
 // ---------------------------------------------------------------- checkpoints

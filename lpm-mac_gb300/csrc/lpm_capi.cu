@@ -621,6 +621,10 @@ int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts
       st = lpm_newton(h, o->max_iter, o->tol, o->precision, o->cg_tol, o->cg_maxit, &ni);
       if (st < 0) return st;
       failed = ni >= o->max_iter;
+      if (!failed && h->tg_ndir > 0) {  // the tangents of this equilibrium and of the state update
+        st = tangent_step(h);
+        if (st) return st;
+      }
       if (!failed) {  // solver_fatigue.h:266-267
         st = launch_update_state(h);
         if (st) return st;
@@ -638,18 +642,30 @@ int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts
           failed = true;
           break;
         }
+        if (h->tg_ndir > 0) {
+          st = tangent_step(h);
+          if (st) return st;
+        }
         st = launch_update_state(h);  // solver_static.h:122-123
         if (st) return st;
         st = launch_static_damage(h, &damaged);
         if (st) return st;
         st = lpm_store_state(h);
         if (st) return st;
+        if (damaged && h->tg_ndir > 0) {
+          h->err = "tangent sensitivity holds the damage fixed: a damage round ended the step";
+          return LPM_ERR_STATE;
+        }
         if (damaged) {
           ++r.damage_rounds;
           st = lpm_update_geometry_force(h);
           if (st) return st;
         }
       } while (damaged);
+    }
+    if (failed && h->tg_ndir > 0) {
+      h->err = "tangent sensitivity does not follow load-step cut-backs";
+      return LPM_ERR_STATE;
     }
     if (failed) {
       if (++r.cuts > o->max_cuts) {
@@ -823,6 +839,27 @@ int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y) {
   if (st) return st;
   LPM_CUDA(h, cudaMemcpyAsync(y, d.adj_q, sizeof(double) * m, cudaMemcpyDeviceToHost, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_tangent_begin(lpm_handle* h, int ndir, const double* dparams, double tol) {
+  if (!h) return LPM_ERR_ARG;
+  return tangent_begin(h, ndir, dparams, tol);
+}
+
+int lpm_tangent_get(const lpm_handle* h, int dir, int field, double* dst) {
+  if (!h || !dst || dir < 0 || dir >= h->tg_ndir || (field != LPM_T_PIN && field != LPM_T_XYZ)) return LPM_ERR_ARG;
+  lpm_handle* hh = const_cast<lpm_handle*>(h);
+  const size_t m = (size_t)h->n * h->dim;
+  const double* src = (field == LPM_T_PIN ? h->d.tg_pin : h->d.tg_x) + (size_t)dir * m;
+  LPM_CUDA(hh, cudaMemcpyAsync(dst, src, sizeof(double) * m, cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(hh, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
+int lpm_tangent_end(lpm_handle* h) {
+  if (!h) return LPM_ERR_ARG;
+  h->tg_ndir = 0;
   return LPM_OK;
 }
 

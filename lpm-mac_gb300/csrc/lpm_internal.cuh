@@ -128,6 +128,12 @@ struct Dev {
   int64_t* jbase;
   int *jslot_of, *jp2, *jopp, *jlayer;
   double *jc, *jk, *jt, *jf, *jd;
+  // tangent-linear sensitivity (lpm_tangent_begin): per direction the
+  // tangents of dLp [nb], of the state variables [n * nstate], of the
+  // equilibrium positions and internal forces [n * dim], and the parameter
+  // direction [n * np]; the stress tangent and the tangent of dLp in the
+  // sliced bond layout are scratch
+  double *tg_dlp, *tg_sv, *tg_x, *tg_pin, *tg_dp, *tg_stress, *tg_jdl;
 };
 
 // One device-resident copy of a step's state (lpm_checkpoint_save).
@@ -169,6 +175,9 @@ struct lpm_handle {
   std::vector<void*> allocations;
   std::vector<lpm::Checkpoint> checkpoints;
   int64_t jslots = 0;  // adjoint: slots of the sliced bond data
+  int tg_ndir = 0;      // tangent directions carried by the load steps (0: off)
+  int tg_cap = 0;       // directions the tangent buffers hold
+  double tg_tol = 1e-12;
   // the FP64 solve's iteration loop as a graph (for the solution vector fp_graph_x)
   cudaGraph_t fp_graph = nullptr;
   cudaGraphExec_t fp_exec = nullptr;
@@ -205,6 +214,8 @@ int adjoint_buffers(lpm_handle* h);
 int adjoint_apply(lpm_handle* h, const double* v, double* y);
 int adjoint_step(lpm_handle* h, const double* a, const double* c, double tol, long long maxit, int accumulate,
                  double* gKn, double* gTv, long long* iters, double* relres);
+int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double tol);
+int tangent_step(lpm_handle* h);
 int checkpoint_save(lpm_handle* h, int* id);
 int checkpoint_restore(lpm_handle* h, int id);
 int checkpoint_drop(lpm_handle* h, int id);
