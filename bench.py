@@ -26,6 +26,8 @@ Reported (one JSON line on rank 0):
   setup        the GPU bond search (checked identical to the CPU
                generator's bonds) and the creation of the device lattice
   fatigue      compact-tension fatigue cycles at full size (configuration 5)
+  j2_sensitivity  cost of carrying d/d(yield stress) and d/d(hardening)
+               through J2 load steps of a BCC polycrystal
 
 --impl reference times the CPU oracle alone on the same workload.
 Multi-GPU runs are independent replicas (the path has no exchange step).
@@ -373,6 +375,61 @@ def fatigue_cost(capi, local, cycles=3):
             "cycle": "1 increment up, 1 down, cycle jump 1000 (lpm_fatigue_cycle)", "precision": "mixed"}
 
 
+def j2_sensitivity_cost(capi, local, ncell=40, steps=4):
+    """The tangent-linear sensitivity of a J2 load history (configuration 4
+    form: BCC polycrystal, 20 grains, E = 110 GPa, nu = 0.34, yield 900 MPa,
+    hardening 1 GPa) with respect to the yield stress and the hardening
+    modulus: device time of `steps` plastic load steps without and with the
+    two tangent directions carried along (mixed precision, tangent solves
+    to 1e-10)."""
+    import math
+    import torch
+    import __graft_entry__ as ge
+    lat = ge.load_package().lattice
+    xyz, gid = lat.bcc_polycrystal(ncell, 0.2, 20, 11)
+    cell = lat.UnitCell(lat.BCC3D, 0.2 * math.sqrt(3.0) / 4.0)
+    xyz = xyz[lat.prune_weak(xyz, cell, 6)]
+    p1, p2, layer = lat.find_bonds(xyz, cell)
+    Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(110e3, 0.34, layout="row"))
+    z = xyz[:, 2]
+    bottom, top = np.where(z < 0.1)[0], np.where(z > z.max() - 0.1)[0]
+    du = 0.0005 * (z.max() - z.min())
+    out = {}
+    for tangent in (False, True):
+        g = capi.Lattice(3, xyz, p1, p2, layer, Kn, Tv, cell.particle_volume, cell.nneighbors)
+        g.set_law(capi.LAW_J2, [110e3, 0.34, 900.0, 0.0, 1e3, 0.0, 0.0])
+        g.update()
+        gb, gt = g.add_group(bottom), g.add_group(top)
+        bcs = [("disp", gb, 0, 0.0), ("disp", gb, 1, 0.0), ("disp", gb, 2, 0.0), ("disp", gt, 2, du)]
+        opts = dict(solver=capi.SOLVER_FATIGUE_STATIC, tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_MIXED,
+                    max_iter=30, tol=1e-5, cg_tol=1e-10)
+        for _ in range(3):  # up to yield
+            g.load_step(bcs, **opts)
+        if tangent:
+            g.tangent_begin([[0, 0, 1, 0, 0, 0, 0], [0, 0, 0, 0, 1, 0, 0]], tol=1e-10)
+        stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        g.reset_stats()
+        g.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            r = g.load_step(bcs, **opts)
+            if r["status"] != 0:
+                raise RuntimeError("J2 step did not converge: %s" % r)
+        e1.record(stream)
+        e1.synchronize()
+        st = g.stats()
+        out["with" if tangent else "without"] = (e0.elapsed_time(e1) / steps, st["tangent_cg_iters"] / steps)
+        plastic = bool(np.abs(g.download(capi.B_DLP)).max() > 0)
+        g.close()
+    return {"workload": "BCC polycrystal %d^3 cells, 20 grains (%d particles), J2, plastic steps" % (ncell, len(xyz)),
+            "directions": "d/d(yield stress), d/d(hardening modulus)", "forward_ms_per_step": out["without"][0],
+            "with_tangents_ms_per_step": out["with"][0],
+            "relative_to_forward_step": out["with"][0] / out["without"][0],
+            "tangent_cg_iters_per_step": out["with"][1], "plastic": plastic}
+
+
 def force_bytes(nb, n):
     """Algorithmic bytes of one force pass: per directed bond the partner
     index, dis0, dLp, bdamage, Kn, Tv and the bond force written; per
@@ -585,6 +642,7 @@ def run_gb300(args):
                            "force_algorithmic_bytes": fb}
     line["setup"] = setup_cost(w, capi)
     line["fatigue"] = fatigue_cost(capi, local)
+    line["j2_sensitivity"] = j2_sensitivity_cost(capi, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         oracle, o = cpu_oracle_system(w, threads)
