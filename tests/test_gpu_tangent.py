@@ -8,7 +8,7 @@ import math
 import numpy as np
 import pytest
 
-from lpm_cases import lat, make_gpu, pkg
+from lpm_cases import gpu_bcs, lat, make_gpu, pkg, plate, tension_bcs
 
 capi = pkg.capi
 pytestmark = pytest.mark.gpu
@@ -77,6 +77,41 @@ def test_j2_reaction_curve_tangents_match_central_differences():
         jm = ((run(args, SIGY - hs, H - hh)[0] - target) ** 2).sum()
         fdj = (jp - jm) / (2 * (hs + hh))
         assert abs(grad[k] - fdj) <= 1e-5 * abs(fdj), (k, grad[k], fdj)
+
+
+def test_j2_tangents_on_a_hexagonal_plate():
+    """The 2-D path: a hexagonal plate pulled past yield, per-step reaction
+    tangents along the yield stress against central differences."""
+    args = plate(9, 9, E=E, nu=NU)
+    dim, xyz = args[0], args[1]
+    L = xyz[:, 1].max() - xyz[:, 1].min()
+    du = 0.006 * L
+    groups, _, _ = tension_bcs(xyz, dim, du)
+
+    def curve(sigy, dirs=None):
+        g = make_gpu(*args)
+        g.set_law(capi.LAW_J2, [E, NU, sigy, XI, H, 0.0, 0.0])
+        g.update()
+        bcs = gpu_bcs(g, groups, dim, du)
+        if dirs is not None:
+            g.tangent_begin(dirs, tol=1e-13)
+        R, dR = [], []
+        for _ in range(4):
+            r = g.load_step(bcs, **OPTS)
+            assert r["status"] == 0, r
+            R.append(g.download(capi.F_PIN)[groups["top"], 1].sum())
+            if dirs is not None:
+                dR.append(g.tangent_get(0, capi.T_PIN)[groups["top"], 1].sum())
+        plastic = np.abs(g.download(capi.B_DLP)).max() > 0
+        g.close()
+        return np.array(R), np.array(dR), plastic
+
+    _, dR, plastic = curve(SIGY, [[0, 0, 1, 0, 0, 0, 0]])
+    assert plastic
+    h = 1e-5 * SIGY
+    fd = (curve(SIGY + h)[0] - curve(SIGY - h)[0]) / (2 * h)
+    assert np.abs(fd).max() > 0
+    assert np.abs(dR - fd).max() <= 1e-5 * np.abs(fd).max(), (dR, fd)
 
 
 def test_tangent_refuses_other_laws():
