@@ -85,3 +85,30 @@ class LoadHistory:
         for cid in self.checkpoints.values():
             self.g.checkpoint_drop(cid)
         self.checkpoints = {}
+
+
+def reaction_curve_sensitivity(lattice, steps, group, axis, dparams, tangent_tol=1e-12, **step_kwargs):
+    """A load history of the J2 law with its tangent-linear sensitivity
+    (``lpm_tangent_begin``): runs the load steps ``steps`` (``load_step``
+    bc lists) and returns the reaction curve R_n (the internal force of the
+    particles ``group`` along ``axis``, summed, at each step's equilibrium)
+    and its derivatives dR_n/dtheta_k along the parameter directions
+    ``dparams`` (one row of the law's parameters, or an (N, np) array, per
+    direction), shapes (steps,) and (steps, directions).  A response of the
+    curve, e.g. sum (R_n - target_n)^2, then has the gradient
+    sum 2 (R_n - target_n) dR_n/dtheta.  tangent_tol is the relative residual
+    of the tangent solves; step_kwargs go to ``load_step``."""
+    g = lattice
+    idx = np.asarray(group, dtype=np.int64)
+    g.tangent_begin(dparams, tol=tangent_tol)
+    R, dR = [], []
+    try:
+        for n, bcs in enumerate(steps):
+            r = g.load_step(bcs, **step_kwargs)
+            if r["status"] != capi.OK:
+                raise RuntimeError("load step %d did not converge: %s" % (n, r))
+            R.append(g.download(capi.F_PIN)[idx, axis].sum())
+            dR.append([g.tangent_get(k, capi.T_PIN)[idx, axis].sum() for k in range(len(dparams))])
+    finally:
+        g.tangent_end()
+    return np.array(R), np.array(dR)

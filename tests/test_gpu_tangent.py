@@ -39,21 +39,20 @@ def run(args, sigy, h, dirs=None):
     bottom, top = np.where(z < 0.1)[0], np.where(z > z.max() - 0.1)[0]
     du = 0.004 * (z.max() - z.min())
     gb, gt = g.add_group(bottom), g.add_group(top)
+    steps = [[("disp", gb, 0, 0.0), ("disp", gb, 1, 0.0), ("disp", gb, 2, 0.0), ("disp", gt, 2, sgn * du)]
+             for sgn in STEPS]
     if dirs is not None:
-        g.tangent_begin(dirs, tol=1e-13)
-    R, dR = [], []
-    for sgn in STEPS:
-        bcs = [("disp", gb, 0, 0.0), ("disp", gb, 1, 0.0), ("disp", gb, 2, 0.0), ("disp", gt, 2, sgn * du)]
-        r = g.load_step(bcs, **OPTS)
-        assert r["status"] == 0, r
-        R.append(g.download(capi.F_PIN)[top, 2].sum())
-        if dirs is not None:
-            dR.append([g.tangent_get(k, capi.T_PIN)[top, 2].sum() for k in range(len(dirs))])
+        R, dR = pkg.adjoint.reaction_curve_sensitivity(g, steps, top, 2, dirs, tangent_tol=1e-13, **OPTS)
+    else:
+        R, dR = [], None
+        for bcs in steps:
+            r = g.load_step(bcs, **OPTS)
+            assert r["status"] == 0, r
+            R.append(g.download(capi.F_PIN)[top, 2].sum())
+        R = np.array(R)
     plastic = np.abs(g.download(capi.B_DLP)).max() > 0
-    if dirs is not None:
-        g.tangent_end()
     g.close()
-    return np.array(R), np.array(dR), plastic
+    return R, dR, plastic
 
 
 def test_j2_reaction_curve_tangents_match_central_differences():
