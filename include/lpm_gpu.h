@@ -342,8 +342,9 @@ int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y);
  * (lpm_load_step) also carries ndir tangent states along: dparams
  * (ndir x n x np, host, np the law's parameters per particle) gives each
  * direction's change of the parameters, e.g. 1 in the yield-stress column
- * for d/d(sigma_y).  At each step, after Newton and before the state update
- * (solver_fatigue.h:266, solver_static.h:122): the change of the
+ * for d/d(sigma_y).  At each state update (lpm_update_state, or the one
+ * inside lpm_load_step: solver_fatigue.h:266, solver_static.h:122), first,
+ * at the converged equilibrium: the change of the
  * equilibrium, H_ff dx_f = -(dPin/d dLp . d dLp)_f with dx = 0 on
  * constrained DOFs (CG on the exact Jacobian to `tol`); the change of the
  * internal forces (LPM_T_PIN) and positions (LPM_T_XYZ) of that equilibrium;

@@ -621,10 +621,6 @@ int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts
       st = lpm_newton(h, o->max_iter, o->tol, o->precision, o->cg_tol, o->cg_maxit, &ni);
       if (st < 0) return st;
       failed = ni >= o->max_iter;
-      if (!failed && h->tg_ndir > 0) {  // the tangents of this equilibrium and of the state update
-        st = tangent_step(h);
-        if (st) return st;
-      }
       if (!failed) {  // solver_fatigue.h:266-267
         st = launch_update_state(h);
         if (st) return st;
@@ -641,10 +637,6 @@ int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts
         if (ni >= o->max_iter) {
           failed = true;
           break;
-        }
-        if (h->tg_ndir > 0) {
-          st = tangent_step(h);
-          if (st) return st;
         }
         st = launch_update_state(h);  // solver_static.h:122-123
         if (st) return st;

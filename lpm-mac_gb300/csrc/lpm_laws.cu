@@ -243,6 +243,12 @@ int read_flag(lpm_handle* h, int* flag, int* out) {
 }  // namespace
 
 int launch_update_state(lpm_handle* h) {
+  // with tangent directions on, their step comes first: it needs the state
+  // before the update (lpm_tangent_begin)
+  if (h->tg_ndir > 0) {
+    const int st = tangent_step(h);
+    if (st) return st;
+  }
   if (h->law == 0) return LPM_OK;  // ParticleElastic has no state update
   const int T = 128;
   k_update_state<<<grid_for(h->n, T), T, 0, h->stream>>>(law_view(h));
