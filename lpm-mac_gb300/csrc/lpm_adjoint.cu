@@ -602,6 +602,13 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
     h->err = "tangent: the J2 law (lpm_set_law 2) is required";
     return LPM_ERR_STATE;
   }
+  // E and nu also set the bond constants Kn, Tv (per-bond inputs), which the
+  // tangent does not follow: directions in them are refused
+  for (int64_t t = 0; t < (int64_t)ndir * h->n; ++t)
+    if (dparams_host[t * h->law_np] != 0.0 || dparams_host[t * h->law_np + 1] != 0.0) {
+      h->err = "tangent: directions in E or nu also change the bond constants; use lpm_backward_step for those";
+      return LPM_ERR_ARG;
+    }
   if (ndir > h->tg_cap) {  // buffers for ndir directions (smaller ones stay owned by the handle)
     const size_t N = (size_t)h->n, B = (size_t)std::max<int64_t>(h->nb, 1), m = N * h->dim;
     d.tg_dlp = (double*)dev_alloc(h, sizeof(double) * ndir * B);

@@ -113,10 +113,15 @@ def test_j2_tangents_on_a_hexagonal_plate():
     assert np.abs(dR - fd).max() <= 1e-5 * np.abs(fd).max(), (dR, fd)
 
 
-def test_tangent_refuses_other_laws():
+def test_tangent_refuses_other_laws_and_elastic_directions():
     args = polycrystal(4, ngrain=2)
     g = make_gpu(*args)
     g.update()
     with pytest.raises(capi.LpmError):
         g.tangent_begin([[0.0]])
+    g.set_law(capi.LAW_J2, [E, NU, SIGY, XI, H, 0.0, 0.0])
+    with pytest.raises(capi.LpmError):
+        g.tangent_begin([[1.0, 0, 0, 0, 0, 0, 0]])
+    g.tangent_begin([[0, 0, 1.0, 0, 0, 0, 0]])
+    g.tangent_end()
     g.close()
