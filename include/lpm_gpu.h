@@ -351,15 +351,17 @@ int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y);
  * then the radial return (particle_j2plasticity.h:78-140) differentiated,
  * which advances the tangents of the state variables and of dLp.  A
  * response R(Pin, x) summed over steps has dR/dtheta = sum over steps of
- * its partial derivatives times these tangents.  Directions may change
- * sigma_y, xi, H and A; E and nu also set the bond constants, which the
- * tangent does not follow, so directions in them give LPM_ERR_ARG (the
- * bond-constant gradients come from lpm_backward_step).  Damage is held fixed
+ * its partial derivatives times these tangents.  E and nu also set the
+ * bond constants (per-bond inputs): a direction that changes them gives the
+ * constants' changes with lpm_tangent_bond_constants (dKn, dTv: nb each,
+ * stored bond order; e.g. from the UnitCell map's derivative) after
+ * lpm_tangent_begin.  Damage is held fixed
  * (bonds intact or broken on both sides; LPM_ERR_STATE otherwise); a
  * load step that cuts back fails with LPM_ERR_STATE. */
 #define LPM_T_PIN 1 /* n x dim: d Pin / d theta at the step's equilibrium */
 #define LPM_T_XYZ 2 /* n x dim: d x / d theta at the step's equilibrium */
 int lpm_tangent_begin(lpm_handle* h, int ndir, const double* dparams, double tol);
+int lpm_tangent_bond_constants(lpm_handle* h, int dir, const double* dKn, const double* dTv);
 int lpm_tangent_get(const lpm_handle* h, int dir, int field, double* dst);
 int lpm_tangent_end(lpm_handle* h);
 

@@ -134,6 +134,7 @@ def load(build_if_needed=True):
         "lpm_backward_step": [H, dp, dp, ctypes.c_double, i64, ctypes.c_int, dp, dp, ctypes.POINTER(AdjointResult)],
         "lpm_apply_jacobian": [H, dp, dp],
         "lpm_tangent_begin": [H, ctypes.c_int, dp, ctypes.c_double],
+        "lpm_tangent_bond_constants": [H, ctypes.c_int, dp, dp],
         "lpm_tangent_get": [H, ctypes.c_int, ctypes.c_int, dp],
         "lpm_tangent_end": [H],
         "lpm_checkpoint_save": [H, ip],
@@ -160,7 +161,8 @@ def exported_symbols():
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
             "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
             "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
-            "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_get", "lpm_tangent_end"]
+            "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_bond_constants", "lpm_tangent_get",
+            "lpm_tangent_end"]
 
 
 def set_device(device):
@@ -493,16 +495,24 @@ class Lattice:
         self._check(self._L.lpm_apply_jacobian(self.h, _d(v), _d(y)))
         return y
 
-    def tangent_begin(self, dparams, tol=1e-12):
+    def tangent_begin(self, dparams, tol=1e-12, dbond=None):
         """Carries len(dparams) tangent directions through the following load
         steps (J2 law): each direction an (N, np) array, or one row of np
-        values for all particles, of parameter changes."""
+        values for all particles, of parameter changes.  dbond: per
+        direction None or (dKn, dTv), the bond constants' changes in input
+        bond order (for directions in E or nu)."""
         rows = []
         for d in dparams:
             d = np.asarray(d, dtype=np.float64)
             rows.append(np.broadcast_to(d, (self.n, d.shape[-1])))
         dp = np.ascontiguousarray(np.stack(rows)) if rows else np.zeros(1)
         self._check(self._L.lpm_tangent_begin(self.h, len(rows), _d(dp), float(tol)))
+        for k, db in enumerate(dbond or []):
+            if db is None:
+                continue
+            dkn = np.ascontiguousarray(np.asarray(db[0], dtype=np.float64)[self.bond_perm])
+            dtv = np.ascontiguousarray(np.asarray(db[1], dtype=np.float64)[self.bond_perm])
+            self._check(self._L.lpm_tangent_bond_constants(self.h, k, _d(dkn), _d(dtv)))
 
     def tangent_get(self, direction, field=T_PIN):
         """The step's d Pin (T_PIN) or d x (T_XYZ) along one direction, (N, dim)."""

@@ -110,9 +110,10 @@ struct JacView {
 };
 
 // Pass 1 of H v: d dLe per slot and the per-layer sums d D_i^l, then d f.
-// With dlp (per slot) the plastic stretches move too: d dLe -= d dLp.
+// With dlp (per slot) the plastic stretches move too: d dLe -= d dLp; with
+// dfk (per slot) the bond constants too: d f += dfk.
 __global__ void k_jvp_bonds(int n, int dim, JacView J, const double* __restrict__ v, const double* __restrict__ dlp,
-                            const CgScalars* cg) {
+                            const double* __restrict__ dfk, const CgScalars* cg) {
   if (cg && cg->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -137,7 +138,7 @@ __global__ void k_jvp_bonds(int n, int dim, JacView J, const double* __restrict_
   }
   for (int k = 0; k < len; ++k) {
     const int64_t s = s0 + 32 * (int64_t)k;
-    J.jd[s] = J.jk[s] * J.jd[s] + J.jt[s] * (J.jlayer[s] == 0 ? dD0 : dD1);
+    J.jd[s] = J.jk[s] * J.jd[s] + J.jt[s] * (J.jlayer[s] == 0 ? dD0 : dD1) + (dfk ? dfk[s] : 0.0);
   }
 }
 
@@ -278,6 +279,21 @@ __global__ void k_dlp_slots(int n, const int64_t* __restrict__ bptr, const int* 
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) out[slot_of[b]] = is_broken(bdamage[b]) ? 0.0 : dlp[b];
+}
+
+// The bond force's change from changes of the bond constants, in the
+// sliced layout: d f_b = w_b (2 dKn_b dLe_b + 2 dTv_b D_i^l) (broken bonds 0).
+__global__ void k_dfk_slots(int n, const int64_t* __restrict__ bptr, const int* __restrict__ slot_of,
+                            const int* __restrict__ blayer, const double* __restrict__ bdamage,
+                            const double* __restrict__ dLe, const double* __restrict__ dle_tot,
+                            const double* __restrict__ dkn, const double* __restrict__ dtv, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    const double w = 1.0 - bdamage[b];
+    out[slot_of[b]] = is_broken(bdamage[b]) ? 0.0
+                                            : 2.0 * w * (dkn[b] * dLe[b] + dtv[b] * dle_tot[NL * i + blayer[b]]);
+  }
 }
 
 // g = -q on the free DOFs, 0 on the constrained ones.
@@ -478,10 +494,10 @@ static int jacobian_prepare(lpm_handle* h) {
 // y = H v (mask: zero the constrained rows); with cg, p.q and alpha too;
 // with dlp (sliced layout) the derivative along a change of dLp as well.
 static int apply_jacobian(lpm_handle* h, const double* v, double* y, bool masked, CgScalars* cg,
-                          const double* dlp = nullptr) {
+                          const double* dlp = nullptr, const double* dfk = nullptr) {
   Dev& d = h->d;
   const JacView J{d.jbase, d.jp2, d.jopp, d.jlayer, d.jc, d.jk, d.jt, d.jf, d.jd, h->jslots};
-  k_jvp_bonds<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, h->dim, J, v, dlp, cg);
+  k_jvp_bonds<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, h->dim, J, v, dlp, dfk, cg);
   LPM_LAUNCHED(h, "k_jvp_bonds");
   k_jvp_particles<<<grid_for(h->n, 256, kMaxRedBlocks), 256, 0, h->stream>>>(
       h->n, h->dim, J, v, masked ? d.mask : nullptr, y, cg, d.red.partials, d.red.ticket + 8);
@@ -602,13 +618,7 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
     h->err = "tangent: the J2 law (lpm_set_law 2) is required";
     return LPM_ERR_STATE;
   }
-  // E and nu also set the bond constants Kn, Tv (per-bond inputs), which the
-  // tangent does not follow: directions in them are refused
-  for (int64_t t = 0; t < (int64_t)ndir * h->n; ++t)
-    if (dparams_host[t * h->law_np] != 0.0 || dparams_host[t * h->law_np + 1] != 0.0) {
-      h->err = "tangent: directions in E or nu also change the bond constants; use lpm_backward_step for those";
-      return LPM_ERR_ARG;
-    }
+
   if (ndir > h->tg_cap) {  // buffers for ndir directions (smaller ones stay owned by the handle)
     const size_t N = (size_t)h->n, B = (size_t)std::max<int64_t>(h->nb, 1), m = N * h->dim;
     d.tg_dlp = (double*)dev_alloc(h, sizeof(double) * ndir * B);
@@ -617,7 +627,10 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
     d.tg_pin = (double*)dev_alloc(h, sizeof(double) * ndir * m);
     d.tg_dp = (double*)dev_alloc(h, sizeof(double) * ndir * N * h->law_np);
     d.tg_stress = (double*)dev_alloc(h, sizeof(double) * 6 * N);
-    if (!d.tg_dlp || !d.tg_sv || !d.tg_x || !d.tg_pin || !d.tg_dp || !d.tg_stress) return LPM_ERR_NOMEM;
+    d.tg_dkn = (double*)dev_alloc(h, sizeof(double) * ndir * B);
+    d.tg_dtv = (double*)dev_alloc(h, sizeof(double) * ndir * B);
+    if (!d.tg_dlp || !d.tg_sv || !d.tg_x || !d.tg_pin || !d.tg_dp || !d.tg_stress || !d.tg_dkn || !d.tg_dtv)
+      return LPM_ERR_NOMEM;
     h->tg_cap = ndir;
   }
   h->tg_ndir = 0;
@@ -627,11 +640,30 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
   LPM_CUDA(h, cudaMemsetAsync(d.tg_sv, 0, sizeof(double) * ndir * N * h->nstate, h->stream));
   LPM_CUDA(h, cudaMemsetAsync(d.tg_x, 0, sizeof(double) * ndir * m, h->stream));
   LPM_CUDA(h, cudaMemsetAsync(d.tg_pin, 0, sizeof(double) * ndir * m, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_dkn, 0, sizeof(double) * ndir * B, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_dtv, 0, sizeof(double) * ndir * B, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.tg_dp, dparams_host, sizeof(double) * ndir * N * h->law_np, cudaMemcpyHostToDevice,
                               h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   h->tg_ndir = ndir;
   h->tg_tol = tol;
+  h->tg_bond = false;
+  return LPM_OK;
+}
+
+int tangent_bond_constants(lpm_handle* h, int dir, const double* dkn_host, const double* dtv_host) {
+  Dev& d = h->d;
+  if (dir < 0 || dir >= h->tg_ndir || !dkn_host || !dtv_host) {
+    h->err = "tangent: bad direction or NULL bond-constant changes";
+    return LPM_ERR_ARG;
+  }
+  const size_t B = (size_t)std::max<int64_t>(h->nb, 1);
+  LPM_CUDA(h, cudaMemcpyAsync(d.tg_dkn + (size_t)dir * B, dkn_host, sizeof(double) * h->nb, cudaMemcpyHostToDevice,
+                              h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.tg_dtv + (size_t)dir * B, dtv_host, sizeof(double) * h->nb, cudaMemcpyHostToDevice,
+                              h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->tg_bond = true;
   return LPM_OK;
 }
 
@@ -650,7 +682,8 @@ int tangent_step(lpm_handle* h) {
   if (st) return st;
   if (!d.tg_jdl) {
     d.tg_jdl = (double*)zeros_dev(h, sizeof(double) * (size_t)std::max<int64_t>(h->jslots, 1));
-    if (!d.tg_jdl) return LPM_ERR_NOMEM;
+    d.tg_jdk = (double*)zeros_dev(h, sizeof(double) * (size_t)std::max<int64_t>(h->jslots, 1));
+    if (!d.tg_jdl || !d.tg_jdk) return LPM_ERR_NOMEM;
   }
   LPM_CUDA(h, cudaMemsetAsync(d.adj_a, 0, sizeof(double) * m, h->stream));  // a zero position change
   const JacView J{d.jbase, d.jp2, d.jopp, d.jlayer, d.jc, d.jk, d.jt, d.jf, d.jd, h->jslots};
@@ -662,8 +695,17 @@ int tangent_step(lpm_handle* h) {
     const double* tdp = d.tg_dp + (size_t)k * n * h->law_np;
     k_dlp_slots<<<grid_for(n, 128), 128, 0, h->stream>>>(n, d.bptr, d.jslot_of, d.bdamage, tdlp, d.tg_jdl);
     LPM_LAUNCHED(h, "k_dlp_slots");
-    // H_ff dx_f = -(dPin/d dLp . d dLp)_f
-    st = apply_jacobian(h, d.adj_a, d.adj_q, false, nullptr, d.tg_jdl);
+    const double* dfk = nullptr;
+    if (h->tg_bond) {  // the bond constants' changes (lpm_tangent_bond_constants)
+      const size_t B = (size_t)std::max<int64_t>(h->nb, 1);
+      k_dfk_slots<<<grid_for(n, 128), 128, 0, h->stream>>>(n, d.bptr, d.jslot_of, d.blayer, d.bdamage, d.dLe,
+                                                          d.dle_tot, d.tg_dkn + (size_t)k * B,
+                                                          d.tg_dtv + (size_t)k * B, d.tg_jdk);
+      LPM_LAUNCHED(h, "k_dfk_slots");
+      dfk = d.tg_jdk;
+    }
+    // H_ff dx_f = -(dPin/d dLp . d dLp + dPin/d(Kn, Tv) . d(Kn, Tv))_f
+    st = apply_jacobian(h, d.adj_a, d.adj_q, false, nullptr, d.tg_jdl, dfk);
     if (st) return st;
     k_tg_rhs<<<grid_for(m, 256), 256, 0, h->stream>>>(n, dim, d.adj_q, d.mask, d.adj_g);
     LPM_LAUNCHED(h, "k_tg_rhs");
@@ -677,7 +719,7 @@ int tangent_step(lpm_handle* h) {
       return LPM_NOT_CONVERGED;
     }
     // dPin and the stress change at the equilibrium (pass 1 leaves d f in J.jd)
-    st = apply_jacobian(h, tx, tpin, false, nullptr, d.tg_jdl);
+    st = apply_jacobian(h, tx, tpin, false, nullptr, d.tg_jdl, dfk);
     if (st) return st;
     k_jvp_stress<<<grid_for(n, 128), 128, 0, h->stream>>>(n, dim, J, tx, d.bptr, d.bp2, d.jslot_of, d.opp, d.bforce,
                                                          d.cs, d.dis, d.nbonds, h->particle_volume, h->nneighbors,

@@ -839,6 +839,11 @@ int lpm_tangent_begin(lpm_handle* h, int ndir, const double* dparams, double tol
   return tangent_begin(h, ndir, dparams, tol);
 }
 
+int lpm_tangent_bond_constants(lpm_handle* h, int dir, const double* dKn, const double* dTv) {
+  if (!h) return LPM_ERR_ARG;
+  return tangent_bond_constants(h, dir, dKn, dTv);
+}
+
 int lpm_tangent_get(const lpm_handle* h, int dir, int field, double* dst) {
   if (!h || !dst || dir < 0 || dir >= h->tg_ndir || (field != LPM_T_PIN && field != LPM_T_XYZ)) return LPM_ERR_ARG;
   lpm_handle* hh = const_cast<lpm_handle*>(h);

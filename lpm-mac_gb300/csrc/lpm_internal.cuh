@@ -134,6 +134,7 @@ struct Dev {
   // direction [n * np]; the stress tangent and the tangent of dLp in the
   // sliced bond layout are scratch
   double *tg_dlp, *tg_sv, *tg_x, *tg_pin, *tg_dp, *tg_stress, *tg_jdl;
+  double *tg_dkn, *tg_dtv, *tg_jdk;  // per direction d Kn, d Tv [nb]; the force change in sliced layout
 };
 
 // One device-resident copy of a step's state (lpm_checkpoint_save).
@@ -178,6 +179,7 @@ struct lpm_handle {
   int tg_ndir = 0;      // tangent directions carried by the load steps (0: off)
   int tg_cap = 0;       // directions the tangent buffers hold
   double tg_tol = 1e-12;
+  bool tg_bond = false;  // some direction changes the bond constants
   // the FP64 solve's iteration loop as a graph (for the solution vector fp_graph_x)
   cudaGraph_t fp_graph = nullptr;
   cudaGraphExec_t fp_exec = nullptr;
@@ -216,6 +218,7 @@ int adjoint_step(lpm_handle* h, const double* a, const double* c, double tol, lo
                  double* gKn, double* gTv, long long* iters, double* relres);
 int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double tol);
 int tangent_step(lpm_handle* h);
+int tangent_bond_constants(lpm_handle* h, int dir, const double* dkn_host, const double* dtv_host);
 int checkpoint_save(lpm_handle* h, int* id);
 int checkpoint_restore(lpm_handle* h, int id);
 int checkpoint_drop(lpm_handle* h, int id);

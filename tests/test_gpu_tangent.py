@@ -113,15 +113,48 @@ def test_j2_tangents_on_a_hexagonal_plate():
     assert np.abs(dR - fd).max() <= 1e-5 * np.abs(fd).max(), (dR, fd)
 
 
-def test_tangent_refuses_other_laws_and_elastic_directions():
+def test_j2_tangent_along_youngs_modulus():
+    """A direction in E changes the return map's shear modulus and, through
+    the UnitCell map, every bond's constants (lpm_tangent_bond_constants):
+    per-step reaction tangents against central differences of runs with the
+    constants rebuilt at E +- h."""
+    d0, xyz, p1, p2, layer, _, _, cell = plate(9, 9, E=E, nu=NU)
+    L = xyz[:, 1].max() - xyz[:, 1].min()
+    du = 0.006 * L
+    groups, _, _ = tension_bcs(xyz, 2, du)
+
+    def curve(e, tangent=False):
+        Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(e, NU, plane_stress=True, layout="row"))
+        g = make_gpu(2, xyz, p1, p2, layer, Kn, Tv, cell)
+        g.set_law(capi.LAW_J2, [e, NU, SIGY, XI, H, 0.0, 0.0])
+        g.update()
+        bcs = gpu_bcs(g, groups, 2, du)
+        if tangent:
+            dm = cell.elastic_constants_grad(e, NU, plane_stress=True, layout="row")[0]
+            dKn, dTv = lat.bond_constants(cell, layer, dm)
+            g.tangent_begin([[1.0, 0, 0, 0, 0, 0, 0]], tol=1e-13, dbond=[(dKn, dTv)])
+        R, dR = [], []
+        for _ in range(4):
+            r = g.load_step(bcs, **OPTS)
+            assert r["status"] == 0, r
+            R.append(g.download(capi.F_PIN)[groups["top"], 1].sum())
+            if tangent:
+                dR.append(g.tangent_get(0, capi.T_PIN)[groups["top"], 1].sum())
+        plastic = np.abs(g.download(capi.B_DLP)).max() > 0
+        g.close()
+        return np.array(R), np.array(dR), plastic
+
+    _, dR, plastic = curve(E, True)
+    assert plastic
+    h = 1e-5 * E
+    fd = (curve(E + h)[0] - curve(E - h)[0]) / (2 * h)
+    assert np.abs(dR - fd).max() <= 1e-5 * np.abs(fd).max(), (dR, fd)
+
+
+def test_tangent_refuses_other_laws():
     args = polycrystal(4, ngrain=2)
     g = make_gpu(*args)
     g.update()
     with pytest.raises(capi.LpmError):
         g.tangent_begin([[0.0]])
-    g.set_law(capi.LAW_J2, [E, NU, SIGY, XI, H, 0.0, 0.0])
-    with pytest.raises(capi.LpmError):
-        g.tangent_begin([[1.0, 0, 0, 0, 0, 0, 0]])
-    g.tangent_begin([[0, 0, 1.0, 0, 0, 0, 0]])
-    g.tangent_end()
     g.close()
