@@ -19,7 +19,8 @@
 // batch.
 //
 // Mixed precision: the same recurrence on an FP32 copy of A with FP32
-// vectors and FP64 dot accumulation.  The FP32 product is taken in
+// vectors; the dots accumulate as compensated FP32 pairs, converted to FP64
+// once per block, and the scalars are FP64.  The FP32 product is taken in
 // difference form, (A p)_i = S_i p_i + sum_j A_ij (p_j - p_i) with S_i the
 // block row sum of A (exact algebra).  The stiffness rows nearly sum to zero
 // (rigid translations cost no force), so for the smooth directions that CG
@@ -28,9 +29,11 @@
 // compensated accumulation (dot2_acc) removes the rounding of the sum.
 // Without both, the FP32 iterate carries errors along the smooth directions
 // that its residual barely shows, and the next Newton solve pays for them
-// (about 50% more iterations at 101^3).  With both, every solve of a load
-// step takes within a few per cent of the FP64 iteration count.  The recurrence runs with reliable updates (residual
-// replacement): when the iterated residual has fallen by kDelta since the
+// (about 50% more iterations at 101^3).  With both, the first solve of a
+// load step takes the FP64 iteration count and later ones 10-30% more, from
+// the FP32 rounding of the operator's values.  The recurrence runs with
+// reliable updates (residual replacement): when the iterated residual has
+// fallen by kDelta since the
 // last update, the FP32 solution increment is folded into the FP64 solution,
 // the residual is recomputed in FP64 as b - A64 x and replaces the iterated
 // one, and the iteration continues with its search direction.  The solve
