@@ -35,9 +35,10 @@ __global__ void k_geometry_force(int n, const double* __restrict__ x, const int6
     const double d0 = dis0[b];
     const double dl = br ? 0.0 : (d - d0);
     const double e = br ? 0.0 : (d - d0 - dLp[b]);
-    const double c0 = br ? 0.0 : dx / d, c1 = br ? 0.0 : dy / d, c2 = br ? 0.0 : dz / d;
+    const double rd = 1.0 / d;  // one division per bond; the four quotients below are products
+    const double c0 = br ? 0.0 : dx * rd, c1 = br ? 0.0 : dy * rd, c2 = br ? 0.0 : dz * rd;
     dis[b] = d;
-    bstrain[b] = br ? 0.0 : dl / d;
+    bstrain[b] = br ? 0.0 : dl * rd;
     dLe[b] = e;
     cs[3 * b] = c0;
     cs[3 * b + 1] = c1;
