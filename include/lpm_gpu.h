@@ -88,8 +88,10 @@ typedef struct lpm_handle lpm_handle;
  * opposite bond in the same layer (LPM_ERR_TOPOLOGY otherwise). */
 /* Selects the CUDA device for the calling host thread's later lpm_create
  * calls (the library links its own CUDA runtime, so a device chosen through
- * another runtime instance does not carry over).  Library-level addition:
- * the reference runs on the host only. */
+ * another runtime instance does not carry over).  Every later call on a
+ * handle must come from a thread whose device is the handle's: the library
+ * launches on the handle's stream and does not switch devices itself.
+ * Library-level addition: the reference runs on the host only. */
 int lpm_set_device(int device);
 
 int lpm_create(int dim, int n, int64_t nb, const double* xyz, const int* p1, const int* p2, const int* layer,
