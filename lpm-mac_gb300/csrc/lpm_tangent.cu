@@ -156,6 +156,8 @@ __device__ __forceinline__ void diag_block(const AsmView& v, int i, double (&K)[
   K[2][2] = k22;
 }
 
+constexpr int kMatch = 8;  // common neighbours collected per merge chunk
+
 template <int DIM>
 __device__ __forceinline__ void off_block(const AsmView& v, int i, int j, double (&K)[3][3]) {
 #pragma unroll
@@ -173,14 +175,26 @@ __device__ __forceinline__ void off_block(const AsmView& v, int i, int j, double
     seg(v.bptr, v.lptr, j, l, ib, eb);
     int direct = -1;
     // merge of the partner-sorted lists; the direct bond i->j shows up as
-    // partner j in i's list
+    // partner j in i's list.  The common neighbours are collected kMatch at
+    // a time and their FP64 terms added after the (integer) merge, in merge
+    // order: the lanes of a warp then run the FP64 work together instead of
+    // each at its own point of the merge.
     while (ia < ea) {
-      const int pa = v.sp2[ia];
-      if (pa == j) direct = v.sbond[ia];
-      while (ib < eb && v.sp2[ib] < pa) ++ib;
-      if (ib < eb && v.sp2[ib] == pa) {
-        const int b1 = v.sbond[ia];           // i -> k
-        const int b3 = v.opp[v.sbond[ib]];    // k -> j, opposite of j -> k
+      int m1[kMatch], m3[kMatch];
+      int nm = 0;
+      while (ia < ea && nm < kMatch) {
+        const int pa = v.sp2[ia];
+        if (pa == j) direct = v.sbond[ia];
+        while (ib < eb && v.sp2[ib] < pa) ++ib;
+        if (ib < eb && v.sp2[ib] == pa) {
+          m1[nm] = v.sbond[ia];          // i -> k
+          m3[nm] = v.opp[v.sbond[ib]];   // k -> j, opposite of j -> k
+          ++nm;
+        }
+        ++ia;
+      }
+      for (int t = 0; t < nm; ++t) {
+        const int b1 = m1[t], b3 = m3[t];
         const double h = 0.5 * ((1 - v.bdamage[b3]) * v.Tv[b3] + (1 - v.bdamage[b1]) * v.Tv[b1]);
         const double n1[3] = {v.cs[3 * (int64_t)b1], v.cs[3 * (int64_t)b1 + 1], v.cs[3 * (int64_t)b1 + 2]};
         const double n3[3] = {v.cs[3 * (int64_t)b3], v.cs[3 * (int64_t)b3 + 1], v.cs[3 * (int64_t)b3 + 2]};
@@ -191,7 +205,6 @@ __device__ __forceinline__ void off_block(const AsmView& v, int i, int j, double
           for (int c = 0; c < DIM; ++c) B[r][c] -= hr * n3[c];
         }
       }
-      ++ia;
     }
     if (direct >= 0) {
       const int64_t b = direct;
