@@ -505,7 +505,7 @@ int lpm_get_K(const lpm_handle* h, double* vals) {
   LPM_CUDA(hh, cudaMemcpy(cidx.data(), h->d.cidx, sizeof(int) * nb, cudaMemcpyDeviceToHost));
   LPM_CUDA(hh, cudaMemcpy(sp.data(), h->d.sell_ptr, sizeof(int64_t) * sp.size(), cudaMemcpyDeviceToHost));
   // block (i, j) of K is block (j, i) of A transposed; (j, i) is the k-th
-  // block of row j, in slot sell_ptr[j/32] + 32 k + j%32
+  // block of row j (sell_slot)
   for (int i = 0; i < h->n; ++i)
     for (int64_t q = cptr[(size_t)i]; q < cptr[(size_t)i + 1]; ++q) {
       const int j = cidx[(size_t)q];
@@ -516,7 +516,7 @@ int lpm_get_K(const lpm_handle* h, double* vals) {
         hh->err = "pattern is not structurally symmetric";
         return LPM_ERR_STATE;
       }
-      const size_t slot = (size_t)lpm::sell_slot(lpm::sell_row_base(sp.data(), j), (int)(f - b));
+      const size_t slot = (size_t)lpm::sell_slot(lpm::sell_row(sp.data(), j), (int)(f - b));
       for (int r = 0; r < dim; ++r)
         for (int s = 0; s < dim; ++s) vals[(size_t)q * e2 + r * dim + s] = A[(size_t)(s * dim + r) * ns + slot];
     }

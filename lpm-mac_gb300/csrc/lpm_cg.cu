@@ -154,6 +154,11 @@ __device__ __forceinline__ float4 op_load(const float* a) {
   if (KEEP) return __ldg(reinterpret_cast<const float4*>(a));
   return __ldcs(reinterpret_cast<const float4*>(a));
 }
+template <bool KEEP>
+__device__ __forceinline__ float op_load1(const float* a) {
+  if (KEEP) return __ldg(a);
+  return __ldcs(a);
+}
 
 // y = row `row` of A times p (FP32), in difference form with compensated
 // accumulation: the sum comes out as if accumulated in twice the precision
@@ -161,7 +166,9 @@ __device__ __forceinline__ float4 op_load(const float* a) {
 // (exact for neighbouring values within a factor of two) and the operator's
 // own rounding.  The row is walked in groups of four blocks: one 16-byte load
 // brings a block element for four blocks.  Padding blocks are zero and point
-// at the row itself.
+// at the row itself.  The blocks past the slice's groups (at most three) are
+// read one at a time, in the same order, so the sum is that of the blocks in
+// slot order either way.
 template <int DIM, bool OFF16, bool KEEP>
 __device__ __forceinline__ void row_product32(const SellView& v, const float* __restrict__ A,
                                               const float* __restrict__ p, int row, float (&y)[DIM]) {
@@ -171,8 +178,10 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
   float pi[DIM];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) pi[k] = __ldg(&p[(int64_t)row * DIM + k]);
-  const int ng = (v.rowlen[row] + kVec - 1) / kVec;
-  const int64_t base = sell_row_base(v.sell_ptr, row);
+  const int len = v.rowlen[row];
+  const SellRow sr = sell_row(v.sell_ptr, row);
+  const int ng = (min(len, sr.g4) + kVec - 1) / kVec;
+  const int64_t base = sr.base;
   // software pipeline: the next group's values and partner values, and the
   // columns of the group after it, are in flight while the current group is
   // multiplied
@@ -219,6 +228,17 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
         for (int k = 0; k < DIM; ++k) dot2_acc(sc[r], cc[r], comp(a[r * DIM + k], t), pc[k]);
     }
   }
+  for (int k = sr.g4; k < len; ++k) {
+    const int64_t st = sr.tail + (int64_t)(k - sr.g4) * kSlice;
+    const int c = OFF16 ? row + __ldg(&v.soff[st]) : __ldg(&v.scol[st]);
+    float pc[DIM];
+#pragma unroll
+    for (int q = 0; q < DIM; ++q) pc[q] = __ldg(&p[(int64_t)c * DIM + q]) - pi[q];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r)
+#pragma unroll
+      for (int q = 0; q < DIM; ++q) dot2_acc(sc[r], cc[r], op_load1<KEEP>(A + (r * DIM + q) * v.nslots + st), pc[q]);
+  }
   const float* Si = v.S + (int64_t)row * DIM * DIM;
 #pragma unroll
   for (int r = 0; r < DIM; ++r) {
@@ -231,6 +251,7 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
 // FP64: the partner values of the four blocks are gathered first; then each
 // element's 32-byte run (four blocks) is read as two back-to-back 16-byte
 // loads, so both halves of a sector are used by the same instruction pair.
+// The blocks past the slice's groups follow one at a time.
 // With ADD32 the product is taken of p + p32 (an FP64 vector plus an FP32
 // increment not yet folded into it).
 template <int DIM, bool ADD32 = false>
@@ -239,8 +260,10 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
                                             const float* __restrict__ p32 = nullptr) {
 #pragma unroll
   for (int r = 0; r < DIM; ++r) y[r] = 0.0;
-  const int ng = (v.rowlen[row] + kVec - 1) / kVec;
-  const int64_t base = sell_row_base(v.sell_ptr, row);
+  const int len = v.rowlen[row];
+  const SellRow sr = sell_row(v.sell_ptr, row);
+  const int ng = (min(len, sr.g4) + kVec - 1) / kVec;
+  const int64_t base = sr.base;
   for (int g = 0; g < ng; ++g) {
     const int64_t s0 = base + (int64_t)g * (kSlice * kVec);
     const int4 c4 = __ldg(reinterpret_cast<const int4*>(v.scol + s0));
@@ -263,6 +286,17 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
         y[r] = fma(hi.x, pc[2][k], y[r]);
         y[r] = fma(hi.y, pc[3][k], y[r]);
       }
+  }
+  for (int k = sr.g4; k < len; ++k) {
+    const int64_t st = sr.tail + (int64_t)(k - sr.g4) * kSlice;
+    const int64_t c = (int64_t)__ldg(&v.scol[st]) * DIM;
+    double pc[DIM];
+#pragma unroll
+    for (int q = 0; q < DIM; ++q) pc[q] = ADD32 ? __ldg(&p[c + q]) + (double)__ldg(&p32[c + q]) : __ldg(&p[c + q]);
+#pragma unroll
+    for (int r = 0; r < DIM; ++r)
+#pragma unroll
+      for (int q = 0; q < DIM; ++q) y[r] = fma(__ldcs(A + (r * DIM + q) * v.nslots + st), pc[q], y[r]);
   }
 }
 

@@ -8,16 +8,21 @@
 //              order, as Particle::bond_layers holds them; SoA per field
 //   pattern    conns CSR (cptr, cidx), ascending ids, self included
 //   operator   A = K^T over the same pattern: block (j, i) of A is K_ij
-//              transposed.  Sliced block-ELL storage in groups of four: rows
-//              are grouped in slices of 32 consecutive rows, each slice is
-//              as long as its longest row rounded up to 4, and block k of
-//              row j sits in slot
-//                sell_ptr[j/32] + 128*(k/4) + 4*(j%32) + k%4,
+//              transposed.  Sliced block-ELL storage in groups of four
+//              with a one-block tail: rows are grouped in slices of 32
+//              consecutive rows, each slice holds 32 x w slots with w its
+//              longest row, g4 = w rounded down to a multiple of 4.  Block k
+//              of row j sits in slot
+//                sell_ptr[j/32] + 128*(k/4) + 4*(j%32) + k%4     (k < g4),
+//                sell_ptr[j/32] + 32*g4 + 32*(k-g4) + j%32       (k >= g4),
 //              so a thread reads four consecutive blocks of its row with one
-//              vector load and the 32 rows of a slice read 512 contiguous
-//              bytes.  Values are stored one array per block element
-//              ("element-major"): A[e * nslots + slot], e = r*dim + s.
-//              Padding slots hold zeros and point at the row itself
+//              vector load, the 32 rows of a slice read 512 contiguous bytes,
+//              and the last w - g4 blocks (at most three) are read one per
+//              row, 128 contiguous bytes per slice: no slot is padding in a
+//              slice of equal rows.  Values are stored one array per block
+//              element ("element-major"): A[e * nslots + slot], e = r*dim + s.
+//              Padding slots of a row's last group of four hold zeros and
+//              point at the row itself
 #pragma once
 
 #include <cuda_runtime.h>
@@ -64,12 +69,26 @@ constexpr int kMaxRedBlocks = 2048;
 constexpr int kSlice = 32;  // rows per slice of the sliced operator
 constexpr int kVec = 4;     // consecutive blocks of a row stored together
 
-// first slot of row j (its blocks k sit at row_base + 128*(k/4) + k%4)
-__host__ __device__ __forceinline__ int64_t sell_row_base(const int64_t* sell_ptr, int j) {
-  return sell_ptr[j / kSlice] + (int64_t)(j % kSlice) * kVec;
+// Row j of the sliced operator: blocks k < g4 in groups of four from base
+// (slot base + 128*(k/4) + k%4), the others one per slot from tail (slot
+// tail + 32*(k - g4)).
+struct SellRow {
+  int64_t base, tail;
+  int g4;
+};
+__host__ __device__ __forceinline__ SellRow sell_row(const int64_t* sell_ptr, int j) {
+  const int64_t s0 = sell_ptr[j / kSlice];
+  const int w = (int)((sell_ptr[j / kSlice + 1] - s0) / kSlice);  // the slice's longest row
+  const int g4 = w / kVec * kVec;
+  return SellRow{s0 + (int64_t)(j % kSlice) * kVec, s0 + (int64_t)g4 * kSlice + j % kSlice, g4};
 }
-__host__ __device__ __forceinline__ int64_t sell_slot(int64_t row_base, int k) {
-  return row_base + (int64_t)(k / kVec) * (kSlice * kVec) + (k % kVec);
+__host__ __device__ __forceinline__ int64_t sell_slot(const SellRow& r, int k) {
+  return k < r.g4 ? r.base + (int64_t)(k / kVec) * (kSlice * kVec) + (k % kVec) : r.tail + (int64_t)(k - r.g4) * kSlice;
+}
+// Slots of row j the products read: its blocks, and in the group region the
+// padding of its last group of four.
+__host__ __device__ __forceinline__ int sell_read_len(const SellRow& r, int len) {
+  return len <= r.g4 ? (len + kVec - 1) / kVec * kVec : len;
 }
 
 struct Group {

@@ -90,15 +90,15 @@ __global__ void k_fill_sell(int n, const int64_t* __restrict__ cptr, const int* 
   if (j >= n) return;
   const int64_t q0 = cptr[j];
   const int len = (int)(cptr[j + 1] - q0);
-  const int64_t base = sell_row_base(sell_ptr, j);
+  const SellRow row = sell_row(sell_ptr, j);
   int ds = -1;
   for (int k = 0; k < len; ++k) {
     const int c = cidx[q0 + k];
-    scol[sell_slot(base, k)] = c;
-    if (c == j) ds = (int)sell_slot(base, k);
+    scol[sell_slot(row, k)] = c;
+    if (c == j) ds = (int)sell_slot(row, k);
   }
   // padding of the row's last group of four points at the row itself
-  for (int k = len; k % kVec != 0; ++k) scol[sell_slot(base, k)] = j;
+  for (int k = len; k < sell_read_len(row, len); ++k) scol[sell_slot(row, k)] = j;
   rowlen[j] = len;
   diag_slot[j] = ds;
 }
@@ -239,9 +239,9 @@ __global__ void __launch_bounds__(256) k_assemble(AsmView v) {
   for (long long sl = w0; sl < v.nslice; sl += nw) {
     const int j = (int)(sl * kSlice) + lane;
     const int len = j < v.n ? v.rowlen[j] : 0;
-    const int64_t base = j < v.n ? sell_row_base(v.sell_ptr, j) : 0;
+    const SellRow row = j < v.n ? sell_row(v.sell_ptr, j) : SellRow{0, 0, 0};
     for (int k = 0; k < len; ++k) {
-      const int64_t slot = sell_slot(base, k);
+      const int64_t slot = sell_slot(row, k);
       const int i = v.scol[slot];
       double K[3][3];
       if (i == j)
@@ -298,9 +298,9 @@ __global__ void __launch_bounds__(256) k_apply_bc(int n, int nslice, const int64
 #pragma unroll
     for (int r = 0; r < DIM; ++r) fj[r] = fixed[DIM * j + r];
     const int len = rowlen[j];
-    const int64_t base = sell_row_base(sell_ptr, j);
+    const SellRow row = sell_row(sell_ptr, j);
     for (int k = 0; k < len; ++k) {
-      const int64_t slot = sell_slot(base, k);
+      const int64_t slot = sell_slot(row, k);
       const int i = scol[slot];
 #pragma unroll
       for (int r = 0; r < DIM; ++r)
@@ -317,17 +317,17 @@ __global__ void k_to_fp32(int64_t m, const double* __restrict__ a, float* __rest
 }
 
 // 16-bit column offsets (column - row) of the slots the product reads for
-// row j: its blocks and the padding of its last group of four.  The flag is
-// set when one does not fit; the slots past them are never read.
+// row j (sell_read_len).  The flag is set when one does not fit; the other
+// slots are never read.
 __global__ void k_col_offsets(int n, const int64_t* __restrict__ sell_ptr, const int* __restrict__ scol,
                               const int* __restrict__ rowlen, short* __restrict__ soff, int* flag) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  const int len = (rowlen[j] + kVec - 1) / kVec * kVec;
-  const int64_t base = sell_row_base(sell_ptr, j);
+  const SellRow row = sell_row(sell_ptr, j);
+  const int len = sell_read_len(row, rowlen[j]);
   bool bad = false;
   for (int k = 0; k < len; ++k) {
-    const int64_t s = sell_slot(base, k);
+    const int64_t s = sell_slot(row, k);
     const int o = scol[s] - j;
     bad |= (o < -32768 || o > 32767);
     soff[s] = (short)o;
@@ -341,12 +341,12 @@ __global__ void k_block_rowsum(int n, const int64_t* __restrict__ sell_ptr, cons
                                const double* __restrict__ A, int64_t nslots, float* __restrict__ S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int64_t base = sell_row_base(sell_ptr, i);
+  const SellRow row = sell_row(sell_ptr, i);
   double acc[DIM * DIM];
 #pragma unroll
   for (int e = 0; e < DIM * DIM; ++e) acc[e] = 0.0;
   for (int k = 0; k < rowlen[i]; ++k) {
-    const int64_t s = sell_slot(base, k);
+    const int64_t s = sell_slot(row, k);
 #pragma unroll
     for (int e = 0; e < DIM * DIM; ++e) acc[e] += A[e * nslots + s];
   }
@@ -383,13 +383,13 @@ int build_pattern(lpm_handle* h) {
     h->err = "pattern has 2^31 or more blocks";
     return LPM_ERR_ARG;
   }
-  // sliced layout: each slice is as long as its longest row
+  // sliced layout: each slice is as long as its longest row (groups of four,
+  // then a tail of at most three single blocks)
   h->nslice = (n + kSlice - 1) / kSlice;
   std::vector<int64_t> sp((size_t)h->nslice + 1, 0);
   for (int sl = 0; sl < h->nslice; ++sl) {
     int64_t mx = 0;
     for (int j = sl * kSlice; j < std::min(n, (sl + 1) * kSlice); ++j) mx = std::max(mx, hc[(size_t)j]);
-    mx = (mx + kVec - 1) / kVec * kVec;  // whole groups of four
     sp[(size_t)sl + 1] = sp[(size_t)sl] + mx * kSlice;
   }
   h->nslots = sp[(size_t)h->nslice];
