@@ -304,8 +304,10 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
 // registers), which measured level with the product before the partner
 // values were prefetched; the 2-D one takes 80 registers (three blocks per SM)
 // and measured 2 % faster on the CT plate's load step than at 64 registers.
+// The FP64 product, bound by the FP64 pipe, is held to four blocks per SM (64
+// registers): at 70 registers and three blocks it measured 2 % slower.
 template <typename T, int DIM>
-constexpr int kSpmvMinBlocks = (sizeof(T) == 4 && DIM == 3) ? 2 : 0;
+constexpr int kSpmvMinBlocks = sizeof(T) == 8 ? 4 : DIM == 3 ? 2 : 0;
 
 template <typename T, int DIM, bool OFF16 = false, bool KEEP = false>
 __global__ void __launch_bounds__(256, (kSpmvMinBlocks<T, DIM>)) k_cg_spmv(SellView v, const T* __restrict__ A,
