@@ -298,6 +298,55 @@ def test_isolated_particle():
     g.close()
 
 
+def test_short_rows_stored_past_the_groups():
+    """Slices whose rows all hold fewer than four blocks keep every block in
+    the one-per-slot tail of the sliced operator, and a slice can mix such
+    rows with full plate rows: a 9x9 plate plus 40 two-particle chains, each
+    chain held at one end and pulled by a force at the other.  FP64 load
+    steps match the oracle within 1e-9, mixed ones the FP64 ones within
+    1e-8."""
+    dim, xyz, _, _, _, _, _, cell = plate(9, 9)
+    n0, a = len(xyz), 0.5
+    x0 = xyz[:, 0].max() + 4 * a
+    ym = 0.5 * (xyz[:, 1].min() + xyz[:, 1].max())
+    pairs = np.array([[x0 + 4 * a * k + a * e, ym, 0.0] for k in range(40) for e in (0, 1)])
+    xyz = np.vstack([xyz, pairs])
+    p1, p2, layer = lat.find_bonds(xyz, cell)
+    Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(69e3, 0.3, plane_stress=True, layout="row"))
+    left, right = n0 + 2 * np.arange(40), n0 + 2 * np.arange(40) + 1
+    du = 1e-3
+    groups, apply, dd = tension_bcs(xyz[:n0], dim, du)
+    apply = np.vstack([apply, np.zeros((80, 3), np.int32)])
+    dd = np.vstack([dd, np.zeros((80, 3))])
+    apply[left, 0] = apply[left, 1] = apply[right, 1] = 1
+    F = 1e-3 * a * Kn[(p1 == left[0]) & (p2 == right[0])][0]
+    f = np.zeros((len(xyz), 3))
+    f[right, 0] = F
+    outs = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        g = make_gpu(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+        cptr, _ = g.pattern()
+        rowlen = np.diff(cptr)
+        assert rowlen[96:160].max() < 4 and rowlen[64:96].max() >= 4
+        gl, gr = g.add_group(left), g.add_group(right)
+        bcs = gpu_bcs(g, groups, dim, du) + [("disp", gl, 0, 0.0), ("disp", gl, 1, 0.0), ("disp", gr, 1, 0.0),
+                                             ("force", gr, 40 * F, 0.0, 0.0)]  # a total, split over the group
+        g.update()
+        for _ in range(2):
+            res = g.load_step(bcs, tangent=capi.TANGENT_SYMMETRIC, precision=prec, cg_tol=1e-10)
+            assert res["status"] == 0
+        outs[prec] = g.download(capi.F_XYZ) - xyz
+        g.close()
+    o = make_oracle(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    o.update()
+    for _ in range(2):
+        o.load_step(apply, dd, f, sym=1, bc_elim=1, cg_tol=1e-10)
+    uo = o.get(oracle.XYZ) - xyz
+    assert np.abs(uo[right, 0]).min() > 0
+    assert rel(outs[capi.PREC_FP64], uo) <= 1e-9
+    assert rel(outs[capi.PREC_MIXED], outs[capi.PREC_FP64]) <= 1e-8
+
+
 def test_mixed_solve_with_wide_pattern_uses_32bit_columns():
     """A particle numbering whose column offsets do not fit 16 bits (a
     randomly permuted 33^3 cube, 35,937 particles) runs the FP32 product on
