@@ -26,6 +26,9 @@ Reported (one JSON line on rank 0):
   setup        the GPU bond search (checked identical to the CPU
                generator's bonds) and the creation of the device lattice
   fatigue      compact-tension fatigue cycles at full size (configuration 5)
+  softening    (--softening) load steps of the notched plate with the
+               softening bond law and damage rounds at full size
+               (configuration 3); minutes, so not in the default run
   j2_sensitivity  cost of carrying d/d(yield stress) and d/d(hardening)
                through J2 load steps of a BCC polycrystal
 
@@ -62,6 +65,8 @@ def parse_args(argv=None):
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--cpu-sample-iters", type=int, default=20)
+    p.add_argument("--softening", action="store_true",
+                   help="also time configuration 3 at full size (several minutes: its crack bursts in the timed steps)")
     return p.parse_args(argv)
 
 
@@ -375,6 +380,60 @@ def fatigue_cost(capi, local, cycles=3):
             "cycle": "1 increment up, 1 down, cycle jump 1000 (lpm_fatigue_cycle)", "precision": "mixed"}
 
 
+def softening_cost(capi, local, steps=4, max_warm=15):
+    """Configuration 3 at full size: the single-edge-notched hexagonal plate
+    (401 rows of 201/200 particles, 0.1 mm spacing, crack over 0.3 W),
+    softening bond law (alpha 3) with Weibull(k = 10, lambda = 1.2e-3)
+    critical stretches, one draw per undirected bond, seed 20261203.  Top
+    edge pulled by 1e-4 of the height per step (static solver with damage
+    rounds on the eliminated tangent, mixed precision); untimed steps until
+    some bond has softened, then `steps` timed steps.  Device time with CUDA
+    events on the library's stream."""
+    import torch
+    import __graft_entry__ as ge
+    lat = ge.load_package().lattice
+    xyz, p1, p2, layer, cell = lat.sent_plate(201, 401, 0.1)
+    Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(69e3, 0.3, plane_stress=True, layout="row"))
+    scrit = lat.weibull_draws(p1, p2, 10.0, 1.2e-3, 20261203)[np.lexsort((layer, p1))]
+    g = capi.Lattice(2, xyz, p1, p2, layer, Kn, Tv, cell.particle_volume, cell.nneighbors)
+    g.set_law(capi.LAW_SOFTENING, [3.0, 1.0e-3])
+    g.upload(capi.B_SCRIT, scrit)
+    g.update()
+    c = xyz[:, 1]
+    bottom, top = np.where(c < c.min() + 1e-9)[0], np.where(c > c.max() - 1e-9)[0]
+    du = 1e-4 * (c.max() - c.min())
+    gb, gc, gt = g.add_group(bottom), g.add_group(bottom[:1]), g.add_group(top)
+    bcs = [("disp", gb, 1, 0.0), ("disp", gc, 0, 0.0), ("disp", gt, 1, du)]
+    opts = dict(solver=capi.SOLVER_STATIC_ELIMINATE, tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_MIXED,
+                max_iter=60, tol=1e-5, cg_tol=1e-10)
+    warm = 0
+    while warm < max_warm and not (g.download(capi.B_BDAMAGE) > 0).any():
+        if g.load_step(bcs, **opts)["status"] != 0:
+            raise RuntimeError("SENT step did not converge")
+        warm += 1
+    stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    g.synchronize()
+    e0.record(stream)
+    recs = [g.load_step(bcs, **opts) for _ in range(steps)]
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    d = g.download(capi.B_BDAMAGE)
+    g.close()
+    if any(r["status"] != 0 for r in recs):
+        raise RuntimeError("SENT step did not converge")
+    return {"workload": "SENT hex plate 401 rows x 201/200, 0.1 mm spacing (%d particles, %d bonds), crack 0.3 W, "
+                        "softening law, Weibull critical stretch" % (len(xyz), len(p1)),
+            "steps_per_s": steps / (ms * 1e-3), "ms_per_step": ms / steps, "steps": steps, "untimed_steps": warm,
+            "newton_iters_per_step": statistics.mean(r["newton_iters"] for r in recs),
+            "damage_rounds_per_step": statistics.mean(r["damage_rounds"] for r in recs),
+            "cg_iters_per_step": statistics.mean(r["cg_iters"] for r in recs),
+            "softened_bonds": int((d > 0).sum()), "broken_bonds": int((d >= 1).sum()),
+            "precision": "mixed", "solver": "static with damage rounds, eliminated tangent"}
+
+
 def j2_sensitivity_cost(capi, local, ncell=40, steps=4):
     """The tangent-linear sensitivity of a J2 load history (configuration 4
     form: BCC polycrystal, 20 grains, E = 110 GPa, nu = 0.34, yield 900 MPa,
@@ -642,6 +701,8 @@ def run_gb300(args):
                            "force_algorithmic_bytes": fb}
     line["setup"] = setup_cost(w, capi)
     line["fatigue"] = fatigue_cost(capi, local)
+    if args.softening:
+        line["softening"] = softening_cost(capi, local)
     line["j2_sensitivity"] = j2_sensitivity_cost(capi, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
