@@ -30,14 +30,15 @@
 // Without both, the FP32 iterate carries errors along the smooth directions
 // that its residual barely shows, and the next Newton solve pays for them
 // (about 50% more iterations at 101^3).  With both, the first solve of a
-// load step takes the FP64 iteration count and later ones 10-30% more, from
-// the FP32 rounding of the operator's values.  The recurrence runs with
-// reliable updates (residual replacement): when the iterated residual has
-// fallen by kDelta since the
-// last update, the FP32 solution increment is folded into the FP64 solution,
-// the residual is recomputed in FP64 as b - A64 x and replaces the iterated
-// one, and the iteration continues with its search direction.  The solve
-// stops on the FP64 residual.  Every update is one FP64 sparse product.
+// load step takes the FP64 iteration count and later ones 10-30% more.  (An
+// operator kept as two FP32 words per value did not remove that excess on a
+// 2-D compact-tension plate, so it is not the operator's rounding alone.)
+// The recurrence runs with reliable updates (residual replacement): when the
+// iterated residual has fallen by kDelta since the last update, the FP32
+// solution increment is folded into the FP64 solution, the residual is
+// recomputed in FP64 as b - A64 x and replaces the iterated one, and the
+// iteration continues with its search direction.  The solve stops on the
+// FP64 residual.  Every update is one FP64 sparse product.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
