@@ -52,3 +52,31 @@ def test_bad_arguments_are_rejected_before_any_device_work():
     assert st == pkg.capi.ERR_ARG
     # NULL handle calls
     assert L.lpm_update_geometry_force(None) == pkg.capi.ERR_ARG
+
+
+def handle_entry_points():
+    """Entry points of the header whose first parameter is the handle."""
+    text = open(os.path.join(ROOT, "include", "lpm_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(lpm_[A-Za-z0-9_]+)\s*\(\s*(?:const\s+)?lpm_handle\s*\*", text)))
+
+
+def test_every_handle_entry_point_rejects_a_null_handle():
+    """Each entry point tests its handle before anything else, so a NULL
+    handle returns LPM_ERR_ARG (lpm_destroy: a no-op; lpm_last_error: the
+    library-wide message) and no other argument is read.  A CDLL of its own
+    gives function objects without the binding's argument types."""
+    pkg.capi.load()
+    L = ctypes.CDLL(pkg.build.build())
+    names = handle_entry_points()
+    assert len(names) >= 40
+    for name in names:
+        fn = getattr(L, name)
+        if name == "lpm_last_error":
+            fn.restype = ctypes.c_char_p
+            assert isinstance(fn(None), bytes)
+        elif name == "lpm_destroy":
+            assert fn(None) == pkg.capi.OK
+        else:
+            fn.restype = ctypes.c_int
+            assert fn(None) == pkg.capi.ERR_ARG, name
