@@ -32,7 +32,9 @@
 // (about 50% more iterations at 101^3).  With both, the first solve of a
 // load step takes the FP64 iteration count and later ones 10-30% more.  (An
 // operator kept as two FP32 words per value did not remove that excess on a
-// 2-D compact-tension plate, so it is not the operator's rounding alone.)
+// 2-D compact-tension plate; an emulation of this recurrence places it in the
+// FP32 residual, product output and solution increment, and in alpha and
+// beta rounded to FP32.)
 // The recurrence runs with reliable updates (residual replacement): when the
 // iterated residual has fallen by kDelta since the last update, the FP32
 // solution increment is folded into the FP64 solution, the residual is
