@@ -19,7 +19,10 @@ Reported (one JSON line on rank 0):
                per launch / average launch time, against the measured HBM
                copy bandwidth
   cpu_baseline the CPU oracle (a restatement of the reference algorithm) on
-               the host cores, bounded sample extrapolated to a full step
+               the host cores: one complete FP64 load step, timed whole
+  parity       that CPU step against the GPU's first FP64 step and the
+               GPU's first mixed step against its FP64 one (displacement and
+               reaction errors)
   adjoint      one backward step (gradient of a reaction with respect to
                every bond's constants), in ms and relative to a forward step
   bonds_per_s  the force pass alone and with the tangent assembly
@@ -32,7 +35,7 @@ Reported (one JSON line on rank 0):
   j2_sensitivity  cost of carrying d/d(yield stress) and d/d(hardening)
                through J2 load steps of a BCC polycrystal
 
---impl reference times the CPU oracle alone on the same workload.
+--impl reference times complete CPU oracle load steps of the same workload.
 Multi-GPU runs are independent replicas (the path has no exchange step).
 """
 import argparse
@@ -64,7 +67,6 @@ def parse_args(argv=None):
     p.add_argument("--cg-tol", type=float, default=1e-10)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
-    p.add_argument("--cpu-sample-iters", type=int, default=20)
     p.add_argument("--softening", action="store_true",
                    help="also time configuration 3 at full size (several minutes: its crack bursts in the timed steps)")
     return p.parse_args(argv)
@@ -527,16 +529,15 @@ def measured_peaks():
 
 def profiled_traffic(kernel_key, nblk):
     """DRAM bytes per launch of the CG sparse product: the bytes per block
-    measured by ncu on the 61^3 lattice (committed summary) times this
-    workload's block count (traffic grows with the blocks processed)."""
-    path = os.path.join(ROOT, "profiles", "cg_spmv_sc61.md")
+    ncu measured on the 61^3 lattice (profiles/cg_spmv_sc61_traffic.json)
+    times this workload's block count (traffic grows with the blocks
+    processed)."""
+    path = os.path.join(ROOT, "profiles", "cg_spmv_sc61_traffic.json")
     try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_block") and line.split()[1] == kernel_key:
-                return float(line.split("=")[1].split()[0]) * nblk
-    except OSError:
-        pass
-    return None
+        with open(path) as f:
+            return float(json.load(f)["kernels"][kernel_key]["bytes_per_block"]) * nblk
+    except (OSError, KeyError, ValueError):
+        return None
 
 
 # --------------------------------------------------------------- CPU arm
@@ -549,38 +550,42 @@ def cpu_oracle_system(w, threads):
     return oracle, o
 
 
-def cpu_sample(oracle, o, w, du, cg_iters):
-    """One bounded sample of a load step on the CPU oracle: BC move, force
-    pass, tangent assembly and `cg_iters` FP64 CG iterations."""
+def oracle_bcs(w, du):
+    """Boundary arrays of one load step for the oracle: bottom face clamped,
+    top face moved by du along z."""
     n = len(w["xyz"])
     apply = np.zeros((n, 3), np.int32)
-    d = np.zeros((n, 3))
     apply[w["bottom"], :] = 1
     apply[w["top"], 2] = 1
-    d[w["top"], 2] = du
-    x = o.get(oracle.XYZ)
-    x[w["top"], 2] += du
-    o.set(oracle.XYZ, x)
-    m = np.zeros((n, 3), np.int32)
-    m[apply == 1] = 1
-    o.set_mask(m)
+    dd = np.zeros((n, 3))
+    dd[w["top"], 2] = du
+    return apply, dd
+
+
+def oracle_step(o, w, args):
+    """One complete FP64 load step on the CPU oracle (symmetric tangent, BC
+    elimination, Jacobi CG to cg_tol, Newton to 1e-5): wall time, Newton
+    and CG iteration counts."""
+    apply, dd = oracle_bcs(w, args.du)
+    o.clear_log()
     t0 = time.perf_counter()
-    o.update()
-    t1 = time.perf_counter()
-    o.assemble(sym=1, bc=1)
-    t2 = time.perf_counter()
-    r, _, _ = o.residual()
-    t3 = time.perf_counter()
-    o.cg(r, 1e-30, maxit=cg_iters)
-    t4 = time.perf_counter()
-    return dict(force=t1 - t0, assemble=t2 - t1, cg_iter=(t4 - t3) / cg_iters)
+    st = o.load_step(apply, dd, sym=1, bc_elim=1, cg_tol=args.cg_tol)
+    t = time.perf_counter() - t0
+    if st < 0:
+        raise RuntimeError("CPU oracle load step did not converge")
+    log = o.log()
+    return t, len(log), int(log[:, 0].sum())
 
 
-def cpu_step_time(s, newton, cg_iters):
-    return s["assemble"] + (newton + 1) * s["force"] + cg_iters * s["cg_iter"]
+REFERENCE_BUDGET_S = 100.0  # complete CPU load steps are timed until this much time is spent
 
 
 def run_reference(args):
+    """The reference algorithm on the host cores: complete FP64 load steps of
+    the same workload on the CPU oracle with every host thread, timed one by
+    one until REFERENCE_BUDGET_S is spent (at least one).  The value is the
+    number of complete steps over their total time; nothing is
+    extrapolated."""
     world, rank, local = dist_env()
     if rank != 0:
         return 0
@@ -588,37 +593,84 @@ def run_reference(args):
     w = workload(args.n)
     oracle, o = cpu_oracle_system(w, threads)
     o.update()
-    # iteration counts of a full step: one complete FP64 load step on the CPU
-    n = len(w["xyz"])
-    apply = np.zeros((n, 3), np.int32)
-    apply[w["bottom"], :] = 1
-    apply[w["top"], 2] = 1
-    dd = np.zeros((n, 3))
-    dd[w["top"], 2] = args.du
-    o.clear_log()
-    t0 = time.perf_counter()
-    o.load_step(apply, dd, sym=1, bc_elim=1, cg_tol=args.cg_tol)
-    full = time.perf_counter() - t0
-    log = o.log()
-    newton, cg_iters = len(log), int(log[:, 0].sum())
-    times = []
-    for k in range(args.warmup + args.steps):
-        s = cpu_sample(oracle, o, w, args.du, args.cpu_sample_iters)
-        if k >= args.warmup:
-            times.append(cpu_step_time(s, newton, cg_iters))
-    value = 1.0 / statistics.mean(times)
-    sample = ("each step: 1 force pass + 1 tangent assembly + %d FP64 CG iterations on the full lattice, "
-              "extrapolated with the %d Newton / %d CG iterations of one complete CPU load step (%.1f s)" %
-              (args.cpu_sample_iters, newton, cg_iters, full))
+    times, newton, cg = [], [], []
+    while len(times) < max(1, args.steps):
+        t, ni, ci = oracle_step(o, w, args)
+        times.append(t)
+        newton.append(ni)
+        cg.append(ci)
+        if sum(times) >= REFERENCE_BUDGET_S:
+            break
+    total = sum(times)
+    value = len(times) / total
+    sample = ("%d complete FP64 load step(s) from the undeformed lattice, timed whole (%s s; %s Newton / %s CG "
+              "iterations); steps are timed until %.0f s is spent" %
+              (len(times), ", ".join("%.1f" % t for t in times), ", ".join(map(str, newton)),
+               ", ".join(map(str, cg)), REFERENCE_BUDGET_S))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+            "steps": len(times), "warmup": 0, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": describe(w), "solver": "CPU oracle (reference algorithm restated), FP64 Jacobi CG",
-                       "cg_tol": args.cg_tol, "newton_tol": 1e-5, "threads": threads},
+            "config": {"workload": describe(w), "precision": "FP64 Jacobi CG (the reference's form)",
+                       "tangent": "symmetric K_ii[1][0]", "bc": "eliminated (updateStiffnessDispBC)",
+                       "cg_tol": args.cg_tol, "newton_tol": 1e-5, "threads": threads,
+                       "solver": "CPU oracle (the reference algorithm restated, pinned bit for bit to it)",
+                       "steps_requested": args.steps, "warmup_requested": args.warmup},
+            "newton_iters_per_step": statistics.mean(newton), "cg_iters_per_step": statistics.mean(cg),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b|."""
+    s = float(np.abs(b).max())
+    return float(np.abs(a - b).max() / (s if s > 0 else 1.0))
+
+
+def headline_parity(w, args, capi):
+    """The first load step of the workload, from the undeformed lattice, three
+    ways: the CPU oracle in FP64 (all host threads; timed whole, the CPU
+    baseline), the GPU in FP64 and the GPU in mixed precision.  Errors are
+    max |u - u_ref| / max |u_ref| over the displacements, and relative errors
+    of the top face's z reaction."""
+    threads = os.cpu_count() or 1
+    oracle, o = cpu_oracle_system(w, threads)
+    o.update()
+    t_cpu, ni_cpu, cg_cpu = oracle_step(o, w, args)
+    xyz, top = w["xyz"], w["top"]
+    u_ref = o.get(oracle.XYZ) - xyz
+    R_ref = float(o.get(oracle.PIN)[top, 2].sum())
+    _, nr_o, nR_o = o.residual()
+    del o
+    gpu = {}
+    for name, prec in (("fp64", capi.PREC_FP64), ("mixed", capi.PREC_MIXED)):
+        g = capi.Lattice(3, xyz, w["p1"], w["p2"], w["layer"], w["Kn"], w["Tv"], w["cell"].particle_volume,
+                         w["cell"].nneighbors)
+        gb, gt = g.add_group(w["bottom"]), g.add_group(top)
+        bcs = [("disp", gb, 0, 0.0), ("disp", gb, 1, 0.0), ("disp", gb, 2, 0.0), ("disp", gt, 2, args.du)]
+        g.update()
+        r = g.load_step(bcs, tangent=capi.TANGENT_SYMMETRIC, precision=prec, max_iter=30, tol=1e-5,
+                        cg_tol=args.cg_tol)
+        if r["status"] != 0:
+            raise RuntimeError("first-step parity: GPU step did not converge: %s" % r)
+        nr, nR = g.residual()
+        gpu[name] = dict(u=g.download(capi.F_XYZ) - xyz, R=float(g.download(capi.F_PIN)[top, 2].sum()),
+                         newton=r["newton_iters"], cg=r["cg_iters"], ratio=nr / nR)
+        g.close()
+    f, m = gpu["fp64"], gpu["mixed"]
+    parity = {"step": "first load step from the undeformed lattice, same inputs on CPU and GPU",
+              "norm": "max|u - u_ref| / max|u_ref| (displacements); |R - R_ref| / |R_ref| (top-face z reaction)",
+              "fp64_vs_oracle": rel_err(f["u"], u_ref), "fp64_reaction_vs_oracle": abs(f["R"] - R_ref) / abs(R_ref),
+              "mixed_vs_fp64": rel_err(m["u"], f["u"]), "mixed_reaction_vs_fp64": abs(m["R"] - f["R"]) / abs(f["R"]),
+              "mixed_vs_oracle": rel_err(m["u"], u_ref),
+              "newton_residual_over_reaction": {"oracle": nr_o / nR_o, "fp64": f["ratio"], "mixed": m["ratio"]},
+              "newton_iters": {"oracle": ni_cpu, "fp64": f["newton"], "mixed": m["newton"]},
+              "cg_iters": {"oracle": cg_cpu, "fp64": f["cg"], "mixed": m["cg"]}, "cg_tol": args.cg_tol}
+    cpu = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": "one complete FP64 load step (the first, from the undeformed lattice) of the same workload on "
+                     "the CPU oracle, timed whole: %.1f s, %d Newton / %d CG iterations" % (t_cpu, ni_cpu, cg_cpu)}
+    return parity, cpu
 
 
 def run_gb300(args):
@@ -704,22 +756,9 @@ def run_gb300(args):
     if args.softening:
         line["softening"] = softening_cost(capi, local)
     line["j2_sensitivity"] = j2_sensitivity_cost(capi, local)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        oracle, o = cpu_oracle_system(w, threads)
-        o.update()
-        newton = line["newton_iters_per_step"]
-        cgi = line.get("fp64", line)["cg_iters_per_step"]
-        s = cpu_sample(oracle, o, w, args.du, args.cpu_sample_iters)
-        t = cpu_step_time(s, newton, cgi)
-        line["cpu_baseline"] = {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "1 force pass + 1 tangent assembly + %d FP64 CG iterations on the full "
-                                          "lattice (%.2f s force, %.2f s assembly, %.3f s/CG iteration), "
-                                          "extrapolated with %.1f Newton / %.0f CG iterations per step" %
-                                          (args.cpu_sample_iters, s["force"], s["assemble"], s["cg_iter"], newton,
-                                           cgi)}
-        del o
     g.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["parity"], line["cpu_baseline"] = headline_parity(w, args, capi)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

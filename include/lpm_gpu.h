@@ -400,21 +400,23 @@ int lpm_find_neighbors(int n, const double* xyz, const double* radius, int64_t c
 /* Allocation-free Jacobi-CG solve.  No counterpart in the reference: it is
  * for callers that cannot allocate device memory while they solve (a
  * real-time loop that reserved its memory up front, a host framework whose
- * allocator owns the device).  The
- * caller passes device buffers: the operator in block CSR (ptr[n+1] int64,
- * col[nnz] int32, vals[nnz*dim*dim] row-major blocks, applied as y = A x),
- * the right-hand side b and the solution x (n*dim doubles each).  The
- * iteration is lpm_solve's FP64 one (Jacobi preconditioner from the
- * diagonal blocks, zero start, |r|^2 < tol^2 |b|^2, maxit < 0: 2*n*dim).
+ * allocator owns the device).  The caller passes device buffers: the
+ * operator in block CSR (ptr[n+1] int64, col[nnz] int32, vals[nnz*dim*dim]
+ * row-major blocks, applied as y = A x), the right-hand side b and the
+ * solution x (n*dim doubles each).  The iteration is lpm_solve's FP64 one
+ * (Jacobi preconditioner from the diagonal blocks, zero start,
+ * |r|^2 < tol^2 |b|^2, maxit < 0: 2*n*dim); its product reads the block CSR
+ * row by row, so an iteration is slower than one of lpm_solve.
  * Work vectors live in one fixed device array inside the library, sized for
- * n*dim <= LPM_NOALLOC_MAX_DOF (about 33.6 MB, held on each device from the
- * first call until the process exits); larger systems are refused with
- * LPM_ERR_ARG.  The first call on a device looks up that array's address:
- * make it before any stream capture.  All calls share the array, so calls
- * that overlap on the same GPU race.  Runs on `stream` (NULL: the default
- * stream) and returns when the solve is done (it synchronises with `stream`
- * to read the counts back, so the call itself cannot be recorded by stream
- * capture); iters/relres may be NULL. */
+ * n*dim <= LPM_NOALLOC_MAX_DOF (about 33.6 MB, created on each GPU when the
+ * library's device code is loaded there, held until the process exits);
+ * larger systems are refused with LPM_ERR_ARG.  The first call on a device
+ * looks up that array's address and caches it: make it before any stream
+ * capture, and do not use the library across a device reset, which
+ * invalidates the cached address.  All calls share the array, so calls that
+ * overlap on the same GPU race.  Runs on `stream` (NULL: the default stream)
+ * and returns when the solve is done (it synchronises with `stream` to read
+ * the counts back); iters/relres may be NULL. */
 #define LPM_NOALLOC_MAX_DOF 1048576
 int lpm_cg_solve_noalloc(int dim, int n, const int64_t* ptr, const int* col, const double* vals, const double* b,
                          double* x, double tol, int64_t maxit, void* stream, int64_t* iters, double* relres);

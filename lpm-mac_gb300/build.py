@@ -16,7 +16,9 @@ LIB = os.path.join(OUT, "liblpmgpu.so")
 SOURCES = ["lpm_capi.cu", "lpm_force.cu", "lpm_tangent.cu", "lpm_cg.cu", "lpm_laws.cu", "lpm_noalloc.cu", "lpm_adjoint.cu", "lpm_search.cu"]
 HEADERS = ["lpm_internal.cuh", "lpm_device.cuh", "lpm_cgvec.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+# host code: no fused multiply-add contraction, so host-side lengths (the
+# initial bond lengths) round like the reference's
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 
 def _nvcc():

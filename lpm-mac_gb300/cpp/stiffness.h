@@ -20,8 +20,14 @@ class Stiffness {
 
   Stiffness(std::vector<Particle<nlayer>*>& pt_sys, StiffnessMode p_mode)
       : mode(p_mode), residual((Eigen::Index)(pt_sys.size() * pt_sys[0]->cell.dim)) {
-    if (mode == StiffnessMode::FiniteDifference)
-      fprintf(stderr, "liblpmgpu: the finite-difference tangent is not on the GPU path; using the analytical one\n");
+    // The forward-difference tangent (localStiffnessFD, stiffness.h:103-154)
+    // is not built on the device.  Asking for it ends the program with an
+    // argument error rather than silently assembling a different matrix.
+    if (mode == StiffnessMode::FiniteDifference) {
+      fprintf(stderr, "liblpmgpu: StiffnessMode::FiniteDifference is not supported on the GPU path "
+                      "(use StiffnessMode::Analytical)\n");
+      exit(1);
+    }
   }
   void attach(Assembly<nlayer>* a) { ass_ = a; }
   void reset(std::vector<Particle<nlayer>*>&) {}

@@ -113,4 +113,12 @@ __device__ __forceinline__ bool grid_fold(const double (&v)[K], double* partials
 
 __device__ __forceinline__ bool is_broken(double bdamage) { return fabs(bdamage - 1.0) < EPS; }
 
+// Particle::distanceTo (particle.h:277-280): sqrt(dx^2 + dy^2 + dz^2) with each
+// square rounded and the sum taken left to right, no fused multiply-add, so
+// the length is the reference's bit for bit (sqrt and the products are
+// correctly rounded on both sides).
+__device__ __forceinline__ double bond_length(double dx, double dy, double dz) {
+  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+}
+
 }  // namespace lpm

@@ -30,15 +30,19 @@ __global__ void k_geometry_force(int n, const double* __restrict__ x, const int6
   for (int64_t b = b0; b < b1; ++b) {
     const int j = bp2[b];
     const double dx = xi0 - x[3 * j], dy = xi1 - x[3 * j + 1], dz = xi2 - x[3 * j + 2];
-    const double d = sqrt(dx * dx + dy * dy + dz * dz);
+    const double d = bond_length(dx, dy, dz);
     const bool br = is_broken(bdamage[b]);
     const double d0 = dis0[b];
     const double dl = br ? 0.0 : (d - d0);
     const double e = br ? 0.0 : (d - d0 - dLp[b]);
-    const double rd = 1.0 / d;  // one division per bond; the four quotients below are products
+    // the direction cosines use one reciprocal per bond (products, within
+    // an ulp of dx/dis); the strain is the quotient dL/dis itself, so that
+    // the brittle test bstrain >= critical (particle_elastic.h:60) sees the
+    // reference's value bit for bit
+    const double rd = 1.0 / d;
     const double c0 = br ? 0.0 : dx * rd, c1 = br ? 0.0 : dy * rd, c2 = br ? 0.0 : dz * rd;
     dis[b] = d;
-    bstrain[b] = br ? 0.0 : dl * rd;
+    bstrain[b] = br ? 0.0 : dl / d;
     dLe[b] = e;
     cs[3 * b] = c0;
     cs[3 * b + 1] = c1;

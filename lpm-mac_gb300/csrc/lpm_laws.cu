@@ -117,7 +117,7 @@ __global__ void k_nonlocal_rate(LawView v) {
     const int j = v.nl_idx[q];
     if (v.ptype[j] == v.undamaged) continue;
     const double dx = x0 - v.x[3 * j], dy = x1 - v.x[3 * j + 1], dz = x2 - v.x[3 * j + 2];
-    const double w = phi(sqrt(dx * dx + dy * dy + dz * dz), L) * (v.pvol * v.nbonds[j] / v.nneighbors);
+    const double w = phi(bond_length(dx, dy, dz), L) * (v.pvol * v.nbonds[j] / v.nneighbors);
     D += v.ddot_local[j] * w;
     A += w;
   }

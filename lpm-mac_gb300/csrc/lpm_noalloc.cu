@@ -4,23 +4,29 @@
 // Who needs it: code that runs inside a region where allocation is not
 // allowed, e.g. a real-time loop that has reserved all its memory up front,
 // or a host framework whose own allocator owns the device and forbids
-// cudaMalloc from libraries.  The call waits for its stream at the end (it
-// reads the iteration count back), so it cannot itself be recorded by
-// stream capture.  Such a
-// caller allocates its inputs and outputs itself and passes them in; the
-// solver's work vectors and reduction scratch live in one file-scope device
-// array of fixed size (LPM_NOALLOC_MAX_DOF), so no call allocates or frees.
+// cudaMalloc from libraries.  Such a caller allocates its inputs and outputs
+// itself and passes them in; the solver's work vectors and reduction scratch
+// live in one file-scope device array of fixed size (LPM_NOALLOC_MAX_DOF),
+// so no call allocates or frees.  The call waits for its stream at the end
+// to read the iteration count back.
 //
-// The array belongs to the library: every GPU that loads liblpmgpu holds it
-// (about 33.6 MB) until the process exits, and all calls on a device share
-// it.  Two calls whose work overlaps on the same GPU (different streams, or
-// different host threads) therefore race; serialise them.  Each call clears
-// the parts that must start at zero (the reduction tickets) before use.
+// The array belongs to the library: it is created when the library's device
+// code is loaded on a GPU (about 33.6 MB), whether or not this entry point
+// is ever called, and stays until the process exits; all calls on a device
+// share it.  Two calls whose work overlaps on the same GPU (different
+// streams, or different host threads) therefore race; serialise them.  Each
+// call clears the parts that must start at zero (the reduction tickets)
+// before use.
 //
 // Device address: in host code the array's name is a host-side stand-in, not
 // a device address, so the first call on each device looks the address up
 // with cudaGetSymbolAddress (with that device current) and caches it.  Make
-// that first call before any stream capture begins.
+// that first call before any stream capture begins.  The cached address
+// belongs to the device's context: after a device reset (cudaDeviceReset) it
+// is stale, so do not use the library across one.
+//
+// The product walks the caller's block CSR one row per thread (plain loads,
+// no sliced layout), so an iteration costs more than one of lpm_solve.
 #include <cfloat>
 #include <cmath>
 #include <mutex>

@@ -27,8 +27,7 @@ struct Grid {
 };
 
 __device__ __forceinline__ double ref_distance(const double* a, const double* b) {
-  const double dx = __dsub_rn(a[0], b[0]), dy = __dsub_rn(a[1], b[1]), dz = __dsub_rn(a[2], b[2]);
-  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+  return bond_length(__dsub_rn(a[0], b[0]), __dsub_rn(a[1], b[1]), __dsub_rn(a[2], b[2]));
 }
 
 __device__ __forceinline__ void cell_of(const Grid& g, const double* x, int (&c)[3]) {

@@ -27,7 +27,10 @@ def test_reference_arm_prints_one_contract_line():
     import bench
     assert d["impl"] == "reference"
     assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT and d["higher_is_better"] is True
-    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 1 and d["n_gpus"] == 1
+    # complete steps are timed (no warm-up on the CPU): steps = the steps timed
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1
+    assert abs(d["ms_per_step"] * d["steps"] - 1e3 * d["steps"] / d["value"]) < 1e-6 * d["ms_per_step"]
+    assert d["config"]["tangent"] and d["config"]["bc"]
     assert d["config"]["workload"].startswith("SC 7^3 lattice")
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]

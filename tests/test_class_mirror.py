@@ -81,3 +81,43 @@ def test_example_matches_reference_headers(tmp_path):
     u_ref = g["xyz"] - g["xyz0"]
     u_gpu = d[:, 1:4] - d[:, 4:7]
     assert np.abs(u_gpu - u_ref).max() <= 1e-8 * np.abs(u_ref).max()
+
+
+FD_PROGRAM = r'''
+#include "lpm.h"
+#include "particle.h"
+#include "assembly.h"
+#include "utilities.h"
+#include "stiffness.h"
+#include "load_step.h"
+#include "solver_static.h"
+int main() {
+  UnitCell cell(LatticeType::Hexagon2D, 0.25);
+  double angles[] = {0.0, 0.0, 0.0};
+  Eigen::MatrixXd R = createRMatrix(0, angles);
+  std::array<double, 2 * NDIM> box{0.0, 3.0, 0.0, 3.0, 0.0, 1.0};
+  std::vector<std::array<double, NDIM>> xyz = createPlateHEX2D(box, cell, R);
+  Assembly<2> ass{xyz, box, cell, ParticleType::Elastic};
+  for (Particle<2>* p : ass.pt_sys)
+    dynamic_cast<ParticleElastic<2>*>(p)->setParticleProperty(0.0, true, 69e3, 0.3, 1.0);
+  SolverStatic<2> solv{-1, ass, StiffnessMode::FiniteDifference, SolverMode::CG, "fd.dump", 30, 1e-5};
+  printf("constructed\n");
+  return 0;
+}
+'''
+
+
+@pytest.mark.gpu
+def test_finite_difference_tangent_is_refused(tmp_path):
+    """StiffnessMode::FiniteDifference (stiffness.h:103-154) has no device
+    version: a program asking for it stops with an error when the solver is
+    constructed, instead of running with the analytical tangent.  (The
+    Assembly constructor already searches bonds on the GPU.)"""
+    src = tmp_path / "fd.cpp"
+    src.write_text(FD_PROGRAM)
+    exe = str(tmp_path / "fd")
+    compile_example(str(src), exe, link=True)
+    r = subprocess.run([exe], capture_output=True, text=True, cwd=str(tmp_path), timeout=120)
+    assert r.returncode == 1
+    assert "FiniteDifference is not supported" in r.stderr
+    assert "constructed" not in r.stdout
