@@ -131,7 +131,10 @@ def test_ct_fatigue_cycles_match_oracle():
         new_o = oracle_cycle(o, apply, f, f_min, F_MAX, f_min, 1, 1000)
         assert rc["status"] == 0 and rc["new_damage"] == new_o
     scale = np.abs(o.get(oracle.XYZ) - xyz).max()
-    assert np.abs((g.download(capi.F_XYZ) - xyz) - (o.get(oracle.XYZ) - xyz)).max() <= 1e-8 * scale
+    eu = np.abs((g.download(capi.F_XYZ) - xyz) - (o.get(oracle.XYZ) - xyz)).max() / scale
+    print("[parity] CT fatigue: displacement %.3e, damage %.3e" % (
+        eu, np.abs(g.download(capi.F_DAMAGE) - o.get(oracle.DAMAGE)).max() / o.get(oracle.DAMAGE).max()))
+    assert eu <= 1e-8
     d_o, d_g = o.get(oracle.DAMAGE), g.download(capi.F_DAMAGE)
     assert d_o.max() > 0
     assert np.abs(d_g - d_o).max() <= 1e-8 * d_o.max()

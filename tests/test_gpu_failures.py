@@ -29,7 +29,7 @@ def test_cut_back_halves_the_step_like_the_oracle():
     in one step with at most 4 Newton iterations: the step fails, is cut,
     and its halves (and quarters) are solved from the reset state.  The GPU
     takes at least one cut and ends where the oracle, running the same
-    cut-back, ends: positions within 1e-9, plastic stretch within 1e-8."""
+    cut-back, ends: positions and plastic stretch within 1e-10."""
     dim, xyz, p1, p2, layer, Kn, Tv, cell = plate(15, 15)
     du = 0.2
     groups, apply, dd = tension_bcs(xyz, dim, du)
@@ -50,7 +50,7 @@ def test_cut_back_halves_the_step_like_the_oracle():
     derr = rel(g.download(capi.B_DLP), o.get_bond(oracle.DLP))
     print("[cut-back] displacement %.3e, plastic stretch %.3e" % (err, derr))
     assert np.abs(o.get_bond(oracle.DLP)).max() > 0
-    assert err <= 1e-9 and derr <= 1e-8
+    assert err <= 1e-10 and derr <= 1e-10
     # one cut too many: the step reports non-convergence after max_cuts
     g2 = make_gpu(dim, xyz, p1, p2, layer, Kn, Tv, cell)
     g2.set_law(capi.LAW_J2, J2)
