@@ -509,12 +509,14 @@ def column_index_bytes(g):
     return 2 if off.size == 0 or off.max() <= 32767 else 4
 
 
-def spmv_bytes(nblk, n, dim, value_bytes, index_bytes=4, row_sums=False):
+def spmv_bytes(nblk, n, dim, value_bytes, index_bytes=4, row_sums=False, out_bytes=None):
     """Algorithmic bytes of one CG sparse-product launch: every block's
     dim*dim values and column index, each row's block count, the search
-    direction read once and the product written once, and for the FP32
+    direction read once and the product written once (out_bytes per entry:
+    the FP32 product writes a double-float pair, 8 bytes), and for the FP32
     difference form each row's block row sum (dim*dim FP32 values)."""
-    b = nblk * (dim * dim * value_bytes + index_bytes) + n * 4 + 2 * n * dim * value_bytes
+    out = value_bytes if out_bytes is None else out_bytes
+    b = nblk * (dim * dim * value_bytes + index_bytes) + n * 4 + n * dim * (value_bytes + out)
     return b + (n * dim * dim * 4 if row_sums else 0)
 
 
@@ -706,7 +708,7 @@ def run_gb300(args):
     n, nb, nblk = g.n, g.nb, g.nblk
     launches = mixed["ktime"]["spmv32_launches"]
     avg_ms = mixed["ktime"]["spmv32_ms"] / max(launches, 1)
-    byts = spmv_bytes(nblk, n, 3, 4, column_index_bytes(g), row_sums=True)
+    byts = spmv_bytes(nblk, n, 3, 4, column_index_bytes(g), row_sums=True, out_bytes=8)
     peak, peak_kind = measured_peaks()
     achieved = byts / (avg_ms * 1e-3) / 1e9
     traffic = profiled_traffic("float", nblk)

@@ -105,6 +105,32 @@ __device__ __forceinline__ void df_add(float& s, float& c, float x, float xc) {
   c = __fadd_rn(c, __fadd_rn(xc, e));
 }
 
+// Double-float vector arithmetic: a value held as an FP32 pair (hi, lo) with
+// |lo| at most half an ulp of hi (Dekker, "A floating-point technique for
+// extending the available precision", Numer. Math. 18 (1971)), built from
+// TwoSum and TwoProduct by FMA as in dot2_acc.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float z = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+}
+
+// (xh, xl) += (ah, al) * (bh, bl), normalised; the product's low-order cross
+// terms are kept, the (al, bl) term (below the pair's precision) is not.
+__device__ __forceinline__ void df_madd(float& xh, float& xl, float ah, float al, float bh, float bl) {
+  const float ph = __fmul_rn(ah, bh);
+  const float pl = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -ph)));
+  float sh, se;
+  two_sum(xh, ph, sh, se);
+  two_sum(sh, __fadd_rn(se, __fadd_rn(xl, pl)), xh, xl);
+}
+
+// A double rounded to a normalised FP32 pair.
+__device__ __forceinline__ void df_split(double v, float& h, float& l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
 // Block sum of per-thread double-float partials, result in thread 0 as
 // FP64.  Both the warp and the cross-warp stage stay in FP32 pairs: GB300's
 // FP64 pipe takes a whole warp slot even for a one-lane instruction, so an
@@ -174,7 +200,8 @@ __device__ __forceinline__ float op_load1(const float* a) {
 // slot order either way.
 template <int DIM, bool OFF16, bool KEEP>
 __device__ __forceinline__ void row_product32(const SellView& v, const float* __restrict__ A,
-                                              const float* __restrict__ p, int row, float (&y)[DIM]) {
+                                              const float* __restrict__ p, int row, float (&y)[DIM],
+                                              float (&ylo)[DIM]) {
   float sc[DIM], cc[DIM];
 #pragma unroll
   for (int r = 0; r < DIM; ++r) sc[r] = cc[r] = 0.f;
@@ -247,7 +274,7 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
   for (int r = 0; r < DIM; ++r) {
 #pragma unroll
     for (int k = 0; k < DIM; ++k) dot2_acc(sc[r], cc[r], __ldg(&Si[r * DIM + k]), pi[k]);
-    y[r] = __fadd_rn(sc[r], cc[r]);
+    two_sum(sc[r], cc[r], y[r], ylo[r]);  // the compensated sum as a double-float pair
   }
 }
 
@@ -255,12 +282,20 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
 // element's 32-byte run (four blocks) is read as two back-to-back 16-byte
 // loads, so both halves of a sector are used by the same instruction pair.
 // The blocks past the slice's groups follow one at a time.
-// With ADD32 the product is taken of p + p32 (an FP64 vector plus an FP32
-// increment not yet folded into it).
+// With ADD32 the product is taken of p + (p32 + p32lo) (an FP64 vector plus
+// a double-float increment not yet folded into it).
+template <int DIM, bool ADD32 = false>
+__device__ __forceinline__ double add_increment(const double* __restrict__ p, const float* __restrict__ p32,
+                                                const float* __restrict__ p32lo, int64_t i) {
+  if (ADD32) return __ldg(&p[i]) + ((double)__ldg(&p32[i]) + (double)__ldg(&p32lo[i]));
+  return __ldg(&p[i]);
+}
+
 template <int DIM, bool ADD32 = false>
 __device__ __forceinline__ void row_product(const SellView& v, const double* __restrict__ A,
                                             const double* __restrict__ p, int row, double (&y)[DIM],
-                                            const float* __restrict__ p32 = nullptr) {
+                                            const float* __restrict__ p32 = nullptr,
+                                            const float* __restrict__ p32lo = nullptr) {
 #pragma unroll
   for (int r = 0; r < DIM; ++r) y[r] = 0.0;
   const int len = v.rowlen[row];
@@ -275,7 +310,7 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
     for (int t = 0; t < kVec; ++t) {
       const int64_t c = (int64_t)comp(c4, t) * DIM;
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) pc[t][k] = ADD32 ? __ldg(&p[c + k]) + (double)__ldg(&p32[c + k]) : __ldg(&p[c + k]);
+      for (int k = 0; k < DIM; ++k) pc[t][k] = add_increment<DIM, ADD32>(p, p32, p32lo, c + k);
     }
 #pragma unroll
     for (int r = 0; r < DIM; ++r)
@@ -295,7 +330,7 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
     const int64_t c = (int64_t)__ldg(&v.scol[st]) * DIM;
     double pc[DIM];
 #pragma unroll
-    for (int q = 0; q < DIM; ++q) pc[q] = ADD32 ? __ldg(&p[c + q]) + (double)__ldg(&p32[c + q]) : __ldg(&p[c + q]);
+    for (int q = 0; q < DIM; ++q) pc[q] = add_increment<DIM, ADD32>(p, p32, p32lo, c + q);
 #pragma unroll
     for (int r = 0; r < DIM; ++r)
 #pragma unroll
@@ -312,27 +347,37 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
 template <typename T, int DIM>
 constexpr int kSpmvMinBlocks = sizeof(T) == 8 ? 4 : DIM == 3 ? 2 : 0;
 
+// q = A p and the p.q sum for alpha.  The FP32 product (mixed solve) writes
+// q as a double-float pair: its high words to q, its low words to qlo.
 template <typename T, int DIM, bool OFF16 = false, bool KEEP = false>
 __global__ void __launch_bounds__(256, (kSpmvMinBlocks<T, DIM>)) k_cg_spmv(SellView v, const T* __restrict__ A,
                                                                          const T* __restrict__ p, T* __restrict__ q,
                                                                          CgScalars* cg, double* partials,
-                                                                         unsigned int* ticket) {
+                                                                         unsigned int* ticket,
+                                                                         float* __restrict__ qlo) {
   if (cg->done) return;
   double acc = 0.0;
   float ps = 0.f, pc = 0.f;  // FP32: p.q as a compensated double-float sum
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < v.n; row += gridDim.x * blockDim.x) {
     T y[DIM];
-    if constexpr (sizeof(T) == 4)
-      row_product32<DIM, OFF16, KEEP>(v, A, p, row, y);
-    else
+    if constexpr (sizeof(T) == 4) {
+      float yl[DIM];
+      row_product32<DIM, OFF16, KEEP>(v, A, p, row, y, yl);
+#pragma unroll
+      for (int r = 0; r < DIM; ++r) {
+        const float pr = p[(int64_t)row * DIM + r];
+        q[(int64_t)row * DIM + r] = y[r];
+        qlo[(int64_t)row * DIM + r] = yl[r];
+        dot2_acc(ps, pc, pr, y[r]);
+        pc = fmaf(pr, yl[r], pc);
+      }
+    } else {
       row_product<DIM>(v, A, p, row, y);
 #pragma unroll
-    for (int r = 0; r < DIM; ++r) {
-      q[(int64_t)row * DIM + r] = y[r];
-      if constexpr (sizeof(T) == 4)
-        dot2_acc(ps, pc, (float)p[(int64_t)row * DIM + r], (float)y[r]);
-      else
+      for (int r = 0; r < DIM; ++r) {
+        q[(int64_t)row * DIM + r] = y[r];
         acc += (double)p[(int64_t)row * DIM + r] * (double)y[r];
+      }
     }
   }
   double w[1], tot[1];
@@ -347,7 +392,7 @@ __global__ void __launch_bounds__(256, (kSpmvMinBlocks<T, DIM>)) k_cg_spmv(SellV
   }
   if (last && threadIdx.x == 0) {
     cg->alpha = cg->abs_new / tot[0];
-    cg->alpha32 = (float)cg->alpha;
+    df_split(cg->alpha, cg->alpha32, cg->alpha32lo);
   }
 }
 
@@ -389,21 +434,25 @@ __device__ __forceinline__ double rhs_scale(const CgScalars* cg) {
   return m > 0.0 ? ldexp(1.0, -ilogb(m)) : 1.0;
 }
 
-// Mixed solve set-up: r32 = s b, x32 = 0, p32 = M r32, |s b|^2, r.z.
+// Mixed solve set-up: (r32, r32lo) = s b, x = 0, p32 = M r32, |s b|^2, r.z.
 __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __restrict__ x32,
-                          float* __restrict__ r32, float* __restrict__ p32, const float* __restrict__ invd,
-                          CgScalars* cg, double tol, long long maxit, double* partials, unsigned int* ticket) {
+                          float* __restrict__ x32lo, float* __restrict__ r32, float* __restrict__ r32lo,
+                          float* __restrict__ p32, const float* __restrict__ invd, CgScalars* cg, double tol,
+                          long long maxit, double* partials, unsigned int* ticket) {
   double v[2] = {0.0, 0.0};
   const double sc = rhs_scale(cg);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
     const double bi = b[i] * sc;
-    const float r = (float)bi;
+    float r, rl;
+    df_split(bi, r, rl);
     const float z = invd[i] * r;
     x32[i] = 0.f;
+    x32lo[i] = 0.f;
     r32[i] = r;
+    r32lo[i] = rl;
     p32[i] = z;
     v[0] += bi * bi;
-    v[1] += (double)r * (double)z;
+    v[1] += bi * (double)z;
   }
   double tot[2];
   if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
@@ -418,7 +467,7 @@ __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __r
     cg->ru_count = 0;
     cg->graph_passes = 0;
     cg->zcoef = 1.0;
-    cg->alpha32 = cg->beta32 = 0.f;
+    cg->alpha32 = cg->beta32 = cg->alpha32lo = cg->beta32lo = 0.f;
     cg->zcoef32 = 1.f;
     cg->bscale = sc;
     cg->rmax = sqrt(tot[0]);
@@ -433,24 +482,34 @@ __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __r
   }
 }
 
-// FP32 update of x32, r32 with FP64 |r|^2 and r.z.  The last block either
-// asks for a reliable update (residual fell by kDelta, or below the
-// tolerance: the true residual decides) or forms beta.
-__global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restrict__ x, float* __restrict__ r,
+// Double-float update of the solution increment x and the residual r:
+// x += alpha p, r -= alpha q, with alpha a double-float pair, then FP64
+// |r|^2 and r.z (z = M r rounded to FP32).  The last block either asks for a
+// reliable update (residual fell by kDelta, or below the tolerance: the true
+// residual decides) or forms beta.
+__global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restrict__ x, float* __restrict__ xlo,
+                                                   float* __restrict__ r, float* __restrict__ rlo,
                                                    const float* __restrict__ p, const float* __restrict__ q,
-                                                   const float* __restrict__ invd, CgScalars* cg, double* partials,
-                                                   unsigned int* ticket, cudaGraphConditionalHandle ru_cond) {
+                                                   const float* __restrict__ qlo, const float* __restrict__ invd,
+                                                   CgScalars* cg, double* partials, unsigned int* ticket,
+                                                   cudaGraphConditionalHandle ru_cond) {
   if (cg->done) return;
-  const float alpha = cg->alpha32;
+  const float ah = cg->alpha32, al = cg->alpha32lo;
   // |r|^2 and r.z as compensated double-float sums, FP64 only per warp
   float s[2] = {0.f, 0.f}, c[2] = {0.f, 0.f};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
-    const float ri = r[i] - alpha * q[i];
-    x[i] = x[i] + alpha * p[i];
-    r[i] = ri;
-    const float zi = invd[i] * ri;
-    dot2_acc(s[0], c[0], ri, ri);
-    dot2_acc(s[1], c[1], ri, zi);
+    float rh = r[i], rl = rlo[i], xh = x[i], xl = xlo[i];
+    df_madd(rh, rl, -ah, -al, q[i], qlo[i]);
+    df_madd(xh, xl, ah, al, p[i], 0.f);
+    x[i] = xh;
+    xlo[i] = xl;
+    r[i] = rh;
+    rlo[i] = rl;
+    const float zi = invd[i] * rh;
+    dot2_acc(s[0], c[0], rh, rh);
+    c[0] = fmaf(2.f * rh, rl, c[0]);
+    dot2_acc(s[1], c[1], rh, zi);
+    c[1] = fmaf(rl, zi, c[1]);
   }
   double v[2];
   block_df_sum<2>(s, c, v);
@@ -472,7 +531,7 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
       cg->abs_new = tot[1];
       cg->beta = tot[1] / old;
       cg->zcoef = 1.0;
-      cg->beta32 = (float)cg->beta;
+      df_split(cg->beta, cg->beta32, cg->beta32lo);
       cg->zcoef32 = 1.f;
     }
     if (cg->it >= cg->maxit) cg->done = 2;
@@ -480,29 +539,32 @@ __global__ void __launch_bounds__(256) k_mx_update(int64_t ndof, float* __restri
   }
 }
 
-// End of the solve: x64 += x32 (what the last iterations added), x32 = 0,
-// and the right-hand-side scaling undone.
-__global__ void k_mx_fold(int64_t ndof, float* __restrict__ x32, double* __restrict__ x64, const CgScalars* cg) {
+// End of the solve: x64 += x (what the last iterations added, a double-float
+// pair), x = 0, and the right-hand-side scaling undone.
+__global__ void k_mx_fold(int64_t ndof, float* __restrict__ x32, float* __restrict__ x32lo, double* __restrict__ x64,
+                          const CgScalars* cg) {
   const double unscale = 1.0 / cg->bscale;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
-    x64[i] = (x64[i] + (double)x32[i]) * unscale;
+    x64[i] = (x64[i] + ((double)x32[i] + (double)x32lo[i])) * unscale;
     x32[i] = 0.f;
+    x32lo[i] = 0.f;
   }
 }
 
-// Reliable update, part 1: r64 = s b - A64 (x64 + x32) and |r64|^2;
-// converged when it is below the threshold.
+// Reliable update, part 1: r64 = s b - A64 (x64 + x) with the increment x a
+// double-float pair, and |r64|^2; converged when it is below the threshold.
 template <int DIM>
 __global__ void __launch_bounds__(256) k_mx_residual(SellView v, const double* __restrict__ A,
                                                      const double* __restrict__ x, const float* __restrict__ x32,
-                                                     const double* __restrict__ b, double* __restrict__ r,
-                                                     CgScalars* cg, double* partials, unsigned int* ticket) {
+                                                     const float* __restrict__ x32lo, const double* __restrict__ b,
+                                                     double* __restrict__ r, CgScalars* cg, double* partials,
+                                                     unsigned int* ticket) {
   if (cg->done || !cg->ru) return;
   double acc = 0.0;
   const double sc = cg->bscale;
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < v.n; row += gridDim.x * blockDim.x) {
     double y[DIM];
-    row_product<DIM, true>(v, A, x, row, y, x32);
+    row_product<DIM, true>(v, A, x, row, y, x32, x32lo);
 #pragma unroll
     for (int c = 0; c < DIM; ++c) {
       const double ri = b[(int64_t)row * DIM + c] * sc - y[c];
@@ -521,22 +583,28 @@ __global__ void __launch_bounds__(256) k_mx_residual(SellView v, const double* _
   }
 }
 
-// Reliable update, part 2: x64 += x32, x32 = 0, r32 = r64, new r.z and
-// beta, reset the maximum.  The replaced residual is no longer orthogonal to
-// the last search direction; the next direction is formed from
-// p - (r.p / r.z) z, which restores r.p = 0, i.e. p_new = (1 - beta gamma) z + beta p.
+// Reliable update, part 2: x64 += x, x = 0, r = r64 (as a double-float
+// pair), new r.z and beta, reset the maximum.  The replaced residual is no
+// longer orthogonal to the last search direction; the next direction is
+// formed from p - (r.p / r.z) z, which restores r.p = 0, i.e.
+// p_new = (1 - beta gamma) z + beta p.
 __global__ void k_mx_replace(int64_t ndof, const double* __restrict__ r64, float* __restrict__ r32,
-                             float* __restrict__ x32, double* __restrict__ x64, const float* __restrict__ p32,
-                             const float* __restrict__ invd, CgScalars* cg, double* partials, unsigned int* ticket) {
+                             float* __restrict__ r32lo, float* __restrict__ x32, float* __restrict__ x32lo,
+                             double* __restrict__ x64, const float* __restrict__ p32, const float* __restrict__ invd,
+                             CgScalars* cg, double* partials, unsigned int* ticket) {
   if (cg->done || !cg->ru) return;
   double v[2] = {0.0, 0.0};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
-    x64[i] += (double)x32[i];
+    x64[i] += (double)x32[i] + (double)x32lo[i];
     x32[i] = 0.f;
-    const float r = (float)r64[i];
-    r32[i] = r;
-    v[0] += (double)r * (double)(invd[i] * r);
-    v[1] += (double)r * (double)p32[i];
+    x32lo[i] = 0.f;
+    const double ri = r64[i];
+    float rh, rl;
+    df_split(ri, rh, rl);
+    r32[i] = rh;
+    r32lo[i] = rl;
+    v[0] += ri * (double)(invd[i] * rh);
+    v[1] += ri * (double)p32[i];
   }
   double tot[2];
   if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
@@ -545,14 +613,15 @@ __global__ void k_mx_replace(int64_t ndof, const double* __restrict__ r64, float
     cg->beta = tot[0] / old;
     const double gamma = tot[0] != 0.0 ? tot[1] / tot[0] : 0.0;
     cg->zcoef = 1.0 - cg->beta * gamma;
-    cg->beta32 = (float)cg->beta;
+    df_split(cg->beta, cg->beta32, cg->beta32lo);
     cg->zcoef32 = (float)cg->zcoef;
     cg->rmax = sqrt(cg->rr);
     cg->ru = 0;
   }
 }
 
-// p = zcoef z + beta p with z = M^-1 r (FP32 vectors).
+// p = zcoef z + beta p with z = M^-1 r (r's high words), beta a
+// double-float pair, p in FP32.
 // Inside the solve graph it is the last kernel of an iteration: block 0
 // sets the loop condition (continue while nothing has ended the solve) and
 // counts the iteration's kernel launches.
@@ -564,9 +633,11 @@ __global__ void __launch_bounds__(256) k_mx_pupdate(int64_t ndof, const float* _
     cg->graph_passes += 1;
   }
   if (cg->done) return;
-  const float beta = cg->beta32, zc = cg->zcoef32;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = zc * (invd[i] * r[i]) + beta * p[i];
+  const float bh = cg->beta32, bl = cg->beta32lo, zc = cg->zcoef32;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
+    const float pi = p[i];
+    p[i] = fmaf(bh, pi, fmaf(bl, pi, __fmul_rn(zc, __fmul_rn(invd[i], r[i]))));
+  }
 }
 
 // Grid of the FP64 row kernels (product, true residual): these are bound by
@@ -646,9 +717,9 @@ int run_cg(lpm_handle* h, const T* A, const T* b, T* x, T* r, T* p, T* q, const 
         if (e0) cudaEventRecord(e0, h->stream);
       }
       if (dim == 3)
-        k_cg_spmv<T, 3><<<GR, 256, 0, h->stream>>>(sv, A, p, q, d.cg, d.red.partials, d.red.ticket + 3);
+        k_cg_spmv<T, 3><<<GR, 256, 0, h->stream>>>(sv, A, p, q, d.cg, d.red.partials, d.red.ticket + 3, nullptr);
       else
-        k_cg_spmv<T, 2><<<GR, 256, 0, h->stream>>>(sv, A, p, q, d.cg, d.red.partials, d.red.ticket + 3);
+        k_cg_spmv<T, 2><<<GR, 256, 0, h->stream>>>(sv, A, p, q, d.cg, d.red.partials, d.red.ticket + 3, nullptr);
       LPM_LAUNCHED(h, "k_cg_spmv");
       if (timing && e1) cudaEventRecord(e1, h->stream);
       k_cg_update<T><<<GV, 256, 0, h->stream>>>(ndof, x, r, p, q, invd, d.cg, d.red.partials, d.red.ticket + 4);
@@ -733,7 +804,7 @@ struct MixedGrids {
 
 // The FP32 product of a mixed solve: 16-bit column offsets when they fit;
 // the operator kept in L2 when its FP32 values take at most kKeepBytes.
-using Spmv32Fn = void (*)(SellView, const float*, const float*, float*, CgScalars*, double*, unsigned int*);
+using Spmv32Fn = void (*)(SellView, const float*, const float*, float*, CgScalars*, double*, unsigned int*, float*);
 constexpr long long kKeepBytes = 64LL << 20;  // half of GB300's L2
 template <int DIM>
 Spmv32Fn spmv32_fn_dim(bool o16, bool keep) {
@@ -820,10 +891,10 @@ int build_mixed_graph(lpm_handle* h, const SellView& sv, const MixedGrids& mg) {
   cudaError_t e;
   const Spmv32Fn spmv = spmv32_fn(h, sv);
   LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, spmv, mg.spmv, 256, sv, (const float*)d.A32, (const float*)d.p32,
-                         d.q32, d.cg, d.red.partials, d.red.ticket + 3));
-  LPM_CUDA(h, add_kernel(&n_upd, body, &n_spmv, k_mx_update, mg.update, 256, ndof, d.x32, d.r32, (const float*)d.p32,
-                         (const float*)d.q32, (const float*)d.invd32, d.cg, d.red.partials, d.red.ticket + 4,
-                         ru_cond));
+                         d.q32, d.cg, d.red.partials, d.red.ticket + 3, d.q32lo));
+  LPM_CUDA(h, add_kernel(&n_upd, body, &n_spmv, k_mx_update, mg.update, 256, ndof, d.x32, d.x32lo, d.r32, d.r32lo,
+                         (const float*)d.p32, (const float*)d.q32, (const float*)d.q32lo, (const float*)d.invd32,
+                         d.cg, d.red.partials, d.red.ticket + 4, ru_cond));
   cudaGraphNodeParams ip = {};
   ip.type = cudaGraphNodeTypeConditional;
   ip.conditional.handle = ru_cond;
@@ -833,13 +904,16 @@ int build_mixed_graph(lpm_handle* h, const SellView& sv, const MixedGrids& mg) {
   cudaGraph_t ifb = ip.conditional.phGraph_out[0];
   if (dim == 3)
     e = add_kernel(&n_res, ifb, nullptr, k_mx_residual<3>, mg.residual, 256, sv, (const double*)d.A64, (const double*)d.x64,
-                   (const float*)d.x32, (const double*)d.rhs, d.r64, d.cg, d.red.partials, d.red.ticket + 6);
+                   (const float*)d.x32, (const float*)d.x32lo, (const double*)d.rhs, d.r64, d.cg, d.red.partials,
+                   d.red.ticket + 6);
   else
     e = add_kernel(&n_res, ifb, nullptr, k_mx_residual<2>, mg.residual, 256, sv, (const double*)d.A64, (const double*)d.x64,
-                   (const float*)d.x32, (const double*)d.rhs, d.r64, d.cg, d.red.partials, d.red.ticket + 6);
+                   (const float*)d.x32, (const float*)d.x32lo, (const double*)d.rhs, d.r64, d.cg, d.red.partials,
+                   d.red.ticket + 6);
   LPM_CUDA(h, e);
-  LPM_CUDA(h, add_kernel(&n_rep, ifb, &n_res, k_mx_replace, mg.replace, 256, ndof, (const double*)d.r64, d.r32, d.x32, d.x64,
-                         (const float*)d.p32, (const float*)d.invd32, d.cg, d.red.partials, d.red.ticket + 7));
+  LPM_CUDA(h, add_kernel(&n_rep, ifb, &n_res, k_mx_replace, mg.replace, 256, ndof, (const double*)d.r64, d.r32, d.r32lo,
+                         d.x32, d.x32lo, d.x64, (const float*)d.p32, (const float*)d.invd32, d.cg, d.red.partials,
+                         d.red.ticket + 7));
   LPM_CUDA(h, add_kernel(&n_pup, body, &n_if, k_mx_pupdate, mg.pupdate, 256, ndof, (const float*)d.r32,
                          (const float*)d.invd32, d.p32, d.cg, loop_cond));
   LPM_CUDA(h, cudaGraphInstantiate(&h->mx_exec, g, 0));
@@ -875,10 +949,10 @@ int build_fp64_graph(lpm_handle* h, const double* A, const double* b, double* x,
   cudaGraph_t body = wp.conditional.phGraph_out[0];
   if (h->dim == 3)
     LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, k_cg_spmv<double, 3>, GR, 256, sv, A, (const double*)p, q, d.cg,
-                           d.red.partials, d.red.ticket + 3));
+                           d.red.partials, d.red.ticket + 3, (float*)nullptr));
   else
     LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, k_cg_spmv<double, 2>, GR, 256, sv, A, (const double*)p, q, d.cg,
-                           d.red.partials, d.red.ticket + 3));
+                           d.red.partials, d.red.ticket + 3, (float*)nullptr));
   LPM_CUDA(h, add_kernel(&n_upd, body, &n_spmv, k_cg_update<double>, GV, 256, ndof, x, r, (const double*)p,
                          (const double*)q, invd, d.cg, d.red.partials, d.red.ticket + 4));
   LPM_CUDA(h, add_kernel(&n_pup, body, &n_upd, k_cg_pupdate<double>, GV, 256, ndof, (const double*)r, invd, p, d.cg,
@@ -896,7 +970,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   const int64_t ndof = (int64_t)h->n * dim;
   if (maxit < 0) maxit = 2LL * ndof;
   if (!d.b32) {  // FP32 work vectors, allocated on the first mixed solve
-    float** vecs[6] = {&d.b32, &d.x32, &d.r32, &d.p32, &d.q32, &d.invd32};
+    float** vecs[9] = {&d.b32, &d.x32, &d.r32, &d.p32, &d.q32, &d.invd32, &d.r32lo, &d.q32lo, &d.x32lo};
     for (float** v : vecs) {
       *v = (float*)dev_alloc(h, sizeof(float) * (size_t)ndof);
       if (!*v) return LPM_ERR_NOMEM;
@@ -906,7 +980,8 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
     const int st0 = convert_A32(h);
     if (st0) return st0;
   }
-  if (!d.A32 || !d.S32 || !d.x32 || !d.r32 || !d.p32 || !d.q32 || !d.invd32 || !d.x64 || !d.r64 || !d.rhs || !d.disp) {
+  if (!d.A32 || !d.S32 || !d.x32 || !d.r32 || !d.p32 || !d.q32 || !d.invd32 || !d.r32lo || !d.q32lo || !d.x32lo ||
+      !d.x64 || !d.r64 || !d.rhs || !d.disp) {
     h->err = "mixed solve: work buffers missing";
     return LPM_ERR_STATE;
   }
@@ -921,8 +996,8 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   LPM_CUDA(h, cudaMemsetAsync(&d.cg->bmax_bits, 0, sizeof(unsigned long long), h->stream));
   k_absmax<<<GV, 256, 0, h->stream>>>(ndof, d.rhs, d.cg);
   LPM_LAUNCHED(h, "k_absmax");
-  k_mx_init<<<GV, 256, 0, h->stream>>>(ndof, d.rhs, d.x32, d.r32, d.p32, d.invd32, d.cg, tol, maxit, d.red.partials,
-                                       d.red.ticket + 2);
+  k_mx_init<<<GV, 256, 0, h->stream>>>(ndof, d.rhs, d.x32, d.x32lo, d.r32, d.r32lo, d.p32, d.invd32, d.cg, tol, maxit,
+                                       d.red.partials, d.red.ticket + 2);
   LPM_LAUNCHED(h, "k_mx_init");
   const bool timing = h->timing;
   const size_t ev0 = h->ev_used;
@@ -947,21 +1022,21 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
         e1 = next_event(h);
         if (e0) cudaEventRecord(e0, h->stream);
       }
-      spmv32<<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials, d.red.ticket + 3);
+      spmv32<<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials, d.red.ticket + 3, d.q32lo);
       LPM_LAUNCHED(h, "k_cg_spmv");
       if (timing && e1) cudaEventRecord(e1, h->stream);
-      k_mx_update<<<mg.update, 256, 0, h->stream>>>(ndof, d.x32, d.r32, d.p32, d.q32, d.invd32, d.cg, d.red.partials,
-                                             d.red.ticket + 4, 0);
+      k_mx_update<<<mg.update, 256, 0, h->stream>>>(ndof, d.x32, d.x32lo, d.r32, d.r32lo, d.p32, d.q32, d.q32lo, d.invd32,
+                                                    d.cg, d.red.partials, d.red.ticket + 4, 0);
       LPM_LAUNCHED(h, "k_mx_update");
       if (dim == 3)
-        k_mx_residual<3><<<mg.residual, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.rhs, d.r64, d.cg, d.red.partials,
-                                                    d.red.ticket + 6);
+        k_mx_residual<3><<<mg.residual, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.x32lo, d.rhs, d.r64, d.cg,
+                                                             d.red.partials, d.red.ticket + 6);
       else
-        k_mx_residual<2><<<mg.residual, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.rhs, d.r64, d.cg, d.red.partials,
-                                                    d.red.ticket + 6);
+        k_mx_residual<2><<<mg.residual, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.x32lo, d.rhs, d.r64, d.cg,
+                                                             d.red.partials, d.red.ticket + 6);
       LPM_LAUNCHED(h, "k_mx_residual");
-      k_mx_replace<<<mg.replace, 256, 0, h->stream>>>(ndof, d.r64, d.r32, d.x32, d.x64, d.p32, d.invd32, d.cg, d.red.partials,
-                                              d.red.ticket + 7);
+      k_mx_replace<<<mg.replace, 256, 0, h->stream>>>(ndof, d.r64, d.r32, d.r32lo, d.x32, d.x32lo, d.x64, d.p32, d.invd32,
+                                                      d.cg, d.red.partials, d.red.ticket + 7);
       LPM_LAUNCHED(h, "k_mx_replace");
       k_mx_pupdate<<<mg.pupdate, 256, 0, h->stream>>>(ndof, d.r32, d.invd32, d.p32, d.cg, 0);
       LPM_LAUNCHED(h, "k_mx_pupdate");
@@ -972,7 +1047,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
     if (batch < 64) batch *= 2;
   }
   // fold what the iterations since the last replacement added
-  k_mx_fold<<<GV, 256, 0, h->stream>>>(ndof, d.x32, d.x64, d.cg);
+  k_mx_fold<<<GV, 256, 0, h->stream>>>(ndof, d.x32, d.x32lo, d.x64, d.cg);
   LPM_LAUNCHED(h, "k_mx_fold");
   LPM_CUDA(h, cudaMemcpyAsync(d.disp, d.x64, sizeof(double) * ndof, cudaMemcpyDeviceToDevice, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));

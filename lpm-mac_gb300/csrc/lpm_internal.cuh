@@ -57,6 +57,7 @@ struct CgScalars {
   unsigned long long bmax_bits;  // mixed solve: bits of max |b| (non-negative doubles order as integers)
   double bscale;      // mixed solve: power of two that brings max |b| to [1, 2)
   float alpha32, beta32, zcoef32;  // mixed solve: FP32 copies, so that the vector kernels convert nothing
+  float alpha32lo, beta32lo;       // mixed solve: alpha - alpha32 and beta - beta32 rounded (double-float pairs)
 };
 
 // Deterministic grid reductions: each block writes a partial, the last block
@@ -123,6 +124,9 @@ struct Dev {
   // solver vectors (n_dof each)
   double *rhs, *disp, *x64, *r64, *p64, *q64, *invd64;
   float *b32, *x32, *r32, *p32, *q32, *invd32;
+  // mixed solve: low words of the residual, the product and the solution
+  // increment (each a double-float pair with the FP32 vector above)
+  float *r32lo, *q32lo, *x32lo;
   // reductions
   RedBuf red;
   CgScalars* cg;   // device scalars
