@@ -67,6 +67,7 @@ def parse_args(argv=None):
     p.add_argument("--cg-tol", type=float, default=1e-10)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-matrix-free", action="store_true")
     p.add_argument("--softening", action="store_true",
                    help="also time configuration 3 at full size (several minutes: its crack bursts in the timed steps)")
     return p.parse_args(argv)
@@ -179,12 +180,13 @@ def aggregate(elapsed_s, steps, world):
 
 
 # --------------------------------------------------------------- GPU arm
-def gpu_run(w, args, precision, world, local):
+def gpu_run(w, args, precision, world, local, operator=0):
     import torch
     import __graft_entry__ as ge
     capi = ge.load_package().capi
     g = capi.Lattice(3, w["xyz"], w["p1"], w["p2"], w["layer"], w["Kn"], w["Tv"], w["cell"].particle_volume,
                      w["cell"].nneighbors)
+    g.set_operator(operator)
     gb, gt = g.add_group(w["bottom"]), g.add_group(w["top"])
     bcs = [("disp", gb, 0, 0.0), ("disp", gb, 1, 0.0), ("disp", gb, 2, 0.0), ("disp", gt, 2, args.du)]
     opts = dict(tangent=capi.TANGENT_SYMMETRIC, precision=precision, max_iter=30, tol=1e-5, cg_tol=args.cg_tol)
@@ -520,6 +522,18 @@ def spmv_bytes(nblk, n, dim, value_bytes, index_bytes=4, row_sums=False, out_byt
     return b + (n * dim * dim * 4 if row_sums else 0)
 
 
+def mf_bytes(nb, n, dim=3, value_bytes=4, out_bytes=8):
+    """Algorithmic bytes of one matrix-free product (two passes): per
+    directed bond the partner word, the opposite bond's cosines and t' read
+    in pass 1 and again with a' - t' in pass 2; per particle the row sums,
+    S, U, V of both layers, the first pass's two sums per layer written and
+    read, the input read by both passes, the output written and the
+    eliminated-DOF flags read twice."""
+    per_bond = 2 * 4 + (2 * dim + 3) * value_bytes
+    per_particle = (dim * dim + 3 * 6 + 2 * 4) * value_bytes + 2 * dim * value_bytes + dim * out_bytes + 2 * dim
+    return nb * per_bond + n * per_particle
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -744,6 +758,22 @@ def run_gb300(args):
                         "spmv_fp64_gflops": 2 * nblk * 9 / (avg64 * 1e-3) / 1e9,
                         "mixed_speedup": value / fv}
         f["handle"].close()
+    if not args.no_matrix_free:
+        mf = gpu_run(w, args, capi.PREC_MIXED, world, local, operator=capi.OPERATOR_MATRIX_FREE)
+        mv, tm = aggregate(mf["ms"] / 1e3, args.steps, world)
+        kt = mf["ktime"]
+        mavg = kt["spmv32_ms"] / max(kt["spmv32_launches"], 1)
+        mb = mf_bytes(nb, n)
+        line["matrix_free"] = {"value": mv, "ms_per_step": tm * 1e3 / args.steps,
+                               "cg_iters_per_step": statistics.mean(mf["cg"]),
+                               "newton_iters_per_step": statistics.mean(mf["newton"]),
+                               "product_avg_launch_ms": mavg, "product_algorithmic_bytes": mb,
+                               "product_achieved_gbs": mb / (mavg * 1e-3) / 1e9,
+                               "product_frac": mb / (mavg * 1e-3) / 1e9 / peak,
+                               "speedup_vs_assembled": mv / value,
+                               "operator": "tangent applied from bond data in two passes (lpm_set_operator), "
+                                           "mixed precision, no assembly"}
+        mf["handle"].close()
     adj = adjoint_cost(g, capi, w, args.cg_tol, local)
     line["adjoint"] = dict(adj, relative_to_forward_step=adj["ms"] / (t_mixed * 1e3 / args.steps))
     fa = force_assembly_rate(g, capi, 5, local)

@@ -77,6 +77,9 @@ typedef struct lpm_handle lpm_handle;
 /* linear-solver precision */
 #define LPM_PREC_FP64 0  /* Jacobi CG in FP64, the Eigen algorithm (solver.h:192-217)       */
 #define LPM_PREC_MIXED 1 /* FP32 Jacobi CG inside FP64 iterative refinement                 */
+/* how the solves apply the tangent (lpm_set_operator) */
+#define LPM_OPERATOR_ASSEMBLED 0   /* assembled block operator, as calcStiffness builds K (default)   */
+#define LPM_OPERATOR_MATRIX_FREE 1 /* the same operator applied from bond data, never assembled       */
 
 /* Creates the device lattice.  Replaces Assembly's constructors
  * (assembly.h:83-106), Assembly::createBonds / readBond (bond lists are given
@@ -191,8 +194,24 @@ int lpm_residual(lpm_handle* h, double* norm_residual, double* norm_reaction);
  * Builds the FP64 tangent and, when mixed precision is requested later, its
  * FP32 copy. */
 int lpm_assemble(lpm_handle* h, int tangent, int bc);
-/* BSR values of K (not transposed) in pattern order, dim*dim row-major. */
+/* BSR values of K (not transposed) in pattern order, dim*dim row-major.
+ * LPM_ERR_STATE under the matrix-free operator (nothing is assembled). */
 int lpm_get_K(const lpm_handle* h, double* vals);
+/* Chooses how lpm_assemble and the solves treat the tangent.  No counterpart
+ * in the reference, which always assembles (stiffness.h:228-263).  With
+ * LPM_OPERATOR_MATRIX_FREE, lpm_assemble keeps the bond data the tangent is
+ * made of (direction cosines, bond constants, damage, per-particle sums)
+ * and each CG product applies A = K^T from it in two passes over the bonds;
+ * the solves give the assembled operator's results up to rounding, for
+ * both tangent variants and BC modes, at less than half the bytes per
+ * product.  The operator must be assembled again after the switch. */
+int lpm_set_operator(lpm_handle* h, int kind);
+/* y = A' v: one product of the operator the solves use (A = K^T of the last
+ * lpm_assemble, BC-eliminated when asked, assembled or matrix-free), in
+ * FP64 or (LPM_PREC_MIXED) as the FP32 product of the mixed solve, whose
+ * double-float result is returned summed in FP64.  v, y: host arrays of
+ * n*dim.  No counterpart in the reference (Eigen applies it inside CG). */
+int lpm_apply_operator(lpm_handle* h, int precision, const double* v, double* y);
 
 /* Solver::LPM_CG (solver.h:192-217): solves with the residual as right-hand
  * side into Solver::disp.  FP64: Eigen's ConjugateGradient with its Jacobi

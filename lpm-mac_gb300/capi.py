@@ -25,6 +25,7 @@ BC_DISP, BC_FORCE = 0, 1
 SOLVER_STATIC, SOLVER_FATIGUE_STATIC, SOLVER_STATIC_ELIMINATE = 0, 1, 2
 LAW_ELASTIC, LAW_DAMAGE, LAW_J2, LAW_FATIGUE_HCF, LAW_SOFTENING = 0, 1, 2, 3, 4
 T_PIN, T_XYZ = 1, 2  # tangent fields (lpm_tangent_get)
+OPERATOR_ASSEMBLED, OPERATOR_MATRIX_FREE = 0, 1
 _NSTATE = {LAW_ELASTIC: 1, LAW_DAMAGE: 1, LAW_J2: 7, LAW_FATIGUE_HCF: 3, LAW_SOFTENING: 1}
 
 
@@ -116,6 +117,8 @@ def load(build_if_needed=True):
         "lpm_residual": [H, dp, dp],
         "lpm_assemble": [H, ctypes.c_int, ctypes.c_int],
         "lpm_get_K": [H, dp],
+        "lpm_set_operator": [H, ctypes.c_int],
+        "lpm_apply_operator": [H, ctypes.c_int, dp, dp],
         "lpm_solve": [H, ctypes.c_int, ctypes.c_double, i64, i64p, dp],
         "lpm_move_by_disp": [H],
         "lpm_newton": [H, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, i64, ip],
@@ -157,7 +160,8 @@ def exported_symbols():
             "lpm_get_bonds", "lpm_upload", "lpm_download", "lpm_set_mask", "lpm_get_mask", "lpm_set_law",
             "lpm_update_damage", "lpm_set_types", "lpm_set_nonlocal", "lpm_update_state", "lpm_fatigue_damage",
             "lpm_add_group", "lpm_apply_disp_bc", "lpm_apply_force_bc",
-            "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_solve",
+            "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_set_operator",
+            "lpm_apply_operator", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
             "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
             "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
@@ -370,6 +374,17 @@ class Lattice:
 
     def assemble(self, tangent=TANGENT_SYMMETRIC, bc=BC_ELIMINATE):
         self._check(self._L.lpm_assemble(self.h, int(tangent), int(bc)))
+
+    def set_operator(self, kind):
+        """OPERATOR_ASSEMBLED (default) or OPERATOR_MATRIX_FREE; assemble again after a switch."""
+        self._check(self._L.lpm_set_operator(self.h, int(kind)))
+
+    def apply_operator(self, v, precision=PREC_FP64):
+        """A' v with the operator the solves use (n*dim vectors)."""
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(self.ndof)
+        y = np.zeros(self.ndof)
+        self._check(self._L.lpm_apply_operator(self.h, int(precision), _d(v), _d(y)))
+        return y
 
     def K_bsr(self):
         v = np.zeros(self.nblk * self.dim * self.dim)

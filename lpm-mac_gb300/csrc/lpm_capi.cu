@@ -488,9 +488,25 @@ int lpm_assemble(lpm_handle* h, int tangent, int bc) {
   return LPM_OK;
 }
 
+int lpm_set_operator(lpm_handle* h, int kind) {
+  if (!h) return LPM_ERR_ARG;
+  if (kind != LPM_OPERATOR_ASSEMBLED && kind != LPM_OPERATOR_MATRIX_FREE) return arg_error(h, "unknown operator kind");
+  const bool mf = kind == LPM_OPERATOR_MATRIX_FREE;
+  if (mf != h->mf) {
+    h->mf = mf;
+    h->have_K = false;
+    h->a32_valid = false;
+  }
+  return LPM_OK;
+}
+
 int lpm_get_K(const lpm_handle* h, double* vals) {
   if (!h || !vals) return LPM_ERR_ARG;
   lpm_handle* hh = const_cast<lpm_handle*>(h);
+  if (h->mf) {
+    hh->err = "matrix-free operator: the tangent is not assembled";
+    return LPM_ERR_STATE;
+  }
   if (!h->have_K) {
     hh->err = "no tangent assembled";
     return LPM_ERR_STATE;
@@ -546,6 +562,16 @@ int lpm_solve(lpm_handle* h, int precision, double tol, int64_t maxit, int64_t* 
   if (iters) *iters = it;
   if (relres) *relres = rr;
   return st;
+}
+
+int lpm_apply_operator(lpm_handle* h, int precision, const double* v, double* y) {
+  if (!h || !v || !y) return arg_error(h, "NULL handle or buffer");
+  if (precision != LPM_PREC_FP64 && precision != LPM_PREC_MIXED) return arg_error(h, "bad precision");
+  if (!h->have_K) {
+    h->err = "lpm_apply_operator before lpm_assemble";
+    return LPM_ERR_STATE;
+  }
+  return apply_operator(h, precision, v, y);
 }
 
 int lpm_move_by_disp(lpm_handle* h) {

@@ -45,9 +45,12 @@
 #include <cfloat>
 #include <cmath>
 #include <tuple>
+#include <vector>
 
 #include "lpm_cgvec.cuh"
 #include "lpm_device.cuh"
+#include "lpm_df.cuh"
+#include "lpm_graph.cuh"
 
 namespace lpm {
 namespace {
@@ -79,99 +82,6 @@ __device__ __forceinline__ int4 group_cols(const SellView& v, int row, int64_t s
 __device__ __forceinline__ int comp(const int4& v, int t) { return t == 0 ? v.x : t == 1 ? v.y : t == 2 ? v.z : v.w; }
 __device__ __forceinline__ float comp(const float4& v, int t) {
   return t == 0 ? v.x : t == 1 ? v.y : t == 2 ? v.z : v.w;
-}
-
-// s + c += a*b with the rounding errors of the product and of the sum kept
-// in c (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
-// Comput. 26 (2005): TwoProduct by FMA, TwoSum).  The _rn intrinsics keep the
-// compiler from contracting the steps into other FMAs.
-__device__ __forceinline__ void dot2_acc(float& s, float& c, float a, float b) {
-  const float p = __fmul_rn(a, b);
-  const float pe = fmaf(a, b, -p);
-  const float t = __fadd_rn(s, p);
-  const float z = __fsub_rn(t, s);
-  const float se = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
-  s = t;
-  c = __fadd_rn(c, __fadd_rn(pe, se));
-}
-
-// (s, c) += (x, xc) for double-float pairs: TwoSum of the leading parts,
-// the rounding error and the trailing parts kept in c.
-__device__ __forceinline__ void df_add(float& s, float& c, float x, float xc) {
-  const float t = __fadd_rn(s, x);
-  const float z = __fsub_rn(t, s);
-  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
-  s = t;
-  c = __fadd_rn(c, __fadd_rn(xc, e));
-}
-
-// Double-float vector arithmetic: a value held as an FP32 pair (hi, lo) with
-// |lo| at most half an ulp of hi (Dekker, "A floating-point technique for
-// extending the available precision", Numer. Math. 18 (1971)), built from
-// TwoSum and TwoProduct by FMA as in dot2_acc.
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  const float z = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
-}
-
-// (xh, xl) += (ah, al) * (bh, bl), normalised; the product's low-order cross
-// terms are kept, the (al, bl) term (below the pair's precision) is not.
-__device__ __forceinline__ void df_madd(float& xh, float& xl, float ah, float al, float bh, float bl) {
-  const float ph = __fmul_rn(ah, bh);
-  const float pl = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -ph)));
-  float sh, se;
-  two_sum(xh, ph, sh, se);
-  two_sum(sh, __fadd_rn(se, __fadd_rn(xl, pl)), xh, xl);
-}
-
-// A double rounded to a normalised FP32 pair.
-__device__ __forceinline__ void df_split(double v, float& h, float& l) {
-  h = (float)v;
-  l = (float)(v - (double)h);
-}
-
-// Block sum of per-thread double-float partials, result in thread 0 as
-// FP64.  Both the warp and the cross-warp stage stay in FP32 pairs: GB300's
-// FP64 pipe takes a whole warp slot even for a one-lane instruction, so an
-// FP64 step per warp over a grid of thousands of warps costs microseconds.
-// One conversion per block remains.
-template <int K>
-__device__ __forceinline__ void block_df_sum(float (&s)[K], float (&c)[K], double (&out)[K]) {
-  __shared__ float sm[K][2][32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const float so = __shfl_xor_sync(0xffffffffu, s[k], o), co = __shfl_xor_sync(0xffffffffu, c[k], o);
-      df_add(s[k], c[k], so, co);
-    }
-  __syncthreads();
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      sm[k][0][warp] = s[k];
-      sm[k][1][warp] = c[k];
-    }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      s[k] = lane < nw ? sm[k][0][lane] : 0.f;
-      c[k] = lane < nw ? sm[k][1][lane] : 0.f;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        const float so = __shfl_xor_sync(0xffffffffu, s[k], o), co = __shfl_xor_sync(0xffffffffu, c[k], o);
-        df_add(s[k], c[k], so, co);
-      }
-    if (lane == 0)
-#pragma unroll
-      for (int k = 0; k < K; ++k) out[k] = (double)s[k] + (double)c[k];
-  }
 }
 
 // Four values of the FP32 operator.  An operator that fits in L2 with room
@@ -693,7 +603,7 @@ int run_cg(lpm_handle* h, const T* A, const T* b, T* x, T* r, T* p, T* q, const 
   const bool timing = h->timing;
   if constexpr (sizeof(T) == 8) {
     if (!timing) {  // the whole iteration loop as one graph launch
-      if (!h->fp_exec || h->fp_graph_x != (const void*)x) {
+      if (!h->fp_exec || h->fp_graph_x != (const void*)x || h->fp_graph_mf != h->mf) {
         const int st = build_fp64_graph(h, A, b, x, r, p, q, invd, GV, GR, sv);
         if (st) return st;
       }
@@ -716,11 +626,16 @@ int run_cg(lpm_handle* h, const T* A, const T* b, T* x, T* r, T* p, T* q, const 
         e1 = next_event(h);
         if (e0) cudaEventRecord(e0, h->stream);
       }
-      if (dim == 3)
-        k_cg_spmv<T, 3><<<GR, 256, 0, h->stream>>>(sv, A, p, q, d.cg, d.red.partials, d.red.ticket + 3, nullptr);
-      else
-        k_cg_spmv<T, 2><<<GR, 256, 0, h->stream>>>(sv, A, p, q, d.cg, d.red.partials, d.red.ticket + 3, nullptr);
-      LPM_LAUNCHED(h, "k_cg_spmv");
+      if (h->mf) {
+        const int st = mf_launch_product(h, sizeof(T) == 4, p, q, nullptr);
+        if (st) return st;
+      } else {
+        if (dim == 3)
+          k_cg_spmv<T, 3><<<GR, 256, 0, h->stream>>>(sv, A, p, q, d.cg, d.red.partials, d.red.ticket + 3, nullptr);
+        else
+          k_cg_spmv<T, 2><<<GR, 256, 0, h->stream>>>(sv, A, p, q, d.cg, d.red.partials, d.red.ticket + 3, nullptr);
+        LPM_LAUNCHED(h, "k_cg_spmv");
+      }
       if (timing && e1) cudaEventRecord(e1, h->stream);
       k_cg_update<T><<<GV, 256, 0, h->stream>>>(ndof, x, r, p, q, invd, d.cg, d.red.partials, d.red.ticket + 4);
       LPM_LAUNCHED(h, "k_cg_update");
@@ -758,6 +673,7 @@ int run_cg(lpm_handle* h, const T* A, const T* b, T* x, T* r, T* p, T* q, const 
 
 // Jacobi preconditioner of the assembled operator (FP64, and FP32 on request).
 int prepare_invd(lpm_handle* h, bool want32) {
+  if (h->mf) return mf_prepare_invd(h, want32);
   Dev& d = h->d;
   if (h->dim == 3)
     k_invd<3><<<grid_for(h->n, 256), 256, 0, h->stream>>>(h->n, d.diag_slot, d.A64, h->nslots, d.invd64,
@@ -772,7 +688,7 @@ int prepare_invd(lpm_handle* h, bool want32) {
 
 int solve_fp64(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres) {
   Dev& d = h->d;
-  if (!d.A64 || !d.rhs || !d.disp || !d.r64 || !d.p64 || !d.q64 || !d.invd64 || !d.diag_slot) {
+  if ((!h->mf && (!d.A64 || !d.diag_slot)) || !d.rhs || !d.disp || !d.r64 || !d.p64 || !d.q64 || !d.invd64) {
     h->err = "FP64 solve: work buffers missing";
     return LPM_ERR_STATE;
   }
@@ -830,35 +746,13 @@ int vector_grid(lpm_handle* h, K kernel, long long ndof) {
 
 int mixed_grids(lpm_handle* h, const SellView& sv, MixedGrids* mg) {
   const long long n = h->n, ndof = n * h->dim;
-  mg->spmv = resident_grid(h, spmv32_fn(h, sv), n);
+  mg->spmv = h->mf ? 0 : resident_grid(h, spmv32_fn(h, sv), n);
   mg->residual = fp64_row_grid(h);
   mg->update = vector_grid(h, k_mx_update, ndof);
   mg->replace = vector_grid(h, k_mx_replace, ndof);
   mg->pupdate = vector_grid(h, k_mx_pupdate, ndof);
   return LPM_OK;
 }
-
-// A kernel node of a graph: the arguments are converted to the kernel's
-// parameter types and passed by address, as cudaGraphAddKernelNode wants.
-template <typename... P, typename... A>
-cudaError_t add_kernel(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* dep, void (*fn)(P...), int grid,
-                       int block, A... a) {
-  std::tuple<P...> vals(a...);
-  void* params[sizeof...(P) > 0 ? sizeof...(P) : 1];
-  std::apply([&](auto&... x) {
-    int i = 0;
-    ((params[i++] = (void*)&x), ...);
-  }, vals);
-  cudaKernelNodeParams kp = {};
-  kp.func = (void*)fn;
-  kp.gridDim = dim3((unsigned)grid);
-  kp.blockDim = dim3((unsigned)block);
-  kp.sharedMemBytes = 0;
-  kp.kernelParams = params;
-  return cudaGraphAddKernelNode(node, g, dep, dep ? 1 : 0, &kp);
-}
-
-
 
 // The mixed solve's iteration loop as one graph:
 //   while (loop_cond) { spmv; update; if (ru_cond) { residual; replace } pupdate }
@@ -889,9 +783,14 @@ int build_mixed_graph(lpm_handle* h, const SellView& sv, const MixedGrids& mg) {
   LPM_CUDA(h, cudaGraphConditionalHandleCreate(&ru_cond, body, 0u, cudaGraphCondAssignDefault));
   cudaGraphNode_t n_spmv, n_upd, n_if, n_res, n_rep, n_pup;
   cudaError_t e;
-  const Spmv32Fn spmv = spmv32_fn(h, sv);
-  LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, spmv, mg.spmv, 256, sv, (const float*)d.A32, (const float*)d.p32,
-                         d.q32, d.cg, d.red.partials, d.red.ticket + 3, d.q32lo));
+  const Spmv32Fn spmv = h->mf ? nullptr : spmv32_fn(h, sv);
+  if (h->mf) {
+    const int st = mf_graph_product(h, body, nullptr, true, d.p32, d.q32, d.q32lo, &n_spmv);
+    if (st) return st;
+  } else {
+    LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, spmv, mg.spmv, 256, sv, (const float*)d.A32, (const float*)d.p32,
+                           d.q32, d.cg, d.red.partials, d.red.ticket + 3, d.q32lo));
+  }
   LPM_CUDA(h, add_kernel(&n_upd, body, &n_spmv, k_mx_update, mg.update, 256, ndof, d.x32, d.x32lo, d.r32, d.r32lo,
                          (const float*)d.p32, (const float*)d.q32, (const float*)d.q32lo, (const float*)d.invd32,
                          d.cg, d.red.partials, d.red.ticket + 4, ru_cond));
@@ -902,7 +801,11 @@ int build_mixed_graph(lpm_handle* h, const SellView& sv, const MixedGrids& mg) {
   ip.conditional.size = 1;
   LPM_CUDA(h, cudaGraphAddNode(&n_if, body, &n_upd, nullptr, 1, &ip));
   cudaGraph_t ifb = ip.conditional.phGraph_out[0];
-  if (dim == 3)
+  if (h->mf) {
+    const int st = mf_graph_residual(h, ifb, nullptr, &n_res);
+    if (st) return st;
+    e = cudaSuccess;
+  } else if (dim == 3)
     e = add_kernel(&n_res, ifb, nullptr, k_mx_residual<3>, mg.residual, 256, sv, (const double*)d.A64, (const double*)d.x64,
                    (const float*)d.x32, (const float*)d.x32lo, (const double*)d.rhs, d.r64, d.cg, d.red.partials,
                    d.red.ticket + 6);
@@ -918,6 +821,7 @@ int build_mixed_graph(lpm_handle* h, const SellView& sv, const MixedGrids& mg) {
                          (const float*)d.invd32, d.p32, d.cg, loop_cond));
   LPM_CUDA(h, cudaGraphInstantiate(&h->mx_exec, g, 0));
   h->mx_graph_spmv = (const void*)spmv;
+  h->mx_graph_mf = h->mf;
   return LPM_OK;
 }
 
@@ -947,41 +851,119 @@ int build_fp64_graph(lpm_handle* h, const double* A, const double* b, double* x,
   cudaGraphNode_t wnode, n_spmv, n_upd, n_pup;
   LPM_CUDA(h, cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
   cudaGraph_t body = wp.conditional.phGraph_out[0];
-  if (h->dim == 3)
+  if (h->mf) {
+    const int st = mf_graph_product(h, body, nullptr, false, p, q, nullptr, &n_spmv);
+    if (st) return st;
+  } else if (h->dim == 3) {
     LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, k_cg_spmv<double, 3>, GR, 256, sv, A, (const double*)p, q, d.cg,
                            d.red.partials, d.red.ticket + 3, (float*)nullptr));
-  else
+  } else {
     LPM_CUDA(h, add_kernel(&n_spmv, body, nullptr, k_cg_spmv<double, 2>, GR, 256, sv, A, (const double*)p, q, d.cg,
                            d.red.partials, d.red.ticket + 3, (float*)nullptr));
+  }
   LPM_CUDA(h, add_kernel(&n_upd, body, &n_spmv, k_cg_update<double>, GV, 256, ndof, x, r, (const double*)p,
                          (const double*)q, invd, d.cg, d.red.partials, d.red.ticket + 4));
   LPM_CUDA(h, add_kernel(&n_pup, body, &n_upd, k_cg_pupdate<double>, GV, 256, ndof, (const double*)r, invd, p, d.cg,
                          loop_cond));
   LPM_CUDA(h, cudaGraphInstantiate(&h->fp_exec, g, 0));
   h->fp_graph_x = x;
+  h->fp_graph_mf = h->mf;
   return LPM_OK;
 }
 
 }  // namespace
 
-int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres) {
+namespace {
+
+// FP32 work vectors, allocated on the first mixed solve (or product).
+int mixed_buffers(lpm_handle* h) {
   Dev& d = h->d;
-  const int dim = h->dim;
-  const int64_t ndof = (int64_t)h->n * dim;
-  if (maxit < 0) maxit = 2LL * ndof;
-  if (!d.b32) {  // FP32 work vectors, allocated on the first mixed solve
+  const int64_t ndof = (int64_t)h->n * h->dim;
+  if (!d.b32) {
     float** vecs[9] = {&d.b32, &d.x32, &d.r32, &d.p32, &d.q32, &d.invd32, &d.r32lo, &d.q32lo, &d.x32lo};
     for (float** v : vecs) {
       *v = (float*)dev_alloc(h, sizeof(float) * (size_t)ndof);
       if (!*v) return LPM_ERR_NOMEM;
     }
   }
-  if (!h->a32_valid) {
+  return LPM_OK;
+}
+
+}  // namespace
+
+// y = A' v with the operator the solves use (assembled or matrix-free), in
+// FP64 or as the FP32 product of the mixed solve (its double-float output
+// summed in FP64).  v and y are host vectors of n*dim.
+int apply_operator(lpm_handle* h, int precision, const double* v, double* y) {
+  Dev& d = h->d;
+  const int dim = h->dim;
+  const int64_t ndof = (int64_t)h->n * dim;
+  LPM_CUDA(h, cudaMemsetAsync(d.cg, 0, sizeof(CgScalars), h->stream));
+  if (precision == LPM_PREC_FP64) {
+    const SellView sv = sell_view(h);
+    LPM_CUDA(h, cudaMemcpyAsync(d.p64, v, sizeof(double) * ndof, cudaMemcpyHostToDevice, h->stream));
+    if (h->mf) {
+      const int st = mf_launch_product(h, false, d.p64, d.q64, nullptr);
+      if (st) return st;
+    } else {
+      const int GR = fp64_row_grid(h);
+      if (dim == 3)
+        k_cg_spmv<double, 3><<<GR, 256, 0, h->stream>>>(sv, d.A64, d.p64, d.q64, d.cg, d.red.partials,
+                                                        d.red.ticket + 3, nullptr);
+      else
+        k_cg_spmv<double, 2><<<GR, 256, 0, h->stream>>>(sv, d.A64, d.p64, d.q64, d.cg, d.red.partials,
+                                                        d.red.ticket + 3, nullptr);
+      LPM_LAUNCHED(h, "k_cg_spmv");
+    }
+    LPM_CUDA(h, cudaMemcpyAsync(y, d.q64, sizeof(double) * ndof, cudaMemcpyDeviceToHost, h->stream));
+    LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return LPM_OK;
+  }
+  int st = mixed_buffers(h);
+  if (st) return st;
+  if (!h->mf && !h->a32_valid) {
+    st = convert_A32(h);
+    if (st) return st;
+  }
+  // the view after the conversion: it carries the row sums and column
+  // offsets that convert_A32 creates on the first FP32 use
+  const SellView sv = sell_view(h);
+  std::vector<float> v32((size_t)ndof), hi((size_t)ndof), lo((size_t)ndof);
+  for (int64_t q = 0; q < ndof; ++q) v32[(size_t)q] = (float)v[q];
+  LPM_CUDA(h, cudaMemcpyAsync(d.p32, v32.data(), sizeof(float) * ndof, cudaMemcpyHostToDevice, h->stream));
+  if (h->mf) {
+    st = mf_launch_product(h, true, d.p32, d.q32, d.q32lo);
+    if (st) return st;
+  } else {
+    MixedGrids mg;
+    st = mixed_grids(h, sv, &mg);
+    if (st) return st;
+    spmv32_fn(h, sv)<<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials, d.red.ticket + 3,
+                                                     d.q32lo);
+    LPM_LAUNCHED(h, "k_cg_spmv");
+  }
+  LPM_CUDA(h, cudaMemcpyAsync(hi.data(), d.q32, sizeof(float) * ndof, cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(lo.data(), d.q32lo, sizeof(float) * ndof, cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (int64_t q = 0; q < ndof; ++q) y[q] = (double)hi[(size_t)q] + (double)lo[(size_t)q];
+  return LPM_OK;
+}
+
+int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres) {
+  Dev& d = h->d;
+  const int dim = h->dim;
+  const int64_t ndof = (int64_t)h->n * dim;
+  if (maxit < 0) maxit = 2LL * ndof;
+  {
+    const int st0 = mixed_buffers(h);
+    if (st0) return st0;
+  }
+  if (!h->mf && !h->a32_valid) {
     const int st0 = convert_A32(h);
     if (st0) return st0;
   }
-  if (!d.A32 || !d.S32 || !d.x32 || !d.r32 || !d.p32 || !d.q32 || !d.invd32 || !d.r32lo || !d.q32lo || !d.x32lo ||
-      !d.x64 || !d.r64 || !d.rhs || !d.disp) {
+  if ((!h->mf && (!d.A32 || !d.S32)) || !d.x32 || !d.r32 || !d.p32 || !d.q32 || !d.invd32 || !d.r32lo || !d.q32lo ||
+      !d.x32lo || !d.x64 || !d.r64 || !d.rhs || !d.disp) {
     h->err = "mixed solve: work buffers missing";
     return LPM_ERR_STATE;
   }
@@ -1003,7 +985,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   const size_t ev0 = h->ev_used;
   if (!timing) {
     // the whole iteration loop as one graph launch
-    if (!h->mx_exec || h->mx_graph_spmv != (const void*)spmv32_fn(h, sv)) {
+    if (!h->mx_exec || h->mx_graph_mf != h->mf || (!h->mf && h->mx_graph_spmv != (const void*)spmv32_fn(h, sv))) {
       st = build_mixed_graph(h, sv, mg);
       if (st) return st;
     }
@@ -1022,19 +1004,30 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
         e1 = next_event(h);
         if (e0) cudaEventRecord(e0, h->stream);
       }
-      spmv32<<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials, d.red.ticket + 3, d.q32lo);
-      LPM_LAUNCHED(h, "k_cg_spmv");
+      if (h->mf) {
+        st = mf_launch_product(h, true, d.p32, d.q32, d.q32lo);
+        if (st) return st;
+      } else {
+        spmv32<<<mg.spmv, 256, 0, h->stream>>>(sv, d.A32, d.p32, d.q32, d.cg, d.red.partials, d.red.ticket + 3,
+                                               d.q32lo);
+        LPM_LAUNCHED(h, "k_cg_spmv");
+      }
       if (timing && e1) cudaEventRecord(e1, h->stream);
       k_mx_update<<<mg.update, 256, 0, h->stream>>>(ndof, d.x32, d.x32lo, d.r32, d.r32lo, d.p32, d.q32, d.q32lo, d.invd32,
                                                     d.cg, d.red.partials, d.red.ticket + 4, 0);
       LPM_LAUNCHED(h, "k_mx_update");
-      if (dim == 3)
-        k_mx_residual<3><<<mg.residual, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.x32lo, d.rhs, d.r64, d.cg,
-                                                             d.red.partials, d.red.ticket + 6);
-      else
-        k_mx_residual<2><<<mg.residual, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.x32lo, d.rhs, d.r64, d.cg,
-                                                             d.red.partials, d.red.ticket + 6);
-      LPM_LAUNCHED(h, "k_mx_residual");
+      if (h->mf) {
+        st = mf_launch_residual(h);
+        if (st) return st;
+      } else {
+        if (dim == 3)
+          k_mx_residual<3><<<mg.residual, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.x32lo, d.rhs, d.r64, d.cg,
+                                                               d.red.partials, d.red.ticket + 6);
+        else
+          k_mx_residual<2><<<mg.residual, 256, 0, h->stream>>>(sv, d.A64, d.x64, d.x32, d.x32lo, d.rhs, d.r64, d.cg,
+                                                               d.red.partials, d.red.ticket + 6);
+        LPM_LAUNCHED(h, "k_mx_residual");
+      }
       k_mx_replace<<<mg.replace, 256, 0, h->stream>>>(ndof, d.r64, d.r32, d.r32lo, d.x32, d.x32lo, d.x64, d.p32, d.invd32,
                                                       d.cg, d.red.partials, d.red.ticket + 7);
       LPM_LAUNCHED(h, "k_mx_replace");

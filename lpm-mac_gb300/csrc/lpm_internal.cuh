@@ -127,6 +127,18 @@ struct Dev {
   // mixed solve: low words of the residual, the product and the solution
   // increment (each a double-float pair with the FP32 vector above)
   float *r32lo, *q32lo, *x32lo;
+  // matrix-free operator (lpm_set_operator): the bonds in slices of 32
+  // particles (bond k of particle i at slot mbase[i/32] + 32 k + i%32), each
+  // slot holding its partner (layer in the top bit) and, in FP64 and FP32,
+  // the opposite bond's direction cosines, a' - t' and t' (t = w Tv,
+  // a = w (2 Kn + Tv)) as five arrays of mslots; per particle and layer the
+  // direction-cosine sums S and the sums U = S + sum n', V = T + sum t' n'
+  // ([n][2][3]); per particle the block row sums of A ([n][9]); the
+  // diagonal of K per DOF; the first pass's two sums per particle and layer
+  int64_t* mbase;
+  unsigned* mp2;
+  double *m64, *mS64, *mU64, *mV64, *mR64, *mdiag, *mHF64;
+  float *m32, *mS32, *mU32, *mV32, *mR32, *mHF32;
   // reductions
   RedBuf red;
   CgScalars* cg;   // device scalars
@@ -189,6 +201,9 @@ struct lpm_handle {
   bool soff16_ok = false;  // every column offset of the pattern fits 16 bits
   int sms = 0;             // multiprocessors of the device (looked up on the first mixed solve)
   int tangent = LPM_TANGENT_AS_WRITTEN;
+  bool mf = false;        // the CG applies the tangent matrix-free (lpm_set_operator)
+  int64_t mslots = 0;     // slots of the matrix-free bond layout
+  int mnsl = 0;           // 32-particle slices of that layout
   // host mirrors
   lpm::CgScalars* h_cg = nullptr;  // pinned
   double* h_norms = nullptr;       // pinned [8]
@@ -211,6 +226,7 @@ struct lpm_handle {
   cudaGraph_t mx_graph = nullptr;
   cudaGraphExec_t mx_exec = nullptr;
   const void* mx_graph_spmv = nullptr;  // the FP32 product kernel the graph launches
+  bool fp_graph_mf = false, mx_graph_mf = false;  // the operator form each graph was built for
 };
 
 namespace lpm {
@@ -230,10 +246,22 @@ int launch_fatigue_damage(lpm_handle* h, double dt, int* any_new);
 int build_pattern(lpm_handle* h);
 int launch_assemble(lpm_handle* h, int tangent, int bc);
 int convert_A32(lpm_handle* h);
+// matrix-free operator (lpm_mfree.cu): the per-assembly data, the Jacobi
+// diagonal, the product q = A p with p.q and alpha (FP32 with q as a
+// double-float pair, or FP64), and the mixed solve's FP64 true residual,
+// launched on the handle's stream or appended to a graph after `dep`
+int mf_assemble(lpm_handle* h, int tangent, int bc);
+int mf_prepare_invd(lpm_handle* h, bool want32);
+int mf_launch_product(lpm_handle* h, bool fp32, const void* p, void* q, float* qlo);
+int mf_launch_residual(lpm_handle* h);
+int mf_graph_product(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, bool fp32, const void* p, void* q,
+                     float* qlo, cudaGraphNode_t* last);
+int mf_graph_residual(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, cudaGraphNode_t* last);
 // solvers (lpm_cg.cu)
 int solve_fp64(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);
 int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);
 int prepare_invd(lpm_handle* h, bool want32);
+int apply_operator(lpm_handle* h, int precision, const double* v_host, double* y_host);
 // adjoint and checkpoints (lpm_adjoint.cu); vectors are device pointers
 int adjoint_buffers(lpm_handle* h);
 int adjoint_apply(lpm_handle* h, const double* v, double* y);

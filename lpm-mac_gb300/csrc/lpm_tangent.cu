@@ -422,6 +422,7 @@ int build_pattern(lpm_handle* h) {
 }
 
 int launch_assemble(lpm_handle* h, int tangent, int bc) {
+  if (h->mf) return mf_assemble(h, tangent, bc);
   Dev& d = h->d;
   const int dim = h->dim;
   const size_t vals = (size_t)h->nslots * dim * dim;

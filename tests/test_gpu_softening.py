@@ -19,13 +19,17 @@ def setup(ncol=21, nrow=31, a=0.1, seed=20261203):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("operator", [capi.OPERATOR_ASSEMBLED, capi.OPERATOR_MATRIX_FREE])
 @pytest.mark.parametrize("precision", [capi.PREC_FP64, capi.PREC_MIXED])
-def test_sent_softening_steps_match_oracle(precision):
+def test_sent_softening_steps_match_oracle(precision, operator):
+    """Both operator forms: the matrix-free one applies the same A = K^T,
+    whose partially damaged bonds make it non-symmetric."""
     args, sc = setup()
     xyz = args[1]
     n = len(xyz)
     o = make_oracle(*args)
     g = make_gpu(*args)
+    g.set_operator(operator)
     for s in (o, g):
         s.set_law(capi.LAW_SOFTENING, [3.0, 1.0e-3])
     o.set_bond(oracle.SCRIT, sc)
