@@ -903,7 +903,7 @@ int apply_operator(lpm_handle* h, int precision, const double* v, double* y) {
     const SellView sv = sell_view(h);
     LPM_CUDA(h, cudaMemcpyAsync(d.p64, v, sizeof(double) * ndof, cudaMemcpyHostToDevice, h->stream));
     if (h->mf) {
-      const int st = mf_launch_product(h, false, d.p64, d.q64, nullptr);
+      const int st = mf_launch_product(h, false, d.p64, d.q64, nullptr, true);
       if (st) return st;
     } else {
       const int GR = fp64_row_grid(h);
@@ -932,7 +932,7 @@ int apply_operator(lpm_handle* h, int precision, const double* v, double* y) {
   for (int64_t q = 0; q < ndof; ++q) v32[(size_t)q] = (float)v[q];
   LPM_CUDA(h, cudaMemcpyAsync(d.p32, v32.data(), sizeof(float) * ndof, cudaMemcpyHostToDevice, h->stream));
   if (h->mf) {
-    st = mf_launch_product(h, true, d.p32, d.q32, d.q32lo);
+    st = mf_launch_product(h, true, d.p32, d.q32, d.q32lo, true);
     if (st) return st;
   } else {
     MixedGrids mg;

@@ -252,7 +252,8 @@ int convert_A32(lpm_handle* h);
 // launched on the handle's stream or appended to a graph after `dep`
 int mf_assemble(lpm_handle* h, int tangent, int bc);
 int mf_prepare_invd(lpm_handle* h, bool want32);
-int mf_launch_product(lpm_handle* h, bool fp32, const void* p, void* q, float* qlo);
+// (mask: the input may be nonzero on eliminated DOFs; the solves' inputs are not)
+int mf_launch_product(lpm_handle* h, bool fp32, const void* p, void* q, float* qlo, bool mask = false);
 int mf_launch_residual(lpm_handle* h);
 int mf_graph_product(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, bool fp32, const void* p, void* q,
                      float* qlo, cudaGraphNode_t* last);

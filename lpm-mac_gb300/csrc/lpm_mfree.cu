@@ -50,7 +50,9 @@
 namespace lpm {
 namespace {
 
-constexpr unsigned kLayerBit = 1u << 31;
+constexpr unsigned kLayerBit = 1u << 31;  // slot word: the bond's layer
+constexpr unsigned kUVBit = 1u << 30;     // slot word: the partner's U, V (this layer) are not zero
+constexpr unsigned kIdMask = kUVBit - 1;  // slot word: the partner
 constexpr int kMfFields = 5;  // per slot: n'x, n'y, n'z, a' - t', t'
 
 // Slot partners: bond k of particle i at mbase[i/32] + 32 k + i%32 in
@@ -172,7 +174,7 @@ __global__ void k_mf_rowsum(int n, const int64_t* __restrict__ bptr, const int64
     for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b, ++k) {
       const int64_t slot = s0 + 32 * k;
       const unsigned w = mp2[slot];
-      const int j = (int)(w & ~kLayerBit), l = (w & kLayerBit) ? 1 : 0;
+      const int j = (int)(w & kIdMask), l = (w & kLayerBit) ? 1 : 0;
       const double np[3] = {m64[slot], m64[ns + slot], m64[2 * ns + slot]};
       const double c1 = m64[3 * ns + slot], tp = m64[4 * ns + slot];
       const double nb[3] = {cs[3 * b], cs[3 * b + 1], cs[3 * b + 2]};
@@ -237,8 +239,11 @@ struct MfView {
 };
 
 // The product's input: p (MODE 0), or the mixed solve's FP64 solution plus
-// its double-float increment x64 + (x32 + x32lo) (MODE 1); eliminated DOFs
-// read as zero unless `raw`.
+// its double-float increment x64 + (x32 + x32lo) (MODE 1).  With MASK the
+// eliminated DOFs read as zero (A' = P A P + nd (I - P)); inside the solves
+// the input is already zero there (the right-hand side, and so every
+// residual, direction and increment, vanishes on eliminated DOFs), so the
+// CG products skip the mask.
 template <typename T, int MODE>
 __device__ __forceinline__ T mf_in(const T* __restrict__ p, const float* __restrict__ a, const float* __restrict__ b,
                                    int64_t q) {
@@ -246,51 +251,81 @@ __device__ __forceinline__ T mf_in(const T* __restrict__ p, const float* __restr
   return p[q];
 }
 
-template <typename T, int DIM, int MODE>
+template <typename T, int DIM, int MODE, bool MASK>
 __device__ __forceinline__ void mf_load(const MfView<T>& v, const T* __restrict__ p, const float* __restrict__ a,
                                         const float* __restrict__ b, int i, T (&o)[3]) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     if (c < DIM) {
       const int64_t q = (int64_t)DIM * i + c;
-      o[c] = v.fixed[q] ? T(0) : mf_in<T, MODE>(p, a, b, q);
+      o[c] = (MASK && v.fixed[q]) ? T(0) : mf_in<T, MODE>(p, a, b, q);
     } else {
       o[c] = T(0);
     }
   }
 }
 
+// One slot's coefficients.
+template <typename T, int DIM>
+struct MfSlot {
+  T n[3], c1, tp;
+};
+
+template <typename T, int DIM>
+__device__ __forceinline__ void mf_slot(const MfView<T>& v, int64_t slot, MfSlot<T, DIM>& o) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) o.n[c] = c < DIM ? v.m[c * v.ns + slot] : T(0);
+  o.c1 = v.m[3 * v.ns + slot];
+  o.tp = v.m[4 * v.ns + slot];
+}
+
 // Pass 1: H_j = sum n'.(p_m - p_j), F_j = sum t' n'.(p_m - p_j) per layer
-// over j's bonds.  FP32 sums are compensated and rounded once.
-template <typename T, int DIM, int MODE>
+// over j's bonds.  FP32 sums are compensated and rounded once.  The loop is
+// software-pipelined: the next slot's coefficients and partner values, and
+// the partner word of the slot after it, are loaded while the current slot
+// is used.
+template <typename T, int DIM, int MODE, bool MASK>
 __global__ void __launch_bounds__(256) k_mf_pass1(MfView<T> v, const T* __restrict__ p, const float* __restrict__ xa,
                                                   const float* __restrict__ xb, const CgScalars* cg) {
   if (cg->done || (MODE == 1 && !cg->ru)) return;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < v.n; j += gridDim.x * blockDim.x) {
     T pj[3];
-    mf_load<T, DIM, MODE>(v, p, xa, xb, j, pj);
+    mf_load<T, DIM, MODE, MASK>(v, p, xa, xb, j, pj);
     const int sl = j / 32;
     const int64_t s0 = v.mbase[sl] + (j % 32);
     const int len = (int)((v.mbase[sl + 1] - v.mbase[sl]) / 32);
     T hs[NL] = {T(0), T(0)}, hc[NL] = {T(0), T(0)}, fs[NL] = {T(0), T(0)}, fc[NL] = {T(0), T(0)};
+    MfSlot<T, DIM> cur{}, nxt{};
+    T pc[3] = {T(0), T(0), T(0)}, pn[3] = {T(0), T(0), T(0)};
+    unsigned wc = 0, wn = 0, w2 = 0;
+    if (len > 0) {
+      wc = v.mp2[s0];
+      mf_slot<T, DIM>(v, s0, cur);
+      mf_load<T, DIM, MODE, MASK>(v, p, xa, xb, (int)(wc & kIdMask), pc);
+      if (len > 1) wn = v.mp2[s0 + 32];
+    }
     for (int k = 0; k < len; ++k) {
-      const int64_t slot = s0 + 32 * (int64_t)k;
-      const unsigned w = v.mp2[slot];
-      const int m = (int)(w & ~kLayerBit);
-      const int l = (w & kLayerBit) ? 1 : 0;
-      T pm[3];
-      mf_load<T, DIM, MODE>(v, p, xa, xb, m, pm);
-      T s = v.m[slot] * (pm[0] - pj[0]);
+      if (k + 1 < len) {
+        mf_slot<T, DIM>(v, s0 + 32 * (int64_t)(k + 1), nxt);
+        mf_load<T, DIM, MODE, MASK>(v, p, xa, xb, (int)(wn & kIdMask), pn);
+        if (k + 2 < len) w2 = v.mp2[s0 + 32 * (int64_t)(k + 2)];
+      }
+      const int l = (wc & kLayerBit) ? 1 : 0;
+      T s = cur.n[0] * (pc[0] - pj[0]);
 #pragma unroll
-      for (int c = 1; c < DIM; ++c) s = fma(v.m[c * v.ns + slot], pm[c] - pj[c], s);
-      const T tp = v.m[4 * v.ns + slot];
+      for (int c = 1; c < DIM; ++c) s = fma(cur.n[c], pc[c] - pj[c], s);
       if constexpr (sizeof(T) == 4) {
         df_add(hs[l], hc[l], s, 0.f);
-        dot2_acc(fs[l], fc[l], tp, s);
+        dot2_acc(fs[l], fc[l], cur.tp, s);
       } else {
         hs[l] += s;
-        fs[l] = fma(tp, s, fs[l]);
+        fs[l] = fma(cur.tp, s, fs[l]);
       }
+      cur = nxt;
+      wc = wn;
+      wn = w2;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) pc[c] = pn[c];
     }
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
@@ -304,18 +339,20 @@ __global__ void __launch_bounds__(256) k_mf_pass1(MfView<T> v, const T* __restri
 //   MODE 0: q = y (FP32: the pair q, qlo), p.q, and alpha in the last block;
 //   MODE 1: r = s b - y, |r|^2, and the reliable update's convergence test
 //           in the last block (as k_mx_residual).
-template <typename T, int DIM, int MODE>
+// Pipelined as pass 1; U and V of the partner are read only for the slots
+// flagged by kUVBit (a bond of the partner is damaged or broken on one side).
+template <typename T, int DIM, int MODE, bool MASK>
 __global__ void __launch_bounds__(256) k_mf_pass2(MfView<T> v, const T* __restrict__ p, const float* __restrict__ xa,
                                                   const float* __restrict__ xb, T* __restrict__ q,
                                                   float* __restrict__ qlo, const double* __restrict__ rhs,
                                                   CgScalars* cg, double* partials, unsigned int* ticket) {
   if (cg->done || (MODE == 1 && !cg->ru)) return;
   double acc = 0.0;
-  float ps = 0.f, pc = 0.f;
+  float ps = 0.f, pcs = 0.f;
   const double nd = v.norms[2];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += gridDim.x * blockDim.x) {
     T pi[3];
-    mf_load<T, DIM, MODE>(v, p, xa, xb, i, pi);
+    mf_load<T, DIM, MODE, MASK>(v, p, xa, xb, i, pi);
     T ys[3] = {T(0), T(0), T(0)}, yc[3] = {T(0), T(0), T(0)};
     const T* Ri = v.R + (int64_t)i * 9;
 #pragma unroll
@@ -331,42 +368,64 @@ __global__ void __launch_bounds__(256) k_mf_pass2(MfView<T> v, const T* __restri
     const int64_t s0 = v.mbase[sl] + (i % 32);
     const int len = (int)((v.mbase[sl + 1] - v.mbase[sl]) / 32);
     T as[NL] = {T(0), T(0)}, ac[NL] = {T(0), T(0)};
+    MfSlot<T, DIM> cur{}, nxt{};
+    T pc[3] = {T(0), T(0), T(0)}, pn[3] = {T(0), T(0), T(0)}, hc2[2] = {T(0), T(0)}, hn2[2] = {T(0), T(0)};
+    unsigned wc = 0, wn = 0, w2 = 0;
+    if (len > 0) {
+      wc = v.mp2[s0];
+      mf_slot<T, DIM>(v, s0, cur);
+      const int j0 = (int)(wc & kIdMask), l0 = (wc & kLayerBit) ? 1 : 0;
+      mf_load<T, DIM, MODE, MASK>(v, p, xa, xb, j0, pc);
+      hc2[0] = v.HF[((int64_t)j0 * NL + l0) * 2];
+      hc2[1] = v.HF[((int64_t)j0 * NL + l0) * 2 + 1];
+      if (len > 1) wn = v.mp2[s0 + 32];
+    }
     for (int k = 0; k < len; ++k) {
-      const int64_t slot = s0 + 32 * (int64_t)k;
-      const unsigned w = v.mp2[slot];
-      const int j = (int)(w & ~kLayerBit);
-      const int l = (w & kLayerBit) ? 1 : 0;
-      T pj[3];
-      mf_load<T, DIM, MODE>(v, p, xa, xb, j, pj);
-      T d[3], np[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        d[c] = c < DIM ? pj[c] - pi[c] : T(0);
-        np[c] = c < DIM ? v.m[c * v.ns + slot] : T(0);
+      if (k + 1 < len) {
+        mf_slot<T, DIM>(v, s0 + 32 * (int64_t)(k + 1), nxt);
+        const int j1 = (int)(wn & kIdMask), l1 = (wn & kLayerBit) ? 1 : 0;
+        mf_load<T, DIM, MODE, MASK>(v, p, xa, xb, j1, pn);
+        hn2[0] = v.HF[((int64_t)j1 * NL + l1) * 2];
+        hn2[1] = v.HF[((int64_t)j1 * NL + l1) * 2 + 1];
+        if (k + 2 < len) w2 = v.mp2[s0 + 32 * (int64_t)(k + 2)];
       }
-      const T c1 = v.m[3 * v.ns + slot], tp = v.m[4 * v.ns + slot];
-      const T* Uj = v.U + ((int64_t)j * NL + l) * 3;
-      const T* Vj = v.V + ((int64_t)j * NL + l) * 3;
-      const T* HFj = v.HF + ((int64_t)j * NL + l) * 2;
-      T s = np[0] * d[0], ud = Uj[0] * d[0], vd = Vj[0] * d[0];
+      const int j = (int)(wc & kIdMask);
+      const int l = (wc & kLayerBit) ? 1 : 0;
+      T d[3];
 #pragma unroll
-      for (int c = 1; c < DIM; ++c) {
-        s = fma(np[c], d[c], s);
-        ud = fma(Uj[c], d[c], ud);
-        vd = fma(Vj[c], d[c], vd);
+      for (int c = 0; c < 3; ++c) d[c] = c < DIM ? pc[c] - pi[c] : T(0);
+      T s = cur.n[0] * d[0];
+#pragma unroll
+      for (int c = 1; c < DIM; ++c) s = fma(cur.n[c], d[c], s);
+      T ud = T(0), vd = T(0);
+      if (wc & kUVBit) {
+        const T* Uj = v.U + ((int64_t)j * NL + l) * 3;
+        const T* Vj = v.V + ((int64_t)j * NL + l) * 3;
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          ud = fma(Uj[c], d[c], ud);
+          vd = fma(Vj[c], d[c], vd);
+        }
       }
-      const T coef = fma(-c1, s, T(-0.5) * fma(tp, ud + HFj[0], vd + HFj[1]));
+      const T coef = fma(-cur.c1, s, T(-0.5) * fma(cur.tp, ud + hc2[0], vd + hc2[1]));
 #pragma unroll
       for (int r = 0; r < DIM; ++r) {
         if constexpr (sizeof(T) == 4)
-          dot2_acc(ys[r], yc[r], np[r], coef);
+          dot2_acc(ys[r], yc[r], cur.n[r], coef);
         else
-          ys[r] = fma(np[r], coef, ys[r]);
+          ys[r] = fma(cur.n[r], coef, ys[r]);
       }
       if constexpr (sizeof(T) == 4)
-        dot2_acc(as[l], ac[l], tp, s);
+        dot2_acc(as[l], ac[l], cur.tp, s);
       else
-        as[l] = fma(tp, s, as[l]);
+        as[l] = fma(cur.tp, s, as[l]);
+      cur = nxt;
+      wc = wn;
+      wn = w2;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) pc[c] = pn[c];
+      hc2[0] = hn2[0];
+      hc2[1] = hn2[1];
     }
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
@@ -399,8 +458,8 @@ __global__ void __launch_bounds__(256) k_mf_pass2(MfView<T> v, const T* __restri
         q[qi] = yh;
         if constexpr (sizeof(T) == 4) {
           qlo[qi] = yl;
-          dot2_acc(ps, pc, pr, yh);
-          pc = fmaf(pr, yl, pc);
+          dot2_acc(ps, pcs, pr, yh);
+          pcs = fmaf(pr, yl, pcs);
         } else {
           acc += (double)pr * (double)yh;
         }
@@ -414,7 +473,7 @@ __global__ void __launch_bounds__(256) k_mf_pass2(MfView<T> v, const T* __restri
   double w[1], tot[1];
   bool last;
   if constexpr (sizeof(T) == 4) {
-    float s1[1] = {ps}, c1[1] = {pc};
+    float s1[1] = {ps}, c1[1] = {pcs};
     block_df_sum<1>(s1, c1, w);
     last = grid_fold<1>(w, partials, ticket, tot);
   } else {
@@ -436,6 +495,27 @@ __global__ void __launch_bounds__(256) k_mf_pass2(MfView<T> v, const T* __restri
   }
 }
 
+// Per assembly: each slot's kUVBit from its partner's U and V (zero for
+// intact bonds, whose opposite bonds mirror them exactly).
+__global__ void k_mf_flags(int n, const int64_t* __restrict__ mbase, const double* __restrict__ U64,
+                           const double* __restrict__ V64, unsigned* __restrict__ mp2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int sl = i / 32;
+  const int64_t s0 = mbase[sl] + (i % 32);
+  const int len = (int)((mbase[sl + 1] - mbase[sl]) / 32);
+  for (int k = 0; k < len; ++k) {
+    const int64_t slot = s0 + 32 * (int64_t)k;
+    const unsigned w = mp2[slot];
+    const int j = (int)(w & kIdMask), l = (w & kLayerBit) ? 1 : 0;
+    bool nz = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      nz = nz || U64[((int64_t)j * NL + l) * 3 + c] != 0.0 || V64[((int64_t)j * NL + l) * 3 + c] != 0.0;
+    mp2[slot] = nz ? (w | kUVBit) : (w & ~kUVBit);
+  }
+}
+
 }  // namespace
 
 namespace {
@@ -445,6 +525,10 @@ namespace {
 int mf_setup(lpm_handle* h) {
   Dev& d = h->d;
   const int n = h->n;
+  if (n >= (1 << 30)) {
+    h->err = "matrix-free operator: 2^30 or more particles";
+    return LPM_ERR_ARG;
+  }
   std::vector<int64_t> bptr((size_t)n + 1);
   LPM_CUDA(h, cudaMemcpy(bptr.data(), d.bptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
   const int nsl = (n + 31) / 32;
@@ -497,7 +581,7 @@ MfView<T> mf_view(lpm_handle* h) {
 // many blocks as the reduction partials hold.
 int mf_grid(const lpm_handle* h) { return grid_for(h->n, 256, kMaxRedBlocks); }
 
-template <typename T, int DIM>
+template <typename T, int DIM, bool MASK>
 int mf_product_dim(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, const T* p, T* q, float* qlo,
                    cudaGraphNode_t* last) {
   Dev& d = h->d;
@@ -506,17 +590,17 @@ int mf_product_dim(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, con
   const float* nf = nullptr;
   const double* nb = nullptr;
   if (!g) {
-    k_mf_pass1<T, DIM, 0><<<G, 256, 0, h->stream>>>(v, p, nf, nf, d.cg);
+    k_mf_pass1<T, DIM, 0, MASK><<<G, 256, 0, h->stream>>>(v, p, nf, nf, d.cg);
     LPM_LAUNCHED(h, "k_mf_pass1");
-    k_mf_pass2<T, DIM, 0><<<G, 256, 0, h->stream>>>(v, p, nf, nf, q, qlo, nb, d.cg, d.red.partials,
-                                                      d.red.ticket + 3);
+    k_mf_pass2<T, DIM, 0, MASK><<<G, 256, 0, h->stream>>>(v, p, nf, nf, q, qlo, nb, d.cg, d.red.partials,
+                                                            d.red.ticket + 3);
     LPM_LAUNCHED(h, "k_mf_pass2");
     return LPM_OK;
   }
   cudaGraphNode_t n1;
-  LPM_CUDA(h, add_kernel(&n1, g, dep, k_mf_pass1<T, DIM, 0>, G, 256, v, p, nf, nf, (const CgScalars*)d.cg));
-  LPM_CUDA(h, add_kernel(last, g, &n1, k_mf_pass2<T, DIM, 0>, G, 256, v, p, nf, nf, q, qlo, nb, d.cg, d.red.partials,
-                         d.red.ticket + 3));
+  LPM_CUDA(h, add_kernel(&n1, g, dep, k_mf_pass1<T, DIM, 0, MASK>, G, 256, v, p, nf, nf, (const CgScalars*)d.cg));
+  LPM_CUDA(h, add_kernel(last, g, &n1, k_mf_pass2<T, DIM, 0, MASK>, G, 256, v, p, nf, nf, q, qlo, nb, d.cg,
+                         d.red.partials, d.red.ticket + 3));
   return LPM_OK;
 }
 
@@ -527,29 +611,30 @@ int mf_residual_dim(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, cu
   const int G = mf_grid(h);
   float* nf = nullptr;
   if (!g) {
-    k_mf_pass1<double, DIM, 1><<<G, 256, 0, h->stream>>>(v, d.x64, d.x32, d.x32lo, d.cg);
+    k_mf_pass1<double, DIM, 1, false><<<G, 256, 0, h->stream>>>(v, d.x64, d.x32, d.x32lo, d.cg);
     LPM_LAUNCHED(h, "k_mf_pass1");
-    k_mf_pass2<double, DIM, 1><<<G, 256, 0, h->stream>>>(v, d.x64, d.x32, d.x32lo, d.r64, nf, d.rhs, d.cg,
-                                                           d.red.partials, d.red.ticket + 6);
+    k_mf_pass2<double, DIM, 1, false><<<G, 256, 0, h->stream>>>(v, d.x64, d.x32, d.x32lo, d.r64, nf, d.rhs, d.cg,
+                                                                  d.red.partials, d.red.ticket + 6);
     LPM_LAUNCHED(h, "k_mf_pass2");
     return LPM_OK;
   }
   cudaGraphNode_t n1;
-  LPM_CUDA(h, add_kernel(&n1, g, dep, k_mf_pass1<double, DIM, 1>, G, 256, v, (const double*)d.x64,
+  LPM_CUDA(h, add_kernel(&n1, g, dep, k_mf_pass1<double, DIM, 1, false>, G, 256, v, (const double*)d.x64,
                          (const float*)d.x32, (const float*)d.x32lo, (const CgScalars*)d.cg));
-  LPM_CUDA(h, add_kernel(last, g, &n1, k_mf_pass2<double, DIM, 1>, G, 256, v, (const double*)d.x64,
+  LPM_CUDA(h, add_kernel(last, g, &n1, k_mf_pass2<double, DIM, 1, false>, G, 256, v, (const double*)d.x64,
                          (const float*)d.x32, (const float*)d.x32lo, d.r64, nf, (const double*)d.rhs, d.cg,
                          d.red.partials, d.red.ticket + 6));
   return LPM_OK;
 }
 
+template <bool MASK>
 int mf_product_any(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, bool fp32, const void* p, void* q,
                    float* qlo, cudaGraphNode_t* last) {
   if (fp32)
-    return h->dim == 3 ? mf_product_dim<float, 3>(h, g, dep, (const float*)p, (float*)q, qlo, last)
-                       : mf_product_dim<float, 2>(h, g, dep, (const float*)p, (float*)q, qlo, last);
-  return h->dim == 3 ? mf_product_dim<double, 3>(h, g, dep, (const double*)p, (double*)q, nullptr, last)
-                     : mf_product_dim<double, 2>(h, g, dep, (const double*)p, (double*)q, nullptr, last);
+    return h->dim == 3 ? mf_product_dim<float, 3, MASK>(h, g, dep, (const float*)p, (float*)q, qlo, last)
+                       : mf_product_dim<float, 2, MASK>(h, g, dep, (const float*)p, (float*)q, qlo, last);
+  return h->dim == 3 ? mf_product_dim<double, 3, MASK>(h, g, dep, (const double*)p, (double*)q, nullptr, last)
+                     : mf_product_dim<double, 2, MASK>(h, g, dep, (const double*)p, (double*)q, nullptr, last);
 }
 
 }  // namespace
@@ -565,6 +650,8 @@ int mf_assemble(lpm_handle* h, int tangent, int bc) {
                                                       d.Tv, d.cs_sum, d.tsum, h->mslots, d.m64, d.m32, d.mS64, d.mU64,
                                                       d.mV64, d.mS32, d.mU32, d.mV32);
   LPM_LAUNCHED(h, "k_mf_prep");
+  k_mf_flags<<<grid_for(n, 128), 128, 0, h->stream>>>(n, d.mbase, d.mU64, d.mV64, d.mp2);
+  LPM_LAUNCHED(h, "k_mf_flags");
   const int G = grid_for(n, kRedThreads, kMaxRedBlocks);
   const int sym = tangent == LPM_TANGENT_SYMMETRIC ? 1 : 0, elim = bc == LPM_BC_ELIMINATE ? 1 : 0;
   if (h->dim == 3)
@@ -592,13 +679,14 @@ int mf_prepare_invd(lpm_handle* h, bool want32) {
   return LPM_OK;
 }
 
-int mf_launch_product(lpm_handle* h, bool fp32, const void* p, void* q, float* qlo) {
-  return mf_product_any(h, nullptr, nullptr, fp32, p, q, qlo, nullptr);
+int mf_launch_product(lpm_handle* h, bool fp32, const void* p, void* q, float* qlo, bool mask) {
+  return mask ? mf_product_any<true>(h, nullptr, nullptr, fp32, p, q, qlo, nullptr)
+              : mf_product_any<false>(h, nullptr, nullptr, fp32, p, q, qlo, nullptr);
 }
 
 int mf_graph_product(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, bool fp32, const void* p, void* q,
                      float* qlo, cudaGraphNode_t* last) {
-  return mf_product_any(h, g, dep, fp32, p, q, qlo, last);
+  return mf_product_any<false>(h, g, dep, fp32, p, q, qlo, last);
 }
 
 int mf_launch_residual(lpm_handle* h) {
