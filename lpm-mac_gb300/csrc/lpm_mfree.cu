@@ -34,8 +34,8 @@
 // (stiffness.h:265-294) is A' = P A P + nd (I - P): the input is masked,
 // the fixed rows return nd p.
 //
-// Bytes per FP32 product: pass 1 reads per slot the partner, n' and t'
-// (20 B), pass 2 the partner, n', a' - t' and t' (24 B); per particle the
+// Bytes per FP32 product: pass 1 reads per slot the partner and one 16-byte
+// word {n', t'} (20 B), pass 2 the same and a' - t' (24 B); per particle the
 // row sums (36 B), S, U, V of both layers (72 B), H and F (16 B), p and
 // the pair q (36 B).  At 101^3 that is about 1.0 GB against 2.4 GB for the
 // assembled FP32 product.
@@ -94,10 +94,10 @@ __global__ void k_mf_prep(int n, const int64_t* __restrict__ bptr, const int64_t
     const double v[kMfFields] = {cs[3 * (int64_t)bo], cs[3 * (int64_t)bo + 1], cs[3 * (int64_t)bo + 2], c1, tp};
     const int64_t slot = s0 + 32 * k;
 #pragma unroll
-    for (int e = 0; e < kMfFields; ++e) {
-      m64[e * ns + slot] = v[e];
-      m32[e * ns + slot] = (float)v[e];
-    }
+    for (int e = 0; e < kMfFields; ++e) m64[e * ns + slot] = v[e];
+    // FP32: one 16-byte word {n'x, n'y, n'z, t'} per slot, then a' - t'
+    reinterpret_cast<float4*>(m32)[slot] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)tp);
+    m32[4 * ns + slot] = (float)c1;
     const int l = blayer[b] != 0;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -226,14 +226,16 @@ template <typename T>
 struct MfView {
   const int64_t* __restrict__ mbase;
   const unsigned* __restrict__ mp2;
-  const T* __restrict__ m;  // [kMfFields][ns]
+  // slot coefficients: FP64 [5][ns] (n'x, n'y, n'z, a' - t', t'); FP32 a
+  // float4 {n'x, n'y, n'z, t'} per slot, then [ns] a' - t'
+  const T* __restrict__ m;
   const T* __restrict__ S;  // [n][2][3]
   const T* __restrict__ U;
   const T* __restrict__ V;
   const T* __restrict__ R;  // [n][9]
   const unsigned char* __restrict__ fixed;
   const double* norms;
-  T* __restrict__ HF;  // [n][2][2]: H, F per layer (pass 1 out, pass 2 in)
+  T* __restrict__ HF;  // [2][n][2]: H, F per layer and particle (pass 1 out, pass 2 in)
   int64_t ns;
   int n;
 };
@@ -273,10 +275,35 @@ struct MfSlot {
 
 template <typename T, int DIM>
 __device__ __forceinline__ void mf_slot(const MfView<T>& v, int64_t slot, MfSlot<T, DIM>& o) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(v.m) + slot);
+    o.n[0] = a.x;
+    o.n[1] = a.y;
+    o.n[2] = DIM == 3 ? a.z : 0.f;
+    o.tp = a.w;
+    o.c1 = v.m[4 * v.ns + slot];
+  } else {
 #pragma unroll
-  for (int c = 0; c < 3; ++c) o.n[c] = c < DIM ? v.m[c * v.ns + slot] : T(0);
-  o.c1 = v.m[3 * v.ns + slot];
-  o.tp = v.m[4 * v.ns + slot];
+    for (int c = 0; c < 3; ++c) o.n[c] = c < DIM ? v.m[c * v.ns + slot] : T(0);
+    o.c1 = v.m[3 * v.ns + slot];
+    o.tp = v.m[4 * v.ns + slot];
+  }
+}
+
+// The first pass's sums (H, F) of particle j, layer l: one 8- or 16-byte
+// load (stored per layer, so a warp's partners read adjacent pairs).
+template <typename T>
+__device__ __forceinline__ void mf_hf(const MfView<T>& v, int j, int l, T (&o)[2]) {
+  const int64_t q = ((int64_t)l * v.n + j) * 2;
+  if constexpr (sizeof(T) == 4) {
+    const float2 a = *reinterpret_cast<const float2*>(v.HF + q);
+    o[0] = a.x;
+    o[1] = a.y;
+  } else {
+    const double2 a = *reinterpret_cast<const double2*>(v.HF + q);
+    o[0] = a.x;
+    o[1] = a.y;
+  }
 }
 
 // Pass 1: H_j = sum n'.(p_m - p_j), F_j = sum t' n'.(p_m - p_j) per layer
@@ -329,8 +356,8 @@ __global__ void __launch_bounds__(256) k_mf_pass1(MfView<T> v, const T* __restri
     }
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
-      v.HF[((int64_t)j * NL + l) * 2] = hs[l] + hc[l];
-      v.HF[((int64_t)j * NL + l) * 2 + 1] = fs[l] + fc[l];
+      v.HF[((int64_t)l * v.n + j) * 2] = hs[l] + hc[l];
+      v.HF[((int64_t)l * v.n + j) * 2 + 1] = fs[l] + fc[l];
     }
   }
 }
@@ -376,8 +403,7 @@ __global__ void __launch_bounds__(256) k_mf_pass2(MfView<T> v, const T* __restri
       mf_slot<T, DIM>(v, s0, cur);
       const int j0 = (int)(wc & kIdMask), l0 = (wc & kLayerBit) ? 1 : 0;
       mf_load<T, DIM, MODE, MASK>(v, p, xa, xb, j0, pc);
-      hc2[0] = v.HF[((int64_t)j0 * NL + l0) * 2];
-      hc2[1] = v.HF[((int64_t)j0 * NL + l0) * 2 + 1];
+      mf_hf<T>(v, j0, l0, hc2);
       if (len > 1) wn = v.mp2[s0 + 32];
     }
     for (int k = 0; k < len; ++k) {
@@ -385,8 +411,7 @@ __global__ void __launch_bounds__(256) k_mf_pass2(MfView<T> v, const T* __restri
         mf_slot<T, DIM>(v, s0 + 32 * (int64_t)(k + 1), nxt);
         const int j1 = (int)(wn & kIdMask), l1 = (wn & kLayerBit) ? 1 : 0;
         mf_load<T, DIM, MODE, MASK>(v, p, xa, xb, j1, pn);
-        hn2[0] = v.HF[((int64_t)j1 * NL + l1) * 2];
-        hn2[1] = v.HF[((int64_t)j1 * NL + l1) * 2 + 1];
+        mf_hf<T>(v, j1, l1, hn2);
         if (k + 2 < len) w2 = v.mp2[s0 + 32 * (int64_t)(k + 2)];
       }
       const int j = (int)(wc & kIdMask);
