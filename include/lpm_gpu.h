@@ -328,6 +328,39 @@ typedef struct {
 int lpm_fatigue_cycle(lpm_handle* h, const lpm_bc* bcs_unit, int nbc, double f0, double f1, double f2,
                       int n_interval, double dNdt, const lpm_step_opts* opts, lpm_cycle_result* res);
 
+/* Cyclic loading: SolverFatigue::solveProblemCyclic (solver_fatigue.h:
+ * 174-210) with generateLoadCycle (:128-172), run inside the library.  The
+ * load spectrum (readLoad's format, solver_fatigue.h:41-60: f_min, then
+ * f_max, f_min pairs; an odd count of values) is copied to the device once
+ * per call; cycle N's increments (f1 - f0)/n_interval and (f2 - f1)/n_interval
+ * with f0, f1, f2 = spectrum[2N..2N+2] are formed there and scale the unit
+ * boundary conditions bcs_unit on the device.  Each simulated cycle is
+ * lpm_fatigue_cycle's work with dNdt from the time map (LPM_TIME_LINEAR:
+ * (int)(1/tau); LPM_TIME_EXPONENTIAL: (int)(exp(t/tau)/tau), t counting
+ * simulated cycles), after which N += dNdt; the run ends when N reaches
+ * (count-1)/2, after max_cycles simulated cycles (if > 0), or after a cycle
+ * with dNdt = 0 (where the reference would loop for ever).  One record per
+ * simulated cycle goes to records (up to capacity): N after the cycle,
+ * dNdt, the cycle's iteration counts, whether new damage appeared, and the
+ * mean strain energy the reference prints (first state variable over the
+ * particles that damage).  *ncycles = simulated cycles run.  Returns
+ * LPM_NOT_CONVERGED if any step of any cycle hit max_iter (kept, as the
+ * reference keeps it). */
+#define LPM_TIME_LINEAR 0
+#define LPM_TIME_EXPONENTIAL 1
+typedef struct {
+  int64_t N;             /* real cycle count after this simulated cycle  */
+  int dNdt;              /* real cycles this simulated cycle stood for   */
+  int newton_iters;
+  int unconverged_steps;
+  int new_damage;
+  int64_t cg_iters;
+  double mean_energy;    /* "Average strain energy" of solveProblemCyclic */
+} lpm_fatigue_record;
+int lpm_fatigue_run(lpm_handle* h, const lpm_bc* bcs_unit, int nbc, const double* spectrum, int64_t nvalues,
+                    int n_interval, int time_mode, double tau, int64_t max_cycles, const lpm_step_opts* opts,
+                    lpm_fatigue_record* records, int64_t capacity, int64_t* ncycles);
+
 /* ---- Adjoint (backward) of a converged load step ----
  * No counterpart in the reference, whose only derivative of the internal
  * force is the forward-difference tangent (Stiffness::localStiffnessFD,

@@ -60,6 +60,15 @@ class CycleResult(ctypes.Structure):
                 ("pad", ctypes.c_int), ("cg_iters", ctypes.c_int64)]
 
 
+class FatigueRecord(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int64), ("dNdt", ctypes.c_int), ("newton_iters", ctypes.c_int),
+                ("unconverged_steps", ctypes.c_int), ("new_damage", ctypes.c_int), ("cg_iters", ctypes.c_int64),
+                ("mean_energy", ctypes.c_double)]
+
+
+TIME_LINEAR, TIME_EXPONENTIAL = 0, 1
+
+
 class AdjointResult(ctypes.Structure):
     _fields_ = [("cg_iters", ctypes.c_int64), ("relres", ctypes.c_double)]
 
@@ -134,6 +143,8 @@ def load(build_if_needed=True):
         "lpm_find_neighbors": [ctypes.c_int, dp, dp, i64, i64p, ip, i64p],
         "lpm_fatigue_cycle": [H, ctypes.POINTER(BC), ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                               ctypes.c_int, ctypes.c_double, ctypes.POINTER(StepOpts), ctypes.POINTER(CycleResult)],
+        "lpm_fatigue_run": [H, ctypes.POINTER(BC), ctypes.c_int, dp, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                            i64, ctypes.POINTER(StepOpts), ctypes.POINTER(FatigueRecord), i64, i64p],
         "lpm_backward_step": [H, dp, dp, ctypes.c_double, i64, ctypes.c_int, dp, dp, ctypes.POINTER(AdjointResult)],
         "lpm_apply_jacobian": [H, dp, dp],
         "lpm_tangent_begin": [H, ctypes.c_int, dp, ctypes.c_double],
@@ -164,7 +175,7 @@ def exported_symbols():
             "lpm_apply_operator", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
             "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
-            "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
+            "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_fatigue_run", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
             "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_bond_constants", "lpm_tangent_get",
             "lpm_tangent_end"]
 
@@ -442,6 +453,23 @@ class Lattice:
                                                    ctypes.byref(o), ctypes.byref(r)), allow=(OK, NOT_CONVERGED))
         return dict(status=st, newton_iters=r.newton_iters, unconverged_steps=r.unconverged_steps,
                     new_damage=bool(r.new_damage), cg_iters=r.cg_iters)
+
+    def fatigue_run(self, bcs_unit, spectrum, n_interval, tau, time_mode=TIME_LINEAR, max_cycles=0,
+                    tangent=TANGENT_SYMMETRIC, precision=PREC_FP64, max_iter=30, tol=1e-5, cg_tol=1e-10, cg_maxit=-1):
+        """lpm_fatigue_run: the whole cyclic loading inside the library, the
+        spectrum on the device.  Returns (status, list of per-cycle records)."""
+        sp = np.ascontiguousarray(spectrum, dtype=np.float64)
+        o = StepOpts(SOLVER_FATIGUE_STATIC, int(tangent), int(precision), int(max_iter), float(tol), float(cg_tol),
+                     int(cg_maxit), 0)
+        nsim = int(max_cycles) if max_cycles > 0 else max(1, (len(sp) - 1) // 2)
+        recs = (FatigueRecord * nsim)()
+        n = ctypes.c_int64()
+        st = self._check(self._L.lpm_fatigue_run(self.h, self._bc_array(bcs_unit), len(bcs_unit), _d(sp), len(sp),
+                                                 int(n_interval), int(time_mode), float(tau), int(max_cycles),
+                                                 ctypes.byref(o), recs, nsim, ctypes.byref(n)),
+                         allow=(OK, NOT_CONVERGED))
+        out = [{k: getattr(recs[i], k) for k, _ in FatigueRecord._fields_} for i in range(min(n.value, nsim))]
+        return st, out
 
     def load_step(self, bcs, solver=SOLVER_FATIGUE_STATIC, tangent=TANGENT_SYMMETRIC, precision=PREC_FP64,
                   max_iter=30, tol=1e-5, cg_tol=1e-10, cg_maxit=-1, max_cuts=8):

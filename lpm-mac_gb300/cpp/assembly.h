@@ -13,6 +13,7 @@
 
 #include <memory>
 
+#include "dump_writer.h"
 #include "particle.h"
 
 template <int nlayer>
@@ -166,18 +167,29 @@ class Assembly {
     for (auto pt : pt_sys) fprintf(f, "%d %d %.4e %.4e %.4e \n", pt->id, pt->type, pt->xyz[0], pt->xyz[1], pt->xyz[2]);
     fclose(f);
   }
-  // LAMMPS dump, the columns of assembly.h:309-335
+  // LAMMPS dump, the columns of assembly.h:309-335.  The particle columns
+  // are copied here and written by the asynchronous dump writer
+  // (dump_writer.h), so the load steps go on while the text is formatted and
+  // appended; flushDumps() waits for it.
   void writeDump(const std::string& dumpFile, int step) {
-    FILE* f = fopen(dumpFile.c_str(), "a+");
-    if (!f) return;
-    header(f, step);
-    fprintf(f, "ITEM: ATOMS id type x y z dx dy dz s11 s22 s33 s23 s13 s12 damage damage_visual state_var[0] \n");
-    for (auto pt : pt_sys)
-      fprintf(f, "%d %d %.4e %.4e %.4e %.4e %.4e %.4e %.4e %.4e %.4e %.4e %.4e %.4e %.4e %.4e %.4e\n", pt->id, pt->type,
-              pt->xyz[0], pt->xyz[1], pt->xyz[2], pt->xyz[0] - pt->xyz_initial[0], pt->xyz[1] - pt->xyz_initial[1],
-              pt->xyz[2] - pt->xyz_initial[2], pt->stress[0], pt->stress[1], pt->stress[2], pt->stress[3],
-              pt->stress[4], pt->stress[5], pt->damage, pt->damage_visual, pt->state_var[0]);
-    fclose(f);
+    DumpRecord r;
+    r.file = dumpFile;
+    r.step = step;
+    r.nparticle = nparticle;
+    for (int k = 0; k < 6; ++k) r.box[k] = box[(size_t)k];
+    r.id.reserve(pt_sys.size());
+    r.type.reserve(pt_sys.size());
+    r.cols.reserve(pt_sys.size() * DumpWriter::kCols);
+    for (auto pt : pt_sys) {
+      r.id.push_back(pt->id);
+      r.type.push_back(pt->type);
+      const double c[DumpWriter::kCols] = {pt->xyz[0], pt->xyz[1], pt->xyz[2], pt->xyz[0] - pt->xyz_initial[0],
+                                           pt->xyz[1] - pt->xyz_initial[1], pt->xyz[2] - pt->xyz_initial[2],
+                                           pt->stress[0], pt->stress[1], pt->stress[2], pt->stress[3], pt->stress[4],
+                                           pt->stress[5], pt->damage, pt->damage_visual, pt->state_var[0]};
+      r.cols.insert(r.cols.end(), c, c + DumpWriter::kCols);
+    }
+    DumpWriter::instance().submit(std::move(r));
   }
   // readDump (assembly.h:337-388): id type x y z, ids 0..N-1
   void readDump(const std::string& dumpFile, UnitCell& cell) {

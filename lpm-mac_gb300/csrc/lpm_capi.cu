@@ -771,28 +771,48 @@ int lpm_synchronize(lpm_handle* h) {
 }
 
 
-int lpm_fatigue_cycle(lpm_handle* h, const lpm_bc* bcs, int nbc, double f0, double f1, double f2, int n_interval,
-                      double dNdt, const lpm_step_opts* o, lpm_cycle_result* res) {
-  if (!h || !o || nbc < 0 || (nbc > 0 && !bcs) || n_interval < 1) return arg_error(h, "bad fatigue cycle");
+}  // extern "C"
+
+namespace {
+
+int check_cycle_args(lpm_handle* h, const lpm_bc* bcs, int nbc, int n_interval, const lpm_step_opts* o) {
+  if (!o || nbc < 0 || (nbc > 0 && !bcs) || n_interval < 1) return arg_error(h, "bad fatigue cycle");
   for (int k = 0; k < nbc; ++k)
-    if (bcs[k].group < 0 || bcs[k].group >= (int)h->groups.size() || (bcs[k].kind != LPM_BC_DISP &&
-                                                                     bcs[k].kind != LPM_BC_FORCE))
+    if (bcs[k].group < 0 || bcs[k].group >= (int)h->groups.size() ||
+        (bcs[k].kind != LPM_BC_DISP && bcs[k].kind != LPM_BC_FORCE) || (bcs[k].mode != 0 && bcs[k].mode != 1) ||
+        (bcs[k].kind == LPM_BC_DISP && (bcs[k].axis < 0 || bcs[k].axis > 2)))
       return arg_error(h, "bad boundary condition");
+  return LPM_OK;
+}
+
+// One fatigue cycle (SolverFatigue::solveProblemOneCycle, solver_fatigue.h:
+// 212-233).  The two load increments, loading and unloading half, come from
+// the host (inc_host) or from device memory (inc_dev, the cyclic driver).
+int cycle_core(lpm_handle* h, const lpm_bc* bcs, int nbc, const double* inc_host, const double* inc_dev,
+               int n_interval, double dNdt, const lpm_step_opts* o, lpm_cycle_result* res) {
   lpm_cycle_result r{};
   const int64_t it0 = h->stats.cg_iters_total;
   int st = LPM_OK;
   for (int half = 0; half < 2; ++half) {
-    const double inc = (half == 0 ? f1 - f0 : f2 - f1) / n_interval;
     for (int step = 0; step < n_interval; ++step) {
       // SolverFatigue::solveProblemStep (solver_fatigue.h:272-296)
       for (int k = 0; k < nbc; ++k)
         if (bcs[k].kind == LPM_BC_FORCE) {
-          st = lpm_apply_force_bc(h, bcs[k].group, bcs[k].mode, bcs[k].fx * inc, bcs[k].fy * inc, bcs[k].fz * inc);
+          const Group& g = h->groups[(size_t)bcs[k].group];
+          if (inc_dev)
+            st = launch_force_bc_scaled(h, g, bcs[k].mode, bcs[k].fx, bcs[k].fy, bcs[k].fz, inc_dev + half);
+          else
+            st = lpm_apply_force_bc(h, bcs[k].group, bcs[k].mode, bcs[k].fx * inc_host[half],
+                                    bcs[k].fy * inc_host[half], bcs[k].fz * inc_host[half]);
           if (st) return st;
         }
       for (int k = 0; k < nbc; ++k)
         if (bcs[k].kind == LPM_BC_DISP) {
-          st = lpm_apply_disp_bc(h, bcs[k].group, bcs[k].axis, bcs[k].mode, bcs[k].value * inc);
+          const Group& g = h->groups[(size_t)bcs[k].group];
+          if (inc_dev)
+            st = launch_disp_bc_scaled(h, g, bcs[k].axis, bcs[k].mode, bcs[k].value, inc_dev + half);
+          else
+            st = lpm_apply_disp_bc(h, bcs[k].group, bcs[k].axis, bcs[k].mode, bcs[k].value * inc_host[half]);
           if (st) return st;
         }
       st = lpm_assemble(h, o->tangent, LPM_BC_ELIMINATE);
@@ -817,6 +837,82 @@ int lpm_fatigue_cycle(lpm_handle* h, const lpm_bc* bcs, int nbc, double f0, doub
   r.cg_iters = h->stats.cg_iters_total - it0;
   if (res) *res = r;
   return r.unconverged_steps ? LPM_NOT_CONVERGED : LPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lpm_fatigue_cycle(lpm_handle* h, const lpm_bc* bcs, int nbc, double f0, double f1, double f2, int n_interval,
+                      double dNdt, const lpm_step_opts* o, lpm_cycle_result* res) {
+  if (!h) return LPM_ERR_ARG;
+  int st = check_cycle_args(h, bcs, nbc, n_interval, o);
+  if (st) return st;
+  const double inc[2] = {(f1 - f0) / n_interval, (f2 - f1) / n_interval};
+  return cycle_core(h, bcs, nbc, inc, nullptr, n_interval, dNdt, o, res);
+}
+
+int lpm_fatigue_run(lpm_handle* h, const lpm_bc* bcs, int nbc, const double* spectrum, int64_t nvalues,
+                    int n_interval, int time_mode, double tau, int64_t max_cycles, const lpm_step_opts* o,
+                    lpm_fatigue_record* records, int64_t capacity, int64_t* ncycles) {
+  if (!h) return LPM_ERR_ARG;
+  int st = check_cycle_args(h, bcs, nbc, n_interval, o);
+  if (st) return st;
+  if (!spectrum || nvalues < 3 || nvalues % 2 == 0)
+    return arg_error(h, "spectrum: f_min then (f_max, f_min) pairs, an odd count of at least 3 values");
+  if (!(tau > 0.0) || (time_mode != LPM_TIME_LINEAR && time_mode != LPM_TIME_EXPONENTIAL))
+    return arg_error(h, "bad time map");
+  if (capacity < 0 || (capacity > 0 && !records)) return arg_error(h, "bad record buffer");
+  Dev& d = h->d;
+  // the spectrum lives on the device for the run; cycle N's increments are
+  // formed there and read by the BC kernels
+  if (h->spectrum_cap < nvalues) {
+    d.spectrum = (double*)dev_alloc(h, sizeof(double) * (size_t)nvalues);
+    if (!d.spectrum) return LPM_ERR_NOMEM;
+    h->spectrum_cap = nvalues;
+  }
+  if (!d.cycle) {
+    d.cycle = (double*)zeros_dev(h, sizeof(double) * 4);
+    if (!d.cycle) return LPM_ERR_NOMEM;
+  }
+  LPM_CUDA(h, cudaMemcpyAsync(d.spectrum, spectrum, sizeof(double) * (size_t)nvalues, cudaMemcpyHostToDevice,
+                              h->stream));
+  // SolverFatigue::solveProblemCyclic (solver_fatigue.h:174-210)
+  const double n_cycles = 0.5 * (double)(nvalues - 1);
+  long long N = 0;
+  double t = 0.0;
+  int64_t done = 0;
+  int result = LPM_OK;
+  while ((double)N < n_cycles && (max_cycles <= 0 || done < max_cycles)) {
+    st = launch_cycle_increments(h, d.spectrum, N, n_interval, d.cycle);
+    if (st) return st;
+    const int dNdt = time_mode == LPM_TIME_LINEAR ? (int)(1 / tau) : (int)(1 / tau * exp(t / tau));
+    if (time_mode == LPM_TIME_EXPONENTIAL) t += 1.0;
+    lpm_cycle_result r{};
+    st = cycle_core(h, bcs, nbc, nullptr, d.cycle, n_interval, (double)dNdt, o, &r);
+    if (st < 0) return st;
+    if (st == LPM_NOT_CONVERGED) result = LPM_NOT_CONVERGED;
+    st = launch_mean_state0(h, d.cycle + 2);
+    if (st) return st;
+    double mean = 0.0;
+    LPM_CUDA(h, cudaMemcpyAsync(&mean, d.cycle + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    N += dNdt;
+    if (done < capacity) {
+      lpm_fatigue_record& rec = records[done];
+      rec.N = N;
+      rec.dNdt = dNdt;
+      rec.newton_iters = r.newton_iters;
+      rec.unconverged_steps = r.unconverged_steps;
+      rec.new_damage = r.new_damage;
+      rec.cg_iters = r.cg_iters;
+      rec.mean_energy = mean;
+    }
+    ++done;
+    if (dNdt <= 0) break;  // a time map below one cycle per step would never end
+  }
+  if (ncycles) *ncycles = done;
+  return result;
 }
 
 int lpm_backward_step(lpm_handle* h, const double* dJdx, const double* dJdpin, double cg_tol, int64_t cg_maxit,

@@ -213,7 +213,103 @@ __global__ void k_force_bc(const int* __restrict__ ids, int count, int mode, dou
   }
 }
 
+// Load increments of cycle N of a spectrum held on the device
+// (SolverFatigue::generateLoadCycle, solver_fatigue.h:128-172): the loading
+// half steps by (f1 - f0)/n_interval, the unloading half by (f2 - f1)/n_interval,
+// with f0, f1, f2 = spectrum[2N], spectrum[2N+1], spectrum[2N+2].
+__global__ void k_cycle_increments(const double* __restrict__ spectrum, long long N, int n_interval,
+                                   double* __restrict__ inc) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const double f0 = spectrum[2 * N], f1 = spectrum[2 * N + 1], f2 = spectrum[2 * N + 2];
+    inc[0] = (f1 - f0) / n_interval;
+    inc[1] = (f2 - f1) / n_interval;
+  }
+}
+
+// DispBC / ForceBC with the unit load scaled by a factor read from device
+// memory (the cycle's increment), so the host never reads the spectrum.
+__global__ void k_disp_bc_scaled(const int* __restrict__ ids, int count, int axis, int mode, double unit,
+                                 const double* __restrict__ scale, double* x, int* mask) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = ids[t];
+  const double value = unit * scale[0];
+  if (mode == 0) {
+    x[3 * i + axis] += value;
+  } else {
+    x[3 * i + 0] = axis == 0 ? value : 0.0;
+    x[3 * i + 1] = axis == 1 ? value : 0.0;
+    x[3 * i + 2] = axis == 2 ? value : 0.0;
+  }
+  mask[3 * i + axis] = 1;
+}
+
+__global__ void k_force_bc_scaled(const int* __restrict__ ids, int count, int mode, double fx, double fy, double fz,
+                                  const double* __restrict__ scale, double* pex) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int i = ids[t];
+  const double s = scale[0];
+  const double a = fx * s / count, b = fy * s / count, c = fz * s / count;
+  if (mode == 0) {
+    pex[3 * i] += a;
+    pex[3 * i + 1] += b;
+    pex[3 * i + 2] += c;
+  } else {
+    pex[3 * i] = a;
+    pex[3 * i + 1] = b;
+    pex[3 * i + 2] = c;
+  }
+}
+
+// Mean of the first state variable (the HCF law's strain energy) over the
+// particles that damage (SolverFatigue::solveProblemCyclic,
+// solver_fatigue.h:201-212).
+__global__ void k_mean_state0(int n, int ns, const double* __restrict__ state, const int* __restrict__ ptype,
+                              int undamaged, double* partials, unsigned int* ticket, double* out) {
+  double v[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (ptype[i] != undamaged) {
+      v[0] += state[(int64_t)i * ns];
+      v[1] += 1.0;
+    }
+  double tot[2];
+  if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) *out = tot[1] > 0 ? tot[0] / tot[1] : 0.0;
+}
+
 }  // namespace
+
+int launch_cycle_increments(lpm_handle* h, const double* spectrum, long long N, int n_interval, double* inc) {
+  k_cycle_increments<<<1, 32, 0, h->stream>>>(spectrum, N, n_interval, inc);
+  LPM_LAUNCHED(h, "k_cycle_increments");
+  return LPM_OK;
+}
+
+int launch_disp_bc_scaled(lpm_handle* h, const Group& g, int axis, int mode, double unit, const double* scale) {
+  if (g.count == 0) return LPM_OK;
+  const int T = 256;
+  k_disp_bc_scaled<<<grid_for(g.count, T), T, 0, h->stream>>>(g.ids, g.count, axis, mode, unit, scale, h->d.x,
+                                                              h->d.mask);
+  LPM_LAUNCHED(h, "k_disp_bc_scaled");
+  return LPM_OK;
+}
+
+int launch_force_bc_scaled(lpm_handle* h, const Group& g, int mode, double fx, double fy, double fz,
+                           const double* scale) {
+  if (g.count == 0) return LPM_OK;
+  const int T = 256;
+  k_force_bc_scaled<<<grid_for(g.count, T), T, 0, h->stream>>>(g.ids, g.count, mode, fx, fy, fz, scale, h->d.pex);
+  LPM_LAUNCHED(h, "k_force_bc_scaled");
+  return LPM_OK;
+}
+
+int launch_mean_state0(lpm_handle* h, double* out_dev) {
+  const int G = grid_for(h->n, kRedThreads, kMaxRedBlocks);
+  k_mean_state0<<<G, kRedThreads, 0, h->stream>>>(h->n, h->nstate, h->d.state, h->d.ptype, h->undamaged,
+                                                  h->d.red.partials, h->d.red.ticket + 12, out_dev);
+  LPM_LAUNCHED(h, "k_mean_state0");
+  return LPM_OK;
+}
 
 int launch_geometry_force(lpm_handle* h) {
   const Dev& d = h->d;

@@ -139,6 +139,9 @@ struct Dev {
   unsigned* mp2;
   double *m64, *mS64, *mU64, *mV64, *mR64, *mdiag, *mHF64;
   float *m32, *mS32, *mU32, *mV32, *mR32, *mHF32;
+  // cyclic driver: the load spectrum, and the cycle's two load increments
+  // and mean strain energy
+  double *spectrum, *cycle;
   // reductions
   RedBuf red;
   CgScalars* cg;   // device scalars
@@ -204,6 +207,7 @@ struct lpm_handle {
   bool mf = false;        // the CG applies the tangent matrix-free (lpm_set_operator)
   int64_t mslots = 0;     // slots of the matrix-free bond layout
   int mnsl = 0;           // 32-particle slices of that layout
+  int64_t spectrum_cap = 0;  // values the device spectrum buffer holds
   // host mirrors
   lpm::CgScalars* h_cg = nullptr;  // pinned
   double* h_norms = nullptr;       // pinned [8]
@@ -238,6 +242,13 @@ int launch_residual(lpm_handle* h, double* norm_r, double* norm_R);
 int launch_move_by_disp(lpm_handle* h);
 int launch_disp_bc(lpm_handle* h, const Group& g, int axis, int mode, double value);
 int launch_force_bc(lpm_handle* h, const Group& g, int mode, double fx, double fy, double fz);
+// the cyclic driver (lpm_fatigue_run): increments of cycle N from a device
+// spectrum, BCs scaled by a device factor, mean strain energy (device out)
+int launch_cycle_increments(lpm_handle* h, const double* spectrum, long long N, int n_interval, double* inc);
+int launch_disp_bc_scaled(lpm_handle* h, const Group& g, int axis, int mode, double unit, const double* scale);
+int launch_force_bc_scaled(lpm_handle* h, const Group& g, int mode, double fx, double fy, double fz,
+                           const double* scale);
+int launch_mean_state0(lpm_handle* h, double* out_dev);
 // material laws (lpm_laws.cu)
 int launch_update_state(lpm_handle* h);
 int launch_static_damage(lpm_handle* h, int* any_new);

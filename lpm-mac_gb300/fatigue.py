@@ -1,13 +1,13 @@
-"""Cyclic fatigue loading over lpm_fatigue_cycle.
+"""Cyclic fatigue loading.
 
-``run_cycles`` follows SolverFatigue::solveProblemCyclic
-(solver_fatigue.h:174-210): cycle N takes its loads f_min, f_max, f_min from
-the spectrum at 2N, 2N+1, 2N+2, each simulated cycle stands for dN/dt real
-cycles (TimeMapMode Linear: int(1/tau); Exponential: int(exp(t/tau)/tau)
-with t counting simulated cycles), and the run ends once N reaches the
-spectrum's cycle count.  Every cycle is one library call, so the load steps,
-Newton solves, state updates and the fatigue damage update of a cycle run
-back to back on the device.
+``run_cycles`` is SolverFatigue::solveProblemCyclic (solver_fatigue.h:174-210)
+run inside the library (lpm_fatigue_run): cycle N takes its loads f_min,
+f_max, f_min from the spectrum at 2N, 2N+1, 2N+2 (the spectrum is held on the
+device and the increments are formed there), each simulated cycle stands
+for dN/dt real cycles (TimeMapMode Linear: int(1/tau); Exponential:
+int(exp(t/tau)/tau) with t counting simulated cycles), and the run ends once
+N reaches the spectrum's cycle count.  ``run_cycles_per_call`` drives the
+same loop from Python with one lpm_fatigue_cycle call per cycle.
 """
 import math
 
@@ -33,9 +33,24 @@ def dNdt(tau, t, mode=LINEAR):
     return int(1.0 / tau * math.exp(t / tau))
 
 
-def run_cycles(lattice, bcs_unit, spectrum, n_interval, tau, mode=LINEAR, max_calls=None, on_cycle=None, **opts):
-    """Runs the cyclic loading; returns one record per simulated cycle
-    (real cycle count N after it, dN/dt, and the call's result)."""
+def run_cycles(lattice, bcs_unit, spectrum, n_interval, tau, mode=LINEAR, max_calls=None, **opts):
+    """Runs the cyclic loading in the library; returns one record per
+    simulated cycle (real cycle count N after it, dN/dt, iteration counts,
+    new damage, mean strain energy, and a status: NOT_CONVERGED if a step of
+    the cycle hit max_iter)."""
+    from .capi import NOT_CONVERGED, OK, TIME_EXPONENTIAL, TIME_LINEAR
+    st, recs = lattice.fatigue_run(bcs_unit, spectrum, n_interval, tau,
+                                   TIME_LINEAR if mode == LINEAR else TIME_EXPONENTIAL,
+                                   max_calls or 0, **opts)
+    for r in recs:
+        r["status"] = NOT_CONVERGED if r["unconverged_steps"] else OK
+        r["new_damage"] = bool(r["new_damage"])
+    return recs
+
+
+def run_cycles_per_call(lattice, bcs_unit, spectrum, n_interval, tau, mode=LINEAR, max_calls=None, **opts):
+    """The same loop driven from Python, one lpm_fatigue_cycle call per
+    simulated cycle (the spectrum values passed from the host)."""
     n_cycles = 0.5 * (len(spectrum) - 1)
     N, t, out = 0, 0, []
     while N < n_cycles:
@@ -45,8 +60,6 @@ def run_cycles(lattice, bcs_unit, spectrum, n_interval, tau, mode=LINEAR, max_ca
         r = lattice.fatigue_cycle(bcs_unit, f0, f1, f2, n_interval, jump, **opts)
         N += jump
         out.append(dict(N=N, dNdt=jump, **r))
-        if on_cycle:
-            on_cycle(N, r)
         if max_calls is not None and len(out) >= max_calls:
             break
     return out

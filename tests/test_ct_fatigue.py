@@ -134,10 +134,61 @@ def test_ct_fatigue_cycles_match_oracle():
     eu = np.abs((g.download(capi.F_XYZ) - xyz) - (o.get(oracle.XYZ) - xyz)).max() / scale
     print("[parity] CT fatigue: displacement %.3e, damage %.3e" % (
         eu, np.abs(g.download(capi.F_DAMAGE) - o.get(oracle.DAMAGE)).max() / o.get(oracle.DAMAGE).max()))
-    assert eu <= 1e-8
+    assert eu <= 1e-10
     d_o, d_g = o.get(oracle.DAMAGE), g.download(capi.F_DAMAGE)
     assert d_o.max() > 0
-    assert np.abs(d_g - d_o).max() <= 1e-8 * d_o.max()
+    assert np.abs(d_g - d_o).max() <= 1e-10 * d_o.max()
     s_o, s_g = o.state(), g.state()
-    assert np.abs(s_g - s_o).max() <= 1e-8 * np.abs(s_o).max()
+    assert np.abs(s_g - s_o).max() <= 1e-10 * np.abs(s_o).max()
+    # the mean strain energy solveProblemCyclic prints (solver_fatigue.h:201-212)
+    mean_o = s_o[types != 4, 0].mean()
+    assert abs(recs[-1]["mean_energy"] - mean_o) <= 1e-10 * abs(mean_o)
     g.close()
+
+
+def _ct_gpu():
+    args, info, groups, params, types, (nl_ptr, nl_idx, L) = ct_case()
+    g = make_gpu(*args)
+    g.set_law(capi.LAW_FATIGUE_HCF, params)
+    g.set_types(types, 4)
+    g.set_nonlocal(nl_ptr, nl_idx, L)
+    g.update()
+    gm, gt, gb = g.add_group(groups["mid"]), g.add_group(groups["top"]), g.add_group(groups["bottom"])
+    fixed = [("disp", gm, 1, 0.0), ("disp", gt, 0, 0.0), ("disp", gb, 0, 0.0)]
+    f_min = R_RATIO * F_MAX
+    r = g.load_step(fixed + [("force", gt, 0.0, f_min, 0.0), ("force", gb, 0.0, -f_min, 0.0)],
+                    solver=capi.SOLVER_FATIGUE_STATIC, tangent=capi.TANGENT_SYMMETRIC, **OPTS)
+    assert r["status"] == 0
+    return g, fixed + [("force", gt, 0.0, 1.0, 0.0), ("force", gb, 0.0, -1.0, 0.0)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,tau", [(pkg.fatigue.LINEAR, 0.001), (pkg.fatigue.EXPONENTIAL, 0.5)])
+def test_cyclic_driver_in_library_matches_per_cycle_calls(mode, tau):
+    """lpm_fatigue_run (the spectrum on the device, the cycle loop inside
+    the library) against the same loop driven from Python with one
+    lpm_fatigue_cycle call per cycle: identical records and identical
+    positions, damage and state, bit for bit, for the linear time map
+    (dN/dt = 1000) and the exponential one (dN/dt = int(exp(t/tau)/tau) =
+    2, 14, 109 for tau = 0.5)."""
+    spectrum = pkg.fatigue.ca_spectrum(F_MAX, R_RATIO, 3000)
+    # a spectrum whose amplitude varies, so the per-cycle loads differ
+    spectrum = [v * (1.0 + 0.1 * math.sin(0.37 * k)) for k, v in enumerate(spectrum)]
+    ga, unit_a = _ct_gpu()
+    gb, unit_b = _ct_gpu()
+    ra = pkg.fatigue.run_cycles(ga, unit_a, spectrum, 2, tau, mode=mode, max_calls=3, tangent=capi.TANGENT_SYMMETRIC,
+                                **OPTS)
+    rb = pkg.fatigue.run_cycles_per_call(gb, unit_b, spectrum, 2, tau, mode=mode, max_calls=3,
+                                         tangent=capi.TANGENT_SYMMETRIC, **OPTS)
+    assert len(ra) == len(rb) == 3
+    for a, b in zip(ra, rb):
+        for k in ("N", "dNdt", "newton_iters", "cg_iters", "unconverged_steps", "new_damage"):
+            assert a[k] == b[k], k
+    for fld in (capi.F_XYZ, capi.F_DAMAGE, capi.F_PEX):
+        assert np.array_equal(ga.download(fld), gb.download(fld)), fld
+    assert np.array_equal(ga.state(), gb.state())
+    with pytest.raises(capi.LpmError) as e:
+        ga.fatigue_run(unit_a, spectrum[:-1], 1, tau)  # an even count of spectrum values
+    assert e.value.code == capi.ERR_ARG
+    ga.close()
+    gb.close()
