@@ -33,7 +33,11 @@ Reported (one JSON line on rank 0):
                softening bond law and damage rounds at full size
                (configuration 3); minutes, so not in the default run
   j2_sensitivity  cost of carrying d/d(yield stress) and d/d(hardening)
-               through J2 load steps of a BCC polycrystal
+               through J2 load steps of a BCC polycrystal (40^3 cells)
+  polycrystal  configuration 4 at full size (BCC 60^3 cells, 20 grains):
+               bounded loading and unloading steps past yield, without and
+               with the two tangent directions
+  matrix_free  the mixed load step with the tangent applied from bond data
 
 --impl reference times complete CPU oracle load steps of the same workload.
 Multi-GPU runs are independent replicas (the path has no exchange step).
@@ -96,6 +100,25 @@ def workload(n, a=0.2, E=200e3, nu=0.3):
 def describe(w):
     return "SC %d^3 lattice (%d particles, %d bonds), a=0.2 mm, E=200 GPa, nu=0.3, clamped base, top +%g mm/step" % (
         round(len(w["xyz"]) ** (1 / 3)), len(w["xyz"]), len(w["p1"]), ARGS.du)
+
+
+T_START = time.perf_counter()
+
+
+def run_leg(line, key, fn, *a, **k):
+    """One optional bench leg: its result under `key`, or the error it
+    raised (an extra leg never takes the headline line down with it)."""
+    progress(key)
+    try:
+        line[key] = fn(*a, **k)
+    except Exception as e:  # noqa: BLE001 - reported in the line
+        line[key] = {"error": "%s: %s" % (type(e).__name__, e)}
+
+
+def progress(what):
+    """One line on stderr per bench leg, with the elapsed time."""
+    sys.stderr.write("[bench %7.1f s] %s\n" % (time.perf_counter() - T_START, what))
+    sys.stderr.flush()
 
 
 # ------------------------------------------------------------- clocks
@@ -496,6 +519,88 @@ def j2_sensitivity_cost(capi, local, ncell=40, steps=4):
             "tangent_cg_iters_per_step": out["with"][1], "plastic": plastic}
 
 
+def polycrystal_cost(capi, local, ncell=60, plastic_steps=6, unload_steps=3):
+    """Configuration 4 at full size: a BCC polycrystal of 60^3 cells (0.2 mm)
+    with 20 Voronoi grains of uniform SO(3) orientations (seeded), J2 law
+    with E = 110 GPa, nu = 0.34, yield 900 MPa, linear isotropic hardening
+    1 GPa, uniaxial tension in z at 2 % strain over 100 steps and unloading
+    over 20.  Untimed steps of 0.1 % take the lattice to 0.7 % strain;
+    then `plastic_steps` loading steps of 0.02 % and `unload_steps`
+    unloading steps of 0.1 % are timed, without and with the two tangent
+    directions (d/d yield stress, d/d hardening modulus) carried along.
+    Mixed precision, BC elimination.  Device time with CUDA events."""
+    import math
+    import torch
+    import __graft_entry__ as ge
+    lat = ge.load_package().lattice
+    t0 = time.perf_counter()
+    xyz, gid = lat.bcc_polycrystal(ncell, 0.2, 20, 11)
+    cell = lat.UnitCell(lat.BCC3D, 0.2 * math.sqrt(3.0) / 4.0)
+    keep = np.arange(len(xyz))
+    while True:  # drop particles with fewer than 6 bonds (lattice.prune_weak, searched on the GPU)
+        q1, _, _ = capi.find_bonds(xyz[keep], cell)
+        ok = np.bincount(q1, minlength=len(keep)) >= 6
+        if ok.all():
+            break
+        keep = keep[ok]
+    xyz = xyz[keep]
+    p1, p2, layer = capi.find_bonds(xyz, cell)
+    Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(110e3, 0.34, layout="row"))
+    setup_s = time.perf_counter() - t0
+    progress("polycrystal: %d particles set up" % len(xyz))
+    z = xyz[:, 2]
+    bottom, top = np.where(z < 0.1)[0], np.where(z > z.max() - 0.1)[0]
+    L = z.max() - z.min()
+    du = 0.02 * L / 100
+    out = {}
+    for tangent in (False, True):
+        g = capi.Lattice(3, xyz, p1, p2, layer, Kn, Tv, cell.particle_volume, cell.nneighbors)
+        g.set_law(capi.LAW_J2, [110e3, 0.34, 900.0, 0.0, 1e3, 0.0, 0.0])
+        g.update()
+        gb, gt = g.add_group(bottom), g.add_group(top)
+        fixed = [("disp", gb, 0, 0.0), ("disp", gb, 1, 0.0), ("disp", gb, 2, 0.0)]
+        opts = dict(solver=capi.SOLVER_FATIGUE_STATIC, tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_MIXED,
+                    max_iter=30, tol=1e-5, cg_tol=1e-10, max_cuts=2)
+        for _ in range(7):
+            r = g.load_step(fixed + [("disp", gt, 2, 0.001 * L)], **opts)
+            if r["status"] != 0:
+                raise RuntimeError("polycrystal elastic step did not converge: %s" % r)
+        progress("polycrystal: elastic steps, last %s" % r)
+        if tangent:
+            g.tangent_begin([[0, 0, 1, 0, 0, 0, 0], [0, 0, 0, 0, 1, 0, 0]], tol=1e-10)
+        stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
+        times, cgs = [], []
+        for n_steps, inc in ((plastic_steps, du), (unload_steps, -5 * du)):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            g.synchronize()
+            e0.record(stream)
+            its = 0
+            for _ in range(n_steps):
+                r = g.load_step(fixed + [("disp", gt, 2, inc)], **opts)
+                if r["status"] != 0:
+                    raise RuntimeError("polycrystal step did not converge: %s" % r)
+                its += r["cg_iters"]
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / n_steps)
+            cgs.append(its / n_steps)
+            progress("polycrystal: %d steps, %.1f ms each, tangents %s" % (n_steps, times[-1], tangent))
+        plastic = bool(np.abs(g.download(capi.B_DLP)).max() > 0)
+        out[tangent] = (times, cgs, plastic)
+        g.close()
+    (tl, tu), (cl, cu), plastic = out[False]
+    (sl, su), _, _ = out[True]
+    return {"workload": "BCC polycrystal %d^3 cells, 20 grains (%d particles, %d bonds), J2, tension to 2 %% in 100 "
+                        "steps, unloading in 20" % (ncell, len(xyz), len(p1)),
+            "loading_ms_per_step": tl, "unloading_ms_per_step": tu, "loading_cg_iters_per_step": cl,
+            "unloading_cg_iters_per_step": cu, "steps_per_s_loading": 1e3 / tl, "plastic": plastic,
+            "with_tangents_loading_ms_per_step": sl, "with_tangents_unloading_ms_per_step": su,
+            "tangent_cost_relative": (sl + su) / (tl + tu), "timed_steps": [plastic_steps, unload_steps],
+            "full_history_estimate_s": (100 * tl + 20 * tu) / 1e3, "setup_s": setup_s,
+            "directions": "d/d(yield stress), d/d(hardening modulus)", "precision": "mixed"}
+
+
 def force_bytes(nb, n):
     """Algorithmic bytes of one force pass: per directed bond the partner
     index, dis0, dLp, bdamage, Kn, Tv and the bond force written; per
@@ -712,6 +817,7 @@ def run_gb300(args):
     for prec in order:
         if prec == capi.PREC_MIXED:
             clocks.start()
+        progress("load steps, %s" % ("mixed" if prec == capi.PREC_MIXED else "FP64"))
         results[prec] = gpu_run(w, args, prec, world, local)
         if prec == capi.PREC_MIXED:
             clk = clocks.stop()
@@ -765,6 +871,7 @@ def run_gb300(args):
                         "mixed_speedup": value / fv}
         f["handle"].close()
     if not args.no_matrix_free:
+        progress("load steps, matrix-free")
         mf = gpu_run(w, args, capi.PREC_MIXED, world, local, operator=capi.OPERATOR_MATRIX_FREE)
         mv, tm = aggregate(mf["ms"] / 1e3, args.steps, world)
         kt = mf["ktime"]
@@ -785,6 +892,7 @@ def run_gb300(args):
         if rank == 0:
             print(json.dumps(line), flush=True)
         return 0
+    progress("adjoint")
     adj = adjoint_cost(g, capi, w, args.cg_tol, local)
     line["adjoint"] = dict(adj, relative_to_forward_step=adj["ms"] / (t_mixed * 1e3 / args.steps))
     fa = force_assembly_rate(g, capi, 5, local)
@@ -794,14 +902,17 @@ def run_gb300(args):
                            "force_ms": fa["force"], "assembly_ms": fa["assembly"], "directed_bonds": nb,
                            "force_achieved_gbs": fb / (fa["force"] * 1e-3) / 1e9,
                            "force_algorithmic_bytes": fb}
-    line["setup"] = setup_cost(w, capi)
-    line["fatigue"] = fatigue_cost(capi, local)
+    run_leg(line, "setup", setup_cost, w, capi)
+    run_leg(line, "fatigue", fatigue_cost, capi, local)
     if args.softening:
-        line["softening"] = softening_cost(capi, local)
-    line["j2_sensitivity"] = j2_sensitivity_cost(capi, local)
+        run_leg(line, "softening", softening_cost, capi, local)
+    run_leg(line, "j2_sensitivity", j2_sensitivity_cost, capi, local)
+    run_leg(line, "polycrystal", polycrystal_cost, capi, local)
     g.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        progress("CPU baseline and parity")
         line["parity"], line["cpu_baseline"] = headline_parity(w, args, capi)
+    progress("done")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
