@@ -560,7 +560,7 @@ def polycrystal_cost(capi, local, ncell=60, plastic_steps=6, unload_steps=3):
         gb, gt = g.add_group(bottom), g.add_group(top)
         fixed = [("disp", gb, 0, 0.0), ("disp", gb, 1, 0.0), ("disp", gb, 2, 0.0)]
         opts = dict(solver=capi.SOLVER_FATIGUE_STATIC, tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_MIXED,
-                    max_iter=30, tol=1e-5, cg_tol=1e-10, max_cuts=2)
+                    max_iter=30, tol=1e-5, cg_tol=1e-10, cg_maxit=20000, max_cuts=2)
         for _ in range(7):
             r = g.load_step(fixed + [("disp", gt, 2, 0.001 * L)], **opts)
             if r["status"] != 0:

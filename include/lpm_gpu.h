@@ -416,6 +416,24 @@ int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y);
 #define LPM_T_XYZ 2 /* n x dim: d x / d theta at the step's equilibrium */
 int lpm_tangent_begin(lpm_handle* h, int ndir, const double* dparams, double tol);
 int lpm_tangent_bond_constants(lpm_handle* h, int dir, const double* dKn, const double* dTv);
+/* Softening law (LPM_LAW_SOFTENING, configuration 3's damage): the same
+ * forward-mode tangents follow the damage history instead of holding it
+ * fixed.  dparams may be NULL (the law's alpha is not a direction); a
+ * direction changes the bond constants (lpm_tangent_bond_constants, e.g.
+ * dKn = Kn/E, dTv = Tv/E for d/dE) and/or the per-bond critical stretch
+ * (lpm_tangent_bond_scrit: d s_c per directed bond, stored order, e.g.
+ * s_c/lambda for the scale lambda of the Weibull draws).  Each damage round
+ * of lpm_load_step (LPM_SOLVER_STATIC_ELIMINATE; solver_static.h:107-136)
+ * then solves the equilibrium's change on the exact Jacobian of the
+ * partially damaged state, which is not symmetric (BiCGSTAB with its exact
+ * diagonal), and differentiates the damage update that follows: the
+ * largest stretch kappa = max(kappa, s) where s sets it, and
+ * d = D(kappa, s_c) where d rises.  LPM_T_PIN after a step is the change of
+ * the internal forces at the step's final equilibrium, so a reaction's
+ * derivative is their sum over the constrained group; the peak reaction's
+ * is that of the step where it peaks.  The derivative is that of the
+ * discrete algorithm (rounds, thresholds) at fixed round counts. */
+int lpm_tangent_bond_scrit(lpm_handle* h, int dir, const double* dscrit);
 int lpm_tangent_get(const lpm_handle* h, int dir, int field, double* dst);
 int lpm_tangent_end(lpm_handle* h);
 

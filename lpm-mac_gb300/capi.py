@@ -150,6 +150,7 @@ def load(build_if_needed=True):
         "lpm_tangent_begin": [H, ctypes.c_int, dp, ctypes.c_double],
         "lpm_tangent_bond_constants": [H, ctypes.c_int, dp, dp],
         "lpm_tangent_get": [H, ctypes.c_int, ctypes.c_int, dp],
+        "lpm_tangent_bond_scrit": [H, ctypes.c_int, dp],
         "lpm_tangent_end": [H],
         "lpm_checkpoint_save": [H, ip],
         "lpm_checkpoint_restore": [H, ctypes.c_int],
@@ -176,7 +177,8 @@ def exported_symbols():
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
             "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
             "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_fatigue_run", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
-            "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_bond_constants", "lpm_tangent_get",
+            "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_bond_constants", "lpm_tangent_bond_scrit",
+            "lpm_tangent_get",
             "lpm_tangent_end"]
 
 
@@ -556,6 +558,23 @@ class Lattice:
             dkn = np.ascontiguousarray(np.asarray(db[0], dtype=np.float64)[self.bond_perm])
             dtv = np.ascontiguousarray(np.asarray(db[1], dtype=np.float64)[self.bond_perm])
             self._check(self._L.lpm_tangent_bond_constants(self.h, k, _d(dkn), _d(dtv)))
+
+    def tangent_begin_softening(self, directions, tol=1e-12):
+        """Tangents through the softening law's damage history (configuration
+        3): one dict per direction with optional "dKn", "dTv" (changes of
+        the bond constants) and "dscrit" (change of the critical stretch),
+        each an array per directed bond in stored order (the order of
+        download and of B_SCRIT uploads)."""
+        null = ctypes.POINTER(ctypes.c_double)()
+        self._check(self._L.lpm_tangent_begin(self.h, len(directions), null, float(tol)))
+        for k, dr in enumerate(directions):
+            if dr.get("dKn") is not None:
+                dkn = np.ascontiguousarray(dr["dKn"], dtype=np.float64)
+                dtv = np.ascontiguousarray(dr.get("dTv", np.zeros(self.nb)), dtype=np.float64)
+                self._check(self._L.lpm_tangent_bond_constants(self.h, k, _d(dkn), _d(dtv)))
+            if dr.get("dscrit") is not None:
+                dsc = np.ascontiguousarray(dr["dscrit"], dtype=np.float64)
+                self._check(self._L.lpm_tangent_bond_scrit(self.h, k, _d(dsc)))
 
     def tangent_get(self, direction, field=T_PIN):
         """The step's d Pin (T_PIN) or d x (T_XYZ) along one direction, (N, dim)."""

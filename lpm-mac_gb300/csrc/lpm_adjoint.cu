@@ -296,6 +296,77 @@ __global__ void k_dfk_slots(int n, const int64_t* __restrict__ bptr, const int* 
   }
 }
 
+// The bond force's change from changes of the bond constants (optional)
+// and of the bond damage, in the sliced layout, for the softening law:
+//   d f_b = w_b (2 dKn_b dLe_b + 2 dTv_b D_i^l) - d d_b (2 Kn_b dLe_b + 2 Tv_b D_i^l)
+// (f_b = (1 - d_b)(2 Kn dLe + 2 Tv D); broken bonds 0).
+__global__ void k_dfs_slots(int n, const int64_t* __restrict__ bptr, const int* __restrict__ slot_of,
+                            const int* __restrict__ blayer, const double* __restrict__ bdamage,
+                            const double* __restrict__ dLe, const double* __restrict__ dle_tot,
+                            const double* __restrict__ Kn, const double* __restrict__ Tv,
+                            const double* __restrict__ dkn, const double* __restrict__ dtv,
+                            const double* __restrict__ dd, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    if (is_broken(bdamage[b])) {
+      out[slot_of[b]] = 0.0;
+      continue;
+    }
+    const double D = dle_tot[NL * i + blayer[b]];
+    double v = -dd[b] * 2.0 * (Kn[b] * dLe[b] + Tv[b] * D);
+    if (dkn) v += 2.0 * (1.0 - bdamage[b]) * (dkn[b] * dLe[b] + dtv[b] * D);
+    out[slot_of[b]] = v;
+  }
+}
+
+// Tangent of the softening law's damage update (k_softening_damage), run
+// just before it on the same state: kappa = max(kappa, s) with
+// s = (dis - dis0)/dis0, d = D(kappa, s_c) when that raises d, where
+//   D = alpha/(alpha - 1) - alpha s_c / ((alpha - 1) kappa)   (s_c < kappa < alpha s_c),
+// 0 below s_c and 1 from alpha s_c.  With dx the equilibrium's change:
+//   d s = c_b . (dx_i - dx_j) / dis0,  d kappa = d s where s sets kappa,
+//   d d = dD/dkappa d kappa + dD/ds_c d s_c where d rises,
+// otherwise both keep their previous tangents.
+__global__ void k_soft_tangent(int n, int dim, const int64_t* __restrict__ bptr, const int* __restrict__ bp2,
+                               const int* __restrict__ ptype, int undamaged, const double* __restrict__ pp, int np,
+                               const double* __restrict__ dis, const double* __restrict__ dis0,
+                               const double* __restrict__ cs, const double* __restrict__ bcrit,
+                               const double* __restrict__ bkappa, const double* __restrict__ bdamage,
+                               const double* __restrict__ dx, const double* __restrict__ dsc,
+                               double* __restrict__ dkappa, double* __restrict__ dd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || ptype[i] == undamaged) return;
+  const double alpha = pp[(int64_t)i * np];
+  double ui[3];
+  load_v(dx, dim, i, ui);
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    if (is_broken(bdamage[b])) continue;  // stays broken: its tangents no longer matter
+    const double s = (dis[b] - dis0[b]) / dis0[b];
+    double uj[3];
+    load_v(dx, dim, bp2[b], uj);
+    const double ds = (cs[3 * b] * (ui[0] - uj[0]) + cs[3 * b + 1] * (ui[1] - uj[1]) +
+                       cs[3 * b + 2] * (ui[2] - uj[2])) / dis0[b];
+    const double kold = bkappa[b];
+    const double k = fmax(kold, s);
+    if (s > kold) dkappa[b] = ds;
+    const double sc = bcrit[b];
+    double d = 0.0;
+    if (k >= alpha * sc)
+      d = 1.0;
+    else if (k > sc)
+      d = 1.0 - (sc / k) * (alpha * sc - k) / ((alpha - 1.0) * sc);
+    if (d > bdamage[b]) {
+      if (k >= alpha * sc || !(k > sc)) {
+        dd[b] = 0.0;
+      } else {
+        const double a1 = alpha / (alpha - 1.0);
+        dd[b] = a1 * sc / (k * k) * dkappa[b] - a1 / k * (dsc ? dsc[b] : 0.0);
+      }
+    }
+  }
+}
+
 // g = -q on the free DOFs, 0 on the constrained ones.
 __global__ void k_tg_rhs(int n, int dim, const double* __restrict__ q, const int* __restrict__ mask,
                          double* __restrict__ g) {
@@ -555,6 +626,194 @@ static int jacobian_cg(lpm_handle* h, const double* g, double* x, double tol, lo
   return LPM_OK;
 }
 
+// BiCGSTAB (van der Vorst, SIAM J. Sci. Stat. Comput. 13 (1992)) for the
+// non-symmetric H_ff of a partially damaged state, right-preconditioned by
+// H's exact diagonal; the vector work of one iteration in three kernels.
+__global__ void k_dot2(int64_t m, const double* __restrict__ a, const double* __restrict__ b,
+                       const double* __restrict__ c, const double* __restrict__ e, double* partials,
+                       unsigned int* ticket, double* out) {
+  double v[2] = {0.0, 0.0};
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+    v[0] += a[t] * b[t];
+    v[1] += c[t] * e[t];
+  }
+  double tot[2];
+  if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
+    out[0] = tot[0];
+    out[1] = tot[1];
+  }
+}
+
+// p = r + beta (p - omega v), phat = M p
+__global__ void k_bicg_p(int64_t m, const double* __restrict__ r, const double* __restrict__ v,
+                         const double* __restrict__ invd, double beta, double omega, double* __restrict__ p,
+                         double* __restrict__ phat) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const double pt = r[t] + beta * (p[t] - omega * v[t]);
+  p[t] = pt;
+  phat[t] = invd[t] * pt;
+}
+
+// s = r - alpha v, shat = M s
+__global__ void k_bicg_s(int64_t m, const double* __restrict__ r, const double* __restrict__ v,
+                         const double* __restrict__ invd, double alpha, double* __restrict__ sv,
+                         double* __restrict__ shat) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const double st = r[t] - alpha * v[t];
+  sv[t] = st;
+  shat[t] = invd[t] * st;
+}
+
+// x += alpha phat + omega shat, r = s - omega t
+__global__ void k_bicg_xr(int64_t m, const double* __restrict__ phat, const double* __restrict__ shat,
+                          const double* __restrict__ sv, const double* __restrict__ tv, double alpha, double omega,
+                          double* __restrict__ x, double* __restrict__ r) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  x[t] += alpha * phat[t] + omega * shat[t];
+  r[t] = sv[t] - omega * tv[t];
+}
+
+// H_ff x = g (g zero on the constrained DOFs) by right-preconditioned
+// BiCGSTAB on the exact Jacobian at the prepared state.
+static int jacobian_bicgstab(lpm_handle* h, const double* g, double* x, double tol, long long maxit,
+                             long long* iters, double* relres) {
+  Dev& d = h->d;
+  const int dim = h->dim;
+  const int64_t m = (int64_t)h->n * dim;
+  if (!d.tg_bicg) {
+    d.tg_bicg = (double*)dev_alloc(h, sizeof(double) * (size_t)(7 * m + 2));
+    if (!d.tg_bicg) return LPM_ERR_NOMEM;
+  }
+  double *r = d.tg_bicg, *rh = r + m, *p = rh + m, *ph = p + m, *v = ph + m, *sv = v + m, *sh = sv + m,
+         *dots = sh + m;
+  double* tv = d.adj_q;  // t = H shat
+  k_jac_invdiag<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, dim, d.bptr, d.blayer, d.opp, d.cs, d.dis,
+                                                            d.bdamage, d.bforce, d.Kn, d.Tv, d.mask, d.adj_invd);
+  LPM_LAUNCHED(h, "k_jac_invdiag");
+  if (maxit < 0) maxit = 2LL * m;
+  const int GV = grid_for(m, 256, kMaxRedBlocks), T = 256, GE = grid_for(m, T);
+  LPM_CUDA(h, cudaMemsetAsync(x, 0, sizeof(double) * m, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(p, 0, sizeof(double) * m, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(v, 0, sizeof(double) * m, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(r, g, sizeof(double) * m, cudaMemcpyDeviceToDevice, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(rh, g, sizeof(double) * m, cudaMemcpyDeviceToDevice, h->stream));
+  auto dot2 = [&](const double* a, const double* b, const double* c, const double* e, double out[2]) -> int {
+    k_dot2<<<GV, 256, 0, h->stream>>>(m, a, b, c, e, d.red.partials, d.red.ticket + 9, dots);
+    LPM_LAUNCHED(h, "k_dot2");
+    LPM_CUDA(h, cudaMemcpyAsync(h->h_norms, dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+    out[0] = h->h_norms[0];
+    out[1] = h->h_norms[1];
+    return LPM_OK;
+  };
+  double q[2];
+  int st = dot2(g, g, rh, r, q);
+  if (st) return st;
+  const double bnorm = sqrt(q[0]);
+  double rho = 1.0, alpha = 1.0, omega = 1.0, rho_new = q[1], rn = bnorm;
+  long long it = 0;
+  if (!std::isfinite(bnorm)) {
+    h->err = "tangent: non-finite right-hand side";
+    return LPM_ERR_NONFINITE;
+  }
+  while (bnorm > 0.0 && rn > tol * bnorm && it < maxit) {
+    if (rho_new == 0.0 || omega == 0.0) break;  // breakdown: reported as not converged
+    const double beta = (rho_new / rho) * (alpha / omega);
+    k_bicg_p<<<GE, T, 0, h->stream>>>(m, r, v, d.adj_invd, it == 0 ? 0.0 : beta, omega, p, ph);
+    LPM_LAUNCHED(h, "k_bicg_p");
+    st = apply_jacobian(h, ph, v, true, nullptr);
+    if (st) return st;
+    st = dot2(rh, v, rh, v, q);
+    if (st) return st;
+    alpha = rho_new / q[0];
+    k_bicg_s<<<GE, T, 0, h->stream>>>(m, r, v, d.adj_invd, alpha, sv, sh);
+    LPM_LAUNCHED(h, "k_bicg_s");
+    st = apply_jacobian(h, sh, tv, true, nullptr);
+    if (st) return st;
+    st = dot2(tv, sv, tv, tv, q);
+    if (st) return st;
+    omega = q[1] > 0.0 ? q[0] / q[1] : 0.0;
+    k_bicg_xr<<<GE, T, 0, h->stream>>>(m, ph, sh, sv, tv, alpha, omega, x, r);
+    LPM_LAUNCHED(h, "k_bicg_xr");
+    rho = rho_new;
+    st = dot2(r, r, rh, r, q);
+    if (st) return st;
+    rn = sqrt(q[0]);
+    rho_new = q[1];
+    ++it;
+    if (!std::isfinite(rn)) {
+      h->err = "tangent: non-finite value in BiCGSTAB";
+      return LPM_ERR_NONFINITE;
+    }
+  }
+  if (iters) *iters = it;
+  *relres = bnorm > 0.0 ? rn / bnorm : 0.0;
+  return LPM_OK;
+}
+
+// One round of the softening law's tangent (called after the round's
+// Newton, before its damage update): for each direction, the equilibrium's
+// change H_ff dx_f = -(dPin/d(d) . dd + dPin/d(Kn, Tv) . d(Kn, Tv))_f with
+// H the exact, non-symmetric Jacobian of the partially damaged state, then
+// dPin there; and the tangent of the damage update that follows.
+static int tangent_soft_round(lpm_handle* h) {
+  Dev& d = h->d;
+  const int dim = h->dim, n = h->n;
+  const int64_t m = (int64_t)n * dim;
+  const size_t B = (size_t)std::max<int64_t>(h->nb, 1);
+  int st = jacobian_prepare(h);
+  if (st) return st;
+  if (!d.tg_jdk) {
+    d.tg_jdl = (double*)zeros_dev(h, sizeof(double) * (size_t)std::max<int64_t>(h->jslots, 1));
+    d.tg_jdk = (double*)zeros_dev(h, sizeof(double) * (size_t)std::max<int64_t>(h->jslots, 1));
+    if (!d.tg_jdl || !d.tg_jdk) return LPM_ERR_NOMEM;
+  }
+  LPM_CUDA(h, cudaMemsetAsync(d.adj_a, 0, sizeof(double) * m, h->stream));
+  for (int k = 0; k < h->tg_ndir; ++k) {
+    double* tx = d.tg_x + (size_t)k * m;
+    double* tpin = d.tg_pin + (size_t)k * m;
+    k_dfs_slots<<<grid_for(n, 128), 128, 0, h->stream>>>(n, d.bptr, d.jslot_of, d.blayer, d.bdamage, d.dLe,
+                                                        d.dle_tot, d.Kn, d.Tv, h->tg_bond ? d.tg_dkn + k * B : nullptr,
+                                                        h->tg_bond ? d.tg_dtv + k * B : nullptr, d.tg_dd + k * B,
+                                                        d.tg_jdk);
+    LPM_LAUNCHED(h, "k_dfs_slots");
+    st = apply_jacobian(h, d.adj_a, d.adj_c, false, nullptr, nullptr, d.tg_jdk);
+    if (st) return st;
+    k_tg_rhs<<<grid_for(m, 256), 256, 0, h->stream>>>(n, dim, d.adj_c, d.mask, d.adj_g);
+    LPM_LAUNCHED(h, "k_tg_rhs");
+    long long it = 0;
+    double rr = 0.0;
+    st = jacobian_bicgstab(h, d.adj_g, tx, h->tg_tol, -1, &it, &rr);
+    if (st) return st;
+    h->stats.tangent_cg_iters += it;
+    if (!(rr <= h->tg_tol)) {
+      h->err = "tangent: the equilibrium change did not converge";
+      return LPM_NOT_CONVERGED;
+    }
+    st = apply_jacobian(h, tx, tpin, false, nullptr, nullptr, d.tg_jdk);
+    if (st) return st;
+  }
+  return LPM_OK;
+}
+
+// The damage update's tangent (before k_softening_damage changes the state).
+int tangent_soft_damage(lpm_handle* h) {
+  Dev& d = h->d;
+  const int n = h->n;
+  const int64_t m = (int64_t)n * h->dim;
+  const size_t B = (size_t)std::max<int64_t>(h->nb, 1);
+  for (int k = 0; k < h->tg_ndir; ++k) {
+    k_soft_tangent<<<grid_for(n, 128), 128, 0, h->stream>>>(
+        n, h->dim, d.bptr, d.bp2, d.ptype, h->undamaged, d.pp, h->law_np, d.dis, d.dis0, d.cs, d.bcrit, d.bkappa,
+        d.bdamage, d.tg_x + (size_t)k * m, d.tg_dsc + k * B, d.tg_dkappa + k * B, d.tg_dd + k * B);
+    LPM_LAUNCHED(h, "k_soft_tangent");
+  }
+  return LPM_OK;
+}
+
 // 1 in the adjoint flag (and LPM_ERR_STATE) when some bond is partially or
 // one-sidedly damaged: the Jacobian is then not symmetric.
 static int check_symmetric_damage(lpm_handle* h) {
@@ -610,13 +869,18 @@ int adjoint_step(lpm_handle* h, const double* a_dev, const double* c_dev, double
 // ------------------------------------------------ tangent-linear sensitivity
 int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double tol) {
   Dev& d = h->d;
-  if (ndir < 0 || (ndir > 0 && !dparams_host) || !(tol > 0.0)) {
+  if (ndir < 0 || !(tol > 0.0)) {
     h->err = "tangent: bad arguments";
     return LPM_ERR_ARG;
   }
-  if (ndir > 0 && (h->law != 2 || !d.pp || !d.state)) {
-    h->err = "tangent: the J2 law (lpm_set_law 2) is required";
+  const bool soft = h->law == LPM_LAW_SOFTENING;
+  if (ndir > 0 && ((h->law != 2 && !soft) || !d.pp || !d.state || (soft && (!d.bcrit || !d.bkappa)))) {
+    h->err = "tangent: the J2 law (lpm_set_law 2) or the softening law (lpm_set_law 4) is required";
     return LPM_ERR_STATE;
+  }
+  if (ndir > 0 && !soft && !dparams_host) {
+    h->err = "tangent: NULL parameter directions";
+    return LPM_ERR_ARG;
   }
 
   if (ndir > h->tg_cap) {  // buffers for ndir directions (smaller ones stay owned by the handle)
@@ -629,7 +893,11 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
     d.tg_stress = (double*)dev_alloc(h, sizeof(double) * 6 * N);
     d.tg_dkn = (double*)dev_alloc(h, sizeof(double) * ndir * B);
     d.tg_dtv = (double*)dev_alloc(h, sizeof(double) * ndir * B);
-    if (!d.tg_dlp || !d.tg_sv || !d.tg_x || !d.tg_pin || !d.tg_dp || !d.tg_stress || !d.tg_dkn || !d.tg_dtv)
+    d.tg_dd = (double*)dev_alloc(h, sizeof(double) * ndir * B);
+    d.tg_dkappa = (double*)dev_alloc(h, sizeof(double) * ndir * B);
+    d.tg_dsc = (double*)dev_alloc(h, sizeof(double) * ndir * B);
+    if (!d.tg_dlp || !d.tg_sv || !d.tg_x || !d.tg_pin || !d.tg_dp || !d.tg_stress || !d.tg_dkn || !d.tg_dtv ||
+        !d.tg_dd || !d.tg_dkappa || !d.tg_dsc)
       return LPM_ERR_NOMEM;
     h->tg_cap = ndir;
   }
@@ -642,8 +910,14 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
   LPM_CUDA(h, cudaMemsetAsync(d.tg_pin, 0, sizeof(double) * ndir * m, h->stream));
   LPM_CUDA(h, cudaMemsetAsync(d.tg_dkn, 0, sizeof(double) * ndir * B, h->stream));
   LPM_CUDA(h, cudaMemsetAsync(d.tg_dtv, 0, sizeof(double) * ndir * B, h->stream));
-  LPM_CUDA(h, cudaMemcpyAsync(d.tg_dp, dparams_host, sizeof(double) * ndir * N * h->law_np, cudaMemcpyHostToDevice,
-                              h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_dd, 0, sizeof(double) * ndir * B, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_dkappa, 0, sizeof(double) * ndir * B, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_dsc, 0, sizeof(double) * ndir * B, h->stream));
+  if (dparams_host)
+    LPM_CUDA(h, cudaMemcpyAsync(d.tg_dp, dparams_host, sizeof(double) * ndir * N * h->law_np, cudaMemcpyHostToDevice,
+                                h->stream));
+  else
+    LPM_CUDA(h, cudaMemsetAsync(d.tg_dp, 0, sizeof(double) * ndir * N * h->law_np, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   h->tg_ndir = ndir;
   h->tg_tol = tol;
@@ -667,6 +941,19 @@ int tangent_bond_constants(lpm_handle* h, int dir, const double* dkn_host, const
   return LPM_OK;
 }
 
+int tangent_bond_scrit(lpm_handle* h, int dir, const double* dsc_host) {
+  Dev& d = h->d;
+  if (dir < 0 || dir >= h->tg_ndir || !dsc_host || h->law != LPM_LAW_SOFTENING) {
+    h->err = "tangent: bad direction, NULL critical-stretch changes, or not the softening law";
+    return LPM_ERR_ARG;
+  }
+  const size_t B = (size_t)std::max<int64_t>(h->nb, 1);
+  LPM_CUDA(h, cudaMemcpyAsync(d.tg_dsc + (size_t)dir * B, dsc_host, sizeof(double) * h->nb, cudaMemcpyHostToDevice,
+                              h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return LPM_OK;
+}
+
 // One converged step's tangents (called after Newton, before the state
 // update): for each direction, the equilibrium's change, the changes of
 // Pin and of the stress there, then the differentiated J2 return.
@@ -676,6 +963,7 @@ int tangent_step(lpm_handle* h) {
   const int64_t m = (int64_t)n * dim;
   int st = adjoint_buffers(h);
   if (st) return st;
+  if (h->law == LPM_LAW_SOFTENING) return tangent_soft_round(h);
   st = check_symmetric_damage(h);
   if (st) return st;
   st = jacobian_prepare(h);

@@ -670,7 +670,7 @@ int lpm_load_step(lpm_handle* h, const lpm_bc* bcs, int nbc, const lpm_step_opts
         if (st) return st;
         st = lpm_store_state(h);
         if (st) return st;
-        if (damaged && h->tg_ndir > 0) {
+        if (damaged && h->tg_ndir > 0 && h->law != LPM_LAW_SOFTENING) {
           h->err = "tangent sensitivity holds the damage fixed: a damage round ended the step";
           return LPM_ERR_STATE;
         }
@@ -964,6 +964,11 @@ int lpm_tangent_begin(lpm_handle* h, int ndir, const double* dparams, double tol
 int lpm_tangent_bond_constants(lpm_handle* h, int dir, const double* dKn, const double* dTv) {
   if (!h) return LPM_ERR_ARG;
   return tangent_bond_constants(h, dir, dKn, dTv);
+}
+
+int lpm_tangent_bond_scrit(lpm_handle* h, int dir, const double* dscrit) {
+  if (!h) return LPM_ERR_ARG;
+  return tangent_bond_scrit(h, dir, dscrit);
 }
 
 int lpm_tangent_get(const lpm_handle* h, int dir, int field, double* dst) {

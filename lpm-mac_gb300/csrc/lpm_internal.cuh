@@ -173,6 +173,11 @@ struct Dev {
   // sliced bond layout are scratch
   double *tg_dlp, *tg_sv, *tg_x, *tg_pin, *tg_dp, *tg_stress, *tg_jdl;
   double *tg_dkn, *tg_dtv, *tg_jdk;  // per direction d Kn, d Tv [nb]; the force change in sliced layout
+  // softening law: per direction the tangents of the bond damage and of the
+  // largest stretch, and the direction's change of the critical stretch
+  // [nb each]; BiCGSTAB work vectors (the partially damaged Jacobian is not
+  // symmetric)
+  double *tg_dd, *tg_dkappa, *tg_dsc, *tg_bicg;
 };
 
 // One device-resident copy of a step's state (lpm_checkpoint_save).
@@ -282,6 +287,8 @@ int adjoint_step(lpm_handle* h, const double* a, const double* c, double tol, lo
 int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double tol);
 int tangent_step(lpm_handle* h);
 int tangent_bond_constants(lpm_handle* h, int dir, const double* dkn_host, const double* dtv_host);
+int tangent_bond_scrit(lpm_handle* h, int dir, const double* dsc_host);
+int tangent_soft_damage(lpm_handle* h);
 int checkpoint_save(lpm_handle* h, int* id);
 int checkpoint_restore(lpm_handle* h, int id);
 int checkpoint_drop(lpm_handle* h, int id);

@@ -274,6 +274,10 @@ int launch_static_damage(lpm_handle* h, int* any_new) {
     LPM_LAUNCHED(h, "k_static_damage");
   }
   if (h->law == LPM_LAW_SOFTENING) {
+    if (h->tg_ndir > 0) {  // the update's tangent reads the state before it
+      const int st = tangent_soft_damage(h);
+      if (st) return st;
+    }
     const Dev& d = h->d;
     k_softening_damage<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.bptr, d.ptype, h->undamaged, d.pp, h->law_np,
                                                                d.dis, d.dis0, d.bcrit, d.bkappa, d.bdamage, flag);

@@ -73,3 +73,73 @@ def test_sent_softening_steps_match_oracle(precision, operator):
         assert abs(R_g - R_o) <= tol_u * abs(R_o)
     assert damaged_steps >= 2
     g.close()
+
+
+def _sent_run(args, sc, scale_k, scale_sc, steps, tangents=False):
+    """The notched plate pulled `steps` times with the constants and the
+    critical stretches scaled; per step the top reaction, the damage rounds
+    and the damaged-bond pattern, and with `tangents` the reaction's
+    derivatives along d/d(log E) and d/d(log lambda)."""
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = args
+    g = make_gpu(dim, xyz, p1, p2, layer, Kn * scale_k, Tv * scale_k, cell)
+    g.set_law(capi.LAW_SOFTENING, [3.0, 1.0e-3])
+    g.upload(capi.B_SCRIT, sc * scale_sc)
+    g.update()
+    c = xyz[:, 1]
+    bottom, top = np.where(c < c.min() + 1e-9)[0], np.where(c > c.max() - 1e-9)[0]
+    gb, gc, gt = g.add_group(bottom), g.add_group(bottom[:1]), g.add_group(top)
+    bcs = [("disp", gb, 1, 0.0), ("disp", gc, 0, 0.0), ("disp", gt, 1, 2.5e-4)]
+    if tangents:
+        kn = g.download(capi.B_KN)
+        tv = g.download(capi.B_TV)
+        g.tangent_begin_softening([{"dKn": kn, "dTv": tv}, {"dscrit": g.download(capi.B_SCRIT)}], tol=1e-12)
+    out = []
+    for _ in range(steps):
+        r = g.load_step(bcs, solver=capi.SOLVER_STATIC_ELIMINATE, tangent=capi.TANGENT_SYMMETRIC,
+                        precision=capi.PREC_FP64, max_iter=400, tol=1e-10, cg_tol=1e-13, max_cuts=0)
+        assert r["status"] == 0 and r["cuts"] == 0, r
+        R = g.download(capi.F_PIN)[top, 1].sum()
+        rec = dict(R=R, rounds=r["damage_rounds"], damaged=g.download(capi.B_BDAMAGE) > 0)
+        if tangents:
+            rec["dR"] = [g.tangent_get(k, capi.T_PIN)[top, 1].sum() for k in range(2)]
+        out.append(rec)
+    if tangents:
+        g.tangent_end()
+    g.close()
+    return out
+
+
+@pytest.mark.gpu
+def test_softening_reaction_tangents_match_central_differences():
+    """Configuration-3 sensitivities: the top reaction of each load step of
+    the notched plate, differentiated along log E (all bond constants) and
+    along log lambda (the scale of the Weibull critical stretches), by the
+    forward-mode tangents that follow the damage rounds, against central
+    differences of whole forward runs (h = 1e-4 relative, Newton to 1e-10).  Compared over
+    the steps before any change of the discrete path (the damage rounds and
+    the set of damaged bonds are the same in the base and both perturbed
+    runs); at least one compared step must have softened bonds.  The peak
+    reaction's derivative is that of the step where it peaks."""
+    args, sc = setup()
+    steps, h = 6, 1e-4
+    base = _sent_run(args, sc, 1.0, 1.0, steps, tangents=True)
+    runs = {(k, sgn): _sent_run(args, sc, *((1 + sgn * h, 1.0) if k == 0 else (1.0, 1 + sgn * h)), steps)
+            for k in range(2) for sgn in (1, -1)}
+    compared, softened = 0, 0
+    for t in range(steps):
+        same = all(runs[k, s][t]["rounds"] == base[t]["rounds"] and
+                   np.array_equal(runs[k, s][t]["damaged"], base[t]["damaged"]) for k in range(2) for s in (1, -1))
+        if not same:
+            break
+        for k in range(2):
+            fd = (runs[k, 1][t]["R"] - runs[k, -1][t]["R"]) / (2 * h)
+            tg = base[t]["dR"][k]
+            err = abs(tg - fd) / max(abs(fd), 1e-12 * abs(base[t]["R"]))
+            print("[softening tangent] step %d dir %d: tangent %.9e FD %.9e rel %.2e rounds %d damaged %d" % (
+                t, k, tg, fd, err, base[t]["rounds"], int(base[t]["damaged"].sum())))
+            assert err <= 1e-5, (t, k)
+        compared += 1
+        softened += bool(base[t]["damaged"].any())
+    assert compared >= 3 and softened >= 1, (compared, softened)
+    t_peak = int(np.argmax([b["R"] for b in base[:compared]]))
+    assert base[t_peak]["dR"][0] != 0.0
