@@ -414,6 +414,7 @@ int lpm_apply_jacobian(lpm_handle* h, const double* v, double* y);
  * load step that cuts back fails with LPM_ERR_STATE. */
 #define LPM_T_PIN 1 /* n x dim: d Pin / d theta at the step's equilibrium */
 #define LPM_T_XYZ 2 /* n x dim: d x / d theta at the step's equilibrium */
+#define LPM_T_DAMAGE 3 /* n: d damage / d theta of each particle (HCF law) */
 int lpm_tangent_begin(lpm_handle* h, int ndir, const double* dparams, double tol);
 int lpm_tangent_bond_constants(lpm_handle* h, int dir, const double* dKn, const double* dTv);
 /* Softening law (LPM_LAW_SOFTENING, configuration 3's damage): the same
@@ -434,6 +435,21 @@ int lpm_tangent_bond_constants(lpm_handle* h, int dir, const double* dKn, const 
  * is that of the step where it peaks.  The derivative is that of the
  * discrete algorithm (rounds, thresholds) at fixed round counts. */
 int lpm_tangent_bond_scrit(lpm_handle* h, int dir, const double* dscrit);
+/* HCF fatigue law (LPM_LAW_FATIGUE_HCF, configuration 5): dparams gives
+ * each direction's change of the per-particle {A, B, d, threshold} (e.g. A
+ * in column 0 for d/d(log A) scaling, 1 in column 1 for d/dB).  Through the
+ * cycles of lpm_fatigue_cycle / lpm_fatigue_run the tangents follow each
+ * step's equilibrium (the partially damaged Jacobian, BiCGSTAB), the strain
+ * energy's history (U_min, U_max, U_hist of particle_fatigue_hcf.h:127-145,
+ * with the branch each takes), the local rate A U_hist^B (U_max - U_min)^d,
+ * its nonlocal average with position-dependent weights
+ * (solver_fatigue.h:79-116), the damage update with the cycle jump
+ * (particle_fatigue_hcf.h:147-160) and the bond damage the force pass raises
+ * to the larger particle damage.  LPM_T_DAMAGE gives d damage / d theta per
+ * particle, so a crack-length measure sum_i w_i D_i (e.g. the damage along
+ * the ligament times the spacing) has the derivative sum_i w_i dD_i.  The
+ * tangents ride along with the forward run: no checkpoint or recompute is
+ * needed for a few parameters. */
 int lpm_tangent_get(const lpm_handle* h, int dir, int field, double* dst);
 int lpm_tangent_end(lpm_handle* h);
 

@@ -24,7 +24,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 BC_DISP, BC_FORCE = 0, 1
 SOLVER_STATIC, SOLVER_FATIGUE_STATIC, SOLVER_STATIC_ELIMINATE = 0, 1, 2
 LAW_ELASTIC, LAW_DAMAGE, LAW_J2, LAW_FATIGUE_HCF, LAW_SOFTENING = 0, 1, 2, 3, 4
-T_PIN, T_XYZ = 1, 2  # tangent fields (lpm_tangent_get)
+T_PIN, T_XYZ, T_DAMAGE = 1, 2, 3  # tangent fields (lpm_tangent_get)
 OPERATOR_ASSEMBLED, OPERATOR_MATRIX_FREE = 0, 1
 _NSTATE = {LAW_ELASTIC: 1, LAW_DAMAGE: 1, LAW_J2: 7, LAW_FATIGUE_HCF: 3, LAW_SOFTENING: 1}
 
@@ -577,7 +577,12 @@ class Lattice:
                 self._check(self._L.lpm_tangent_bond_scrit(self.h, k, _d(dsc)))
 
     def tangent_get(self, direction, field=T_PIN):
-        """The step's d Pin (T_PIN) or d x (T_XYZ) along one direction, (N, dim)."""
+        """The step's d Pin (T_PIN) or d x (T_XYZ) along one direction, (N, dim);
+        T_DAMAGE: d damage per particle (N,)."""
+        if field == T_DAMAGE:
+            y = np.zeros(self.n)
+            self._check(self._L.lpm_tangent_get(self.h, int(direction), int(field), _d(y)))
+            return y
         y = np.zeros(self.ndof)
         self._check(self._L.lpm_tangent_get(self.h, int(direction), int(field), _d(y)))
         return y.reshape(self.n, self.dim)

@@ -873,9 +873,10 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
     h->err = "tangent: bad arguments";
     return LPM_ERR_ARG;
   }
-  const bool soft = h->law == LPM_LAW_SOFTENING;
-  if (ndir > 0 && ((h->law != 2 && !soft) || !d.pp || !d.state || (soft && (!d.bcrit || !d.bkappa)))) {
-    h->err = "tangent: the J2 law (lpm_set_law 2) or the softening law (lpm_set_law 4) is required";
+  const bool soft = h->law == LPM_LAW_SOFTENING, hcf = h->law == LPM_LAW_FATIGUE_HCF;
+  if (ndir > 0 && ((h->law != 2 && !soft && !hcf) || !d.pp || !d.state || (soft && (!d.bcrit || !d.bkappa)) ||
+                   (hcf && !d.nl_ptr))) {
+    h->err = "tangent: the J2 law (2), the HCF law with nonlocal neighbours (3) or the softening law (4) is required";
     return LPM_ERR_STATE;
   }
   if (ndir > 0 && !soft && !dparams_host) {
@@ -896,8 +897,11 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
     d.tg_dd = (double*)dev_alloc(h, sizeof(double) * ndir * B);
     d.tg_dkappa = (double*)dev_alloc(h, sizeof(double) * ndir * B);
     d.tg_dsc = (double*)dev_alloc(h, sizeof(double) * ndir * B);
+    d.tg_dD = (double*)dev_alloc(h, sizeof(double) * ndir * N);
+    d.tg_ddot = (double*)dev_alloc(h, sizeof(double) * ndir * N);
+    d.tg_dnl = (double*)dev_alloc(h, sizeof(double) * ndir * N);
     if (!d.tg_dlp || !d.tg_sv || !d.tg_x || !d.tg_pin || !d.tg_dp || !d.tg_stress || !d.tg_dkn || !d.tg_dtv ||
-        !d.tg_dd || !d.tg_dkappa || !d.tg_dsc)
+        !d.tg_dd || !d.tg_dkappa || !d.tg_dsc || !d.tg_dD || !d.tg_ddot || !d.tg_dnl)
       return LPM_ERR_NOMEM;
     h->tg_cap = ndir;
   }
@@ -913,6 +917,9 @@ int tangent_begin(lpm_handle* h, int ndir, const double* dparams_host, double to
   LPM_CUDA(h, cudaMemsetAsync(d.tg_dd, 0, sizeof(double) * ndir * B, h->stream));
   LPM_CUDA(h, cudaMemsetAsync(d.tg_dkappa, 0, sizeof(double) * ndir * B, h->stream));
   LPM_CUDA(h, cudaMemsetAsync(d.tg_dsc, 0, sizeof(double) * ndir * B, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_dD, 0, sizeof(double) * ndir * N, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_ddot, 0, sizeof(double) * ndir * N, h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.tg_dnl, 0, sizeof(double) * ndir * N, h->stream));
   if (dparams_host)
     LPM_CUDA(h, cudaMemcpyAsync(d.tg_dp, dparams_host, sizeof(double) * ndir * N * h->law_np, cudaMemcpyHostToDevice,
                                 h->stream));
@@ -964,6 +971,11 @@ int tangent_step(lpm_handle* h) {
   int st = adjoint_buffers(h);
   if (st) return st;
   if (h->law == LPM_LAW_SOFTENING) return tangent_soft_round(h);
+  if (h->law == LPM_LAW_FATIGUE_HCF) {  // equilibrium with the damage's tangent, then the state update's
+    st = tangent_soft_round(h);
+    if (st) return st;
+    return tangent_hcf_state(h);
+  }
   st = check_symmetric_damage(h);
   if (st) return st;
   st = jacobian_prepare(h);

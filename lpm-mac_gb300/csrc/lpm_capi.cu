@@ -972,8 +972,16 @@ int lpm_tangent_bond_scrit(lpm_handle* h, int dir, const double* dscrit) {
 }
 
 int lpm_tangent_get(const lpm_handle* h, int dir, int field, double* dst) {
-  if (!h || !dst || dir < 0 || dir >= h->tg_ndir || (field != LPM_T_PIN && field != LPM_T_XYZ)) return LPM_ERR_ARG;
+  if (!h || !dst || dir < 0 || dir >= h->tg_ndir || (field != LPM_T_PIN && field != LPM_T_XYZ &&
+                                                     field != LPM_T_DAMAGE))
+    return LPM_ERR_ARG;
   lpm_handle* hh = const_cast<lpm_handle*>(h);
+  if (field == LPM_T_DAMAGE) {
+    LPM_CUDA(hh, cudaMemcpyAsync(dst, h->d.tg_dD + (size_t)dir * h->n, sizeof(double) * h->n,
+                                 cudaMemcpyDeviceToHost, h->stream));
+    LPM_CUDA(hh, cudaStreamSynchronize(h->stream));
+    return LPM_OK;
+  }
   const size_t m = (size_t)h->n * h->dim;
   const double* src = (field == LPM_T_PIN ? h->d.tg_pin : h->d.tg_x) + (size_t)dir * m;
   LPM_CUDA(hh, cudaMemcpyAsync(dst, src, sizeof(double) * m, cudaMemcpyDeviceToHost, h->stream));

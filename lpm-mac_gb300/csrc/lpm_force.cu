@@ -312,6 +312,10 @@ int launch_mean_state0(lpm_handle* h, double* out_dev) {
 }
 
 int launch_geometry_force(lpm_handle* h) {
+  if (h->tg_ndir > 0 && h->law == LPM_LAW_FATIGUE_HCF) {  // the bond damage's tangent reads it before the pass
+    const int st = tangent_hcf_bdamage(h);
+    if (st) return st;
+  }
   const Dev& d = h->d;
   const int T = 128;
   k_geometry_force<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.x, d.bptr, d.bp2, d.blayer, d.dis0, d.dLp,

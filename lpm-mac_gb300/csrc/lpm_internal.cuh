@@ -178,6 +178,9 @@ struct Dev {
   // [nb each]; BiCGSTAB work vectors (the partially damaged Jacobian is not
   // symmetric)
   double *tg_dd, *tg_dkappa, *tg_dsc, *tg_bicg;
+  // HCF law: per direction the tangents of the particle damage, of the
+  // local and of the nonlocal damage rate [n each]
+  double *tg_dD, *tg_ddot, *tg_dnl;
 };
 
 // One device-resident copy of a step's state (lpm_checkpoint_save).
@@ -289,6 +292,8 @@ int tangent_step(lpm_handle* h);
 int tangent_bond_constants(lpm_handle* h, int dir, const double* dkn_host, const double* dtv_host);
 int tangent_bond_scrit(lpm_handle* h, int dir, const double* dsc_host);
 int tangent_soft_damage(lpm_handle* h);
+int tangent_hcf_state(lpm_handle* h);
+int tangent_hcf_bdamage(lpm_handle* h);
 int checkpoint_save(lpm_handle* h, int* id);
 int checkpoint_restore(lpm_handle* h, int id);
 int checkpoint_drop(lpm_handle* h, int id);

@@ -8,6 +8,7 @@
 //   law 2 ParticleJ2Plasticity   params {E, mu, sigmay, xi, H, A, damage_threshold}
 //   law 3 ParticleFatigueHCF     params {A, B, d, damage_threshold}
 //   law 4 softening bond law     params {alpha, s_c} (per-bond s_c in bcrit)
+#include <algorithm>
 #include <climits>
 
 #include "lpm_device.cuh"
@@ -21,7 +22,7 @@ struct LawView {
   int nneighbors;
   const int64_t *bptr, *lptr;
   const int *bp2, *blayer, *nbonds, *ptype;
-  const double *Kn, *dLe, *dis, *cs, *dle_tot, *tdle_tot, *stress, *pp, *x, *nonlocal_L;
+  const double *Kn, *Tv, *dLe, *dis, *cs, *dle_tot, *tdle_tot, *stress, *pp, *x, *nonlocal_L;
   double *dLp, *state, *ddot_local, *ddot_nl, *damage, *bdamage;
   const double *state_last, *damage_last, *bstrain, *crit;
   const int64_t* nl_ptr;
@@ -191,6 +192,133 @@ __global__ void k_fatigue_damage(LawView v, double dt, int* any) {
   if (fabs(d - v.damage_last[i]) > 1e-3) atomicOr(any, 1);
 }
 
+// ---- forward-mode tangents of the HCF law (lpm_tangent_begin with law 3)
+// Per direction: dx the step's equilibrium change, dp the parameter
+// directions [n][np], tsv the state tangents [n][3] (U_hist, U_min, U_max),
+// tdd the local rate's tangent, tdnl the nonlocal rate's, tdD the damage's.
+
+__device__ __forceinline__ void load_dv(const double* __restrict__ v, int dim, int i, double (&o)[3]) {
+  o[0] = v[(int64_t)dim * i];
+  o[1] = v[(int64_t)dim * i + 1];
+  o[2] = dim == 3 ? v[(int64_t)dim * i + 2] : 0.0;
+}
+
+// Tangent of ParticleFatigueHCF::updateParticleStateVariables (k_update_state,
+// law 3), run before it on the same state.  U = sum Kn dLe^2/(2 Vm) +
+// sum_l T_l D_l/(2 Vm) with d dLe = c . (dx_i - dx_j); U_min, U_max, U_hist
+// follow the branch the update takes; the local rate
+// A U_hist^B (U_max - U_min)^d is differentiated along A, B, d and the states.
+__global__ void k_hcf_tangent_state(LawView v, int dim, const double* __restrict__ dx,
+                                    const double* __restrict__ dp, double* __restrict__ tsv,
+                                    double* __restrict__ tdd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n) return;
+  const double Vm = v.pvol * v.nbonds[i] / v.nneighbors;
+  double ui[3];
+  load_dv(dx, dim, i, ui);
+  double dU = 0.0;
+  for (int l = 0; l < NL; ++l) {
+    const int64_t b0 = l == 0 ? v.bptr[i] : v.lptr[i], b1 = l == 0 ? v.lptr[i] : v.bptr[i + 1];
+    double dD = 0.0, dT = 0.0;
+    for (int64_t b = b0; b < b1; ++b) {
+      double uj[3];
+      load_dv(dx, dim, v.bp2[b], uj);
+      const double de = v.cs[3 * b] * (ui[0] - uj[0]) + v.cs[3 * b + 1] * (ui[1] - uj[1]) +
+                        v.cs[3 * b + 2] * (ui[2] - uj[2]);
+      dU += v.Kn[b] * v.dLe[b] * de / Vm;
+      dD += de;
+      dT += v.Tv[b] * de;
+    }
+    dU += 0.5 * (dT * v.dle_tot[NL * i + l] + v.tdle_tot[NL * i + l] * dD) / Vm;
+  }
+  const double u = strain_energy(v, i);
+  const double* sv = v.state + (int64_t)i * v.ns;
+  double* ts = tsv + (int64_t)i * v.ns;
+  if (u < sv[1]) ts[1] = dU;
+  if (u > sv[2]) ts[2] = dU;
+  const double umin = fmin(u, sv[1]), umax = fmax(u, sv[2]);
+  if (umax > sv[0]) ts[0] = ts[2];
+  const double uh = fmax(umax, sv[0]);
+  const double* P = v.pp + (int64_t)i * v.np;
+  const double* dP = dp + (int64_t)i * v.np;
+  const double r = umax - umin;
+  if (r > 0) {
+    const double A = P[0], B = P[1], d = P[2];
+    const double g = pow(uh, B) * pow(r, d);
+    const double dg = g * (log(uh) * dP[1] + B * ts[0] / uh + log(r) * dP[2] + d * (ts[2] - ts[1]) / r);
+    tdd[i] = dP[0] * g + A * dg;
+  } else {
+    tdd[i] = 0.0;
+  }
+}
+
+// Tangent of the nonlocal rate (k_nonlocal_rate) at the same positions:
+// weights w_ij = phi(r_ij, L) Vm_j move with the positions,
+// d r = (x_i - x_j).(dx_i - dx_j)/r, d phi/d r = -16 t^7 g^3 / L (t = r/L, g = 1/(1+t^8)).
+__global__ void k_hcf_tangent_nonlocal(LawView v, int dim, const double* __restrict__ dx,
+                                       const double* __restrict__ tdd, double* __restrict__ tdnl) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n || v.ptype[i] == v.undamaged) return;
+  double A = 0.0, D = 0.0, dA = 0.0, dD = 0.0;
+  const double x0 = v.x[3 * i], x1 = v.x[3 * i + 1], x2 = v.x[3 * i + 2];
+  double ui[3];
+  load_dv(dx, dim, i, ui);
+  const double L = v.nonlocal_L[i];
+  for (int64_t q = v.nl_ptr[i]; q < v.nl_ptr[i + 1]; ++q) {
+    const int j = v.nl_idx[q];
+    if (v.ptype[j] == v.undamaged) continue;
+    const double ex = x0 - v.x[3 * j], ey = x1 - v.x[3 * j + 1], ez = x2 - v.x[3 * j + 2];
+    const double rr = bond_length(ex, ey, ez);
+    const double vm = v.pvol * v.nbonds[j] / v.nneighbors;
+    const double w = phi(rr, L) * vm;
+    double dw = 0.0;
+    if (rr > 0.0) {
+      double uj[3];
+      load_dv(dx, dim, j, uj);
+      const double dr = (ex * (ui[0] - uj[0]) + ey * (ui[1] - uj[1]) + ez * (ui[2] - uj[2])) / rr;
+      const double t = rr / L, t2 = t * t, t4 = t2 * t2, t7 = t4 * t2 * t;
+      const double g = 1 / (1 + t4 * t4);
+      dw = -16.0 * t7 * g * g * g / L * dr * vm;
+    }
+    D += v.ddot_local[j] * w;
+    dD += tdd[j] * w + v.ddot_local[j] * dw;
+    A += w;
+    dA += dw;
+  }
+  tdnl[i] = (dD - (D / A) * dA) / A;
+}
+
+// Tangent of ParticleFatigueHCF::updateParticleFatigueDamage (k_fatigue_damage),
+// run before it: D += Ddot_nl dt unless it reaches the threshold (then 1);
+// the reset U_min, U_max are constants.
+__global__ void k_hcf_tangent_damage(LawView v, double dt, const double* __restrict__ tdnl, double* __restrict__ tdD,
+                                     double* __restrict__ tsv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v.n || v.ptype[i] == v.undamaged) return;
+  const double thr = v.pp[(int64_t)i * v.np + 3];
+  const double d = v.damage[i] + v.ddot_nl[i] * dt;
+  tdD[i] = d >= thr ? 0.0 : tdD[i] + tdnl[i] * dt;
+  tsv[(int64_t)i * v.ns + 1] = 0.0;
+  tsv[(int64_t)i * v.ns + 2] = 0.0;
+}
+
+// Tangent of the bond damage the force pass raises to the larger particle
+// damage (bdamage = max(bdamage, D_i, D_j), particle_fatigue_hcf.h:74),
+// run before the force pass.
+__global__ void k_hcf_tangent_bdamage(int n, const int64_t* __restrict__ bptr, const int* __restrict__ bp2,
+                                      const double* __restrict__ bdamage, const double* __restrict__ damage,
+                                      const double* __restrict__ tdD, double* __restrict__ tdd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double di = damage[i];
+  for (int64_t b = bptr[i]; b < bptr[i + 1]; ++b) {
+    const int j = bp2[b];
+    const double dj = damage[j];
+    const double m = fmax(di, dj);
+    if (m > bdamage[b]) tdd[b] = di >= dj ? tdD[i] : tdD[j];
+  }
+}
+
 LawView law_view(lpm_handle* h) {
   Dev& d = h->d;
   LawView v;
@@ -208,6 +336,7 @@ LawView law_view(lpm_handle* h) {
   v.nbonds = d.nbonds;
   v.ptype = d.ptype;
   v.Kn = d.Kn;
+  v.Tv = d.Tv;
   v.dLe = d.dLe;
   v.dis = d.dis;
   v.cs = d.cs;
@@ -241,6 +370,33 @@ int read_flag(lpm_handle* h, int* flag, int* out) {
 }
 
 }  // namespace
+
+// HCF tangents (lpm_tangent_begin with law 3), one launch per direction.
+int tangent_hcf_state(lpm_handle* h) {
+  const int T = 128;
+  const int64_t m = (int64_t)h->n * h->dim;
+  const LawView v = law_view(h);
+  Dev& d = h->d;
+  for (int k = 0; k < h->tg_ndir; ++k) {
+    k_hcf_tangent_state<<<grid_for(h->n, T), T, 0, h->stream>>>(
+        v, h->dim, d.tg_x + k * m, d.tg_dp + (int64_t)k * h->n * h->law_np, d.tg_sv + (int64_t)k * h->n * h->nstate,
+        d.tg_ddot + (int64_t)k * h->n);
+    LPM_LAUNCHED(h, "k_hcf_tangent_state");
+  }
+  return LPM_OK;
+}
+
+int tangent_hcf_bdamage(lpm_handle* h) {
+  const int T = 128;
+  Dev& d = h->d;
+  const size_t B = (size_t)std::max<int64_t>(h->nb, 1);
+  for (int k = 0; k < h->tg_ndir; ++k) {
+    k_hcf_tangent_bdamage<<<grid_for(h->n, T), T, 0, h->stream>>>(h->n, d.bptr, d.bp2, d.bdamage, d.damage,
+                                                                 d.tg_dD + (int64_t)k * h->n, d.tg_dd + k * B);
+    LPM_LAUNCHED(h, "k_hcf_tangent_bdamage");
+  }
+  return LPM_OK;
+}
 
 int launch_update_state(lpm_handle* h) {
   // with tangent directions on, their step comes first: it needs the state
@@ -298,6 +454,18 @@ int launch_fatigue_damage(lpm_handle* h, double dt, int* any_new) {
     const LawView v = law_view(h);
     k_nonlocal_rate<<<grid_for(h->n, T), T, 0, h->stream>>>(v);
     LPM_LAUNCHED(h, "k_nonlocal_rate");
+    const int64_t m = (int64_t)h->n * h->dim;
+    Dev& d = h->d;
+    for (int k = 0; k < h->tg_ndir; ++k) {  // tangents first: they read the state before the update
+      k_hcf_tangent_nonlocal<<<grid_for(h->n, T), T, 0, h->stream>>>(v, h->dim, d.tg_x + k * m,
+                                                                     d.tg_ddot + (int64_t)k * h->n,
+                                                                     d.tg_dnl + (int64_t)k * h->n);
+      LPM_LAUNCHED(h, "k_hcf_tangent_nonlocal");
+      k_hcf_tangent_damage<<<grid_for(h->n, T), T, 0, h->stream>>>(v, dt, d.tg_dnl + (int64_t)k * h->n,
+                                                                   d.tg_dD + (int64_t)k * h->n,
+                                                                   d.tg_sv + (int64_t)k * h->n * h->nstate);
+      LPM_LAUNCHED(h, "k_hcf_tangent_damage");
+    }
     k_fatigue_damage<<<grid_for(h->n, T), T, 0, h->stream>>>(v, dt, flag);
     LPM_LAUNCHED(h, "k_fatigue_damage");
   }

@@ -192,3 +192,70 @@ def test_cyclic_driver_in_library_matches_per_cycle_calls(mode, tau):
     assert e.value.code == capi.ERR_ARG
     ga.close()
     gb.close()
+
+
+def _ct_run(scale_a, shift_b, cycles, tangents=False):
+    """The CT plate at test size: a static step to f_min, then `cycles`
+    fatigue cycles (cycle jump 1000) through lpm_fatigue_run, with A scaled
+    and B shifted; returns the particle damage, and with `tangents` its
+    tangents along d/d(log A) and d/dB."""
+    args, info, groups, params, types, (nl_ptr, nl_idx, L) = ct_case()
+    p = params.copy()
+    p[:, 0] *= scale_a
+    p[:, 1] += shift_b
+    g = make_gpu(*args)
+    g.set_law(capi.LAW_FATIGUE_HCF, p)
+    g.set_types(types, 4)
+    g.set_nonlocal(nl_ptr, nl_idx, L)
+    g.update()
+    gm, gt, gb = g.add_group(groups["mid"]), g.add_group(groups["top"]), g.add_group(groups["bottom"])
+    fixed = [("disp", gm, 1, 0.0), ("disp", gt, 0, 0.0), ("disp", gb, 0, 0.0)]
+    opts = dict(tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_FP64, **OPTS)
+    f_min = R_RATIO * F_MAX
+    r = g.load_step(fixed + [("force", gt, 0.0, f_min, 0.0), ("force", gb, 0.0, -f_min, 0.0)],
+                    solver=capi.SOLVER_FATIGUE_STATIC, **opts)
+    assert r["status"] == 0, r
+    if tangents:
+        da = np.zeros_like(p)
+        da[:, 0] = p[:, 0]
+        db = np.zeros_like(p)
+        db[:, 1] = 1.0
+        g.tangent_begin([da, db], tol=1e-12)
+    unit = fixed + [("force", gt, 0.0, 1.0, 0.0), ("force", gb, 0.0, -1.0, 0.0)]
+    spectrum = pkg.fatigue.ca_spectrum(F_MAX, R_RATIO, 1000 * cycles)
+    recs = pkg.fatigue.run_cycles(g, unit, spectrum, 1, 0.001, **opts)
+    assert len(recs) == cycles and all(rc["status"] == 0 for rc in recs), recs
+    out = dict(D=g.download(capi.F_DAMAGE), info=info, xyz=args[1])
+    if tangents:
+        out["dD"] = [g.tangent_get(k, capi.T_DAMAGE) for k in range(2)]
+        g.tangent_end()
+    g.close()
+    return out
+
+
+@pytest.mark.gpu
+def test_crack_length_tangents_match_central_differences():
+    """Configuration-5 sensitivities: a crack-length measure after three
+    fatigue cycles, the damage summed along the ligament ahead of the notch
+    times the spacing, differentiated along log A and B (the two drawn HCF
+    parameters, all particles at once) by the forward-mode tangents that
+    follow the cycles, against central differences of whole runs
+    (h = 1e-3; Newton to 1e-9), within 1e-5.  The particle damage tangents
+    are checked too where the damage is above 1 % of its largest value."""
+    base = _ct_run(1.0, 0.0, 3, tangents=True)
+    xyz, info = base["xyz"], base["info"]
+    lig = (np.abs(xyz[:, 1] - info["crack_y"]) < SP) & (xyz[:, 0] > info["tip"][0])
+    crack = lambda D: SP * D[lig].sum()
+    assert crack(base["D"]) > 0
+    h = 1e-3
+    for k, (dA, dB) in enumerate([((1 + h, 0.0), (1 - h, 0.0)), ((1.0, h), (1.0, -h))]):
+        plus, minus = _ct_run(*dA, 3), _ct_run(*dB, 3)
+        fd = (crack(plus["D"]) - crack(minus["D"])) / (2 * h)
+        tg = SP * base["dD"][k][lig].sum()
+        err = abs(tg - fd) / abs(fd)
+        big = base["D"] > 0.01 * base["D"].max()
+        fdD = (plus["D"] - minus["D"]) / (2 * h)
+        errD = np.abs(base["dD"][k][big] - fdD[big]).max() / np.abs(fdD[big]).max()
+        print("[crack-length tangent] dir %d: tangent %.9e FD %.9e rel %.2e; damage field rel %.2e" % (
+            k, tg, fd, err, errD))
+        assert err <= 1e-5 and errD <= 1e-4, (k, err, errD)
