@@ -26,6 +26,7 @@ SOLVER_STATIC, SOLVER_FATIGUE_STATIC, SOLVER_STATIC_ELIMINATE = 0, 1, 2
 LAW_ELASTIC, LAW_DAMAGE, LAW_J2, LAW_FATIGUE_HCF, LAW_SOFTENING = 0, 1, 2, 3, 4
 T_PIN, T_XYZ, T_DAMAGE = 1, 2, 3  # tangent fields (lpm_tangent_get)
 OPERATOR_ASSEMBLED, OPERATOR_MATRIX_FREE = 0, 1
+CG_LOOP_AUTO, CG_LOOP_GRAPH, CG_LOOP_PERSISTENT = 0, 1, 2
 _NSTATE = {LAW_ELASTIC: 1, LAW_DAMAGE: 1, LAW_J2: 7, LAW_FATIGUE_HCF: 3, LAW_SOFTENING: 1}
 
 
@@ -40,7 +41,7 @@ class Stats(ctypes.Structure):
                 ("spmv_launches", ctypes.c_int64), ("spmv_ms", ctypes.c_double),
                 ("spmv32_launches", ctypes.c_int64), ("spmv32_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("mixed_fallbacks", ctypes.c_int64),
-                ("tangent_cg_iters", ctypes.c_int64)]
+                ("tangent_cg_iters", ctypes.c_int64), ("persistent_solves", ctypes.c_int64)]
 
 
 class BC(ctypes.Structure):
@@ -137,6 +138,7 @@ def load(build_if_needed=True):
         "lpm_get_stats": [H, ctypes.POINTER(Stats)],
         "lpm_reset_stats": [H],
         "lpm_set_kernel_timing": [H, ctypes.c_int],
+        "lpm_set_cg_loop": [H, ctypes.c_int],
         "lpm_get_stream": [H, ctypes.POINTER(ctypes.c_void_p)],
         "lpm_synchronize": [H],
         "lpm_find_bonds": [ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, i64, ip, ip, ip, i64p],
@@ -175,7 +177,7 @@ def exported_symbols():
             "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_set_operator",
             "lpm_apply_operator", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
-            "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_get_stream", "lpm_synchronize",
+            "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_set_cg_loop", "lpm_get_stream", "lpm_synchronize",
             "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_fatigue_run", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
             "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_bond_constants", "lpm_tangent_bond_scrit",
             "lpm_tangent_get",
@@ -504,6 +506,11 @@ class Lattice:
 
     def reset_stats(self):
         self._check(self._L.lpm_reset_stats(self.h))
+
+    def set_cg_loop(self, mode):
+        """CG_LOOP_AUTO (default), CG_LOOP_GRAPH or CG_LOOP_PERSISTENT: how the
+        mixed solve runs its iteration loop."""
+        self._check(self._L.lpm_set_cg_loop(self.h, int(mode)))
 
     def set_kernel_timing(self, on):
         self._check(self._L.lpm_set_kernel_timing(self.h, int(bool(on))))

@@ -238,7 +238,7 @@ int lpm_create(int dim, int n, int64_t nb, const double* xyz, const int* p1, con
        (d.invd64 = zeros_new<double>(h, ndof));
   ok = ok && (d.red.partials = zeros_new<double>(h, (size_t)kMaxRedBlocks * 4)) &&
        (d.red.ticket = zeros_new<unsigned int>(h, 16)) && (d.cg = zeros_new<CgScalars>(h, 1)) &&
-       (d.norms = zeros_new<double>(h, 8));
+       (d.norms = zeros_new<double>(h, 8)) && (d.gbar = zeros_new<unsigned long long>(h, 1));
   std::vector<double> crit(N, 1.0);
   ok = ok && (d.crit = upload_new(h, crit.data(), N)) && (d.pp = upload_new(h, crit.data(), N)) &&
        (d.ptype = zeros_new<int>(h, N)) && (d.state = zeros_new<double>(h, N)) &&
@@ -749,6 +749,14 @@ int lpm_get_stats(const lpm_handle* h, lpm_stats* st) {
 int lpm_reset_stats(lpm_handle* h) {
   if (!h) return LPM_ERR_ARG;
   h->stats = lpm_stats{};
+  return LPM_OK;
+}
+
+int lpm_set_cg_loop(lpm_handle* h, int mode) {
+  if (!h) return LPM_ERR_ARG;
+  if (mode != LPM_CG_LOOP_AUTO && mode != LPM_CG_LOOP_GRAPH && mode != LPM_CG_LOOP_PERSISTENT)
+    return arg_error(h, "unknown CG loop mode");
+  h->cg_loop = mode;
   return LPM_OK;
 }
 

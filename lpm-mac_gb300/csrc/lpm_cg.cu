@@ -99,6 +99,21 @@ __device__ __forceinline__ float op_load1(const float* a) {
   return __ldcs(a);
 }
 
+// A vector entry.  Kernels that never write the vector read it through the
+// read-only cache; the persistent solve (COH), whose blocks write the
+// vectors between grid barriers, reads them from L2 (ld.global.cg), which
+// the barrier's fences order after the writes.
+template <bool COH>
+__device__ __forceinline__ float ldv(const float* a) {
+  if (COH) return __ldcg(a);
+  return __ldg(a);
+}
+template <bool COH>
+__device__ __forceinline__ double ldv(const double* a) {
+  if (COH) return __ldcg(a);
+  return __ldg(a);
+}
+
 // y = row `row` of A times p (FP32), in difference form with compensated
 // accumulation: the sum comes out as if accumulated in twice the precision
 // and then rounded, so the only FP32 errors left are in the differences
@@ -108,7 +123,7 @@ __device__ __forceinline__ float op_load1(const float* a) {
 // at the row itself.  The blocks past the slice's groups (at most three) are
 // read one at a time, in the same order, so the sum is that of the blocks in
 // slot order either way.
-template <int DIM, bool OFF16, bool KEEP>
+template <int DIM, bool OFF16, bool KEEP, bool COH = false>
 __device__ __forceinline__ void row_product32(const SellView& v, const float* __restrict__ A,
                                               const float* __restrict__ p, int row, float (&y)[DIM],
                                               float (&ylo)[DIM]) {
@@ -117,7 +132,7 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
   for (int r = 0; r < DIM; ++r) sc[r] = cc[r] = 0.f;
   float pi[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) pi[k] = __ldg(&p[(int64_t)row * DIM + k]);
+  for (int k = 0; k < DIM; ++k) pi[k] = ldv<COH>(&p[(int64_t)row * DIM + k]);
   const int len = v.rowlen[row];
   const SellRow sr = sell_row(v.sell_ptr, row);
   const int ng = (min(len, sr.g4) + kVec - 1) / kVec;
@@ -135,7 +150,7 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
 #pragma unroll
     for (int t = 0; t < kVec; ++t)
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) pn[t][k] = __ldg(&p[(int64_t)comp(c40, t) * DIM + k]);
+      for (int k = 0; k < DIM; ++k) pn[t][k] = ldv<COH>(&p[(int64_t)comp(c40, t) * DIM + k]);
     if (ng > 1) c4n = group_cols<OFF16>(v, row, base + kSlice * kVec);
   }
   for (int g = 0; g < ng; ++g) {
@@ -154,7 +169,7 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
 #pragma unroll
       for (int t = 0; t < kVec; ++t)
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) pn[t][k] = __ldg(&p[(int64_t)comp(c4n, t) * DIM + k]);
+        for (int k = 0; k < DIM; ++k) pn[t][k] = ldv<COH>(&p[(int64_t)comp(c4n, t) * DIM + k]);
       if (g + 2 < ng) c4n = group_cols<OFF16>(v, row, s1 + kSlice * kVec);
     }
 #pragma unroll
@@ -173,7 +188,7 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
     const int c = OFF16 ? row + __ldg(&v.soff[st]) : __ldg(&v.scol[st]);
     float pc[DIM];
 #pragma unroll
-    for (int q = 0; q < DIM; ++q) pc[q] = __ldg(&p[(int64_t)c * DIM + q]) - pi[q];
+    for (int q = 0; q < DIM; ++q) pc[q] = ldv<COH>(&p[(int64_t)c * DIM + q]) - pi[q];
 #pragma unroll
     for (int r = 0; r < DIM; ++r)
 #pragma unroll
@@ -194,14 +209,14 @@ __device__ __forceinline__ void row_product32(const SellView& v, const float* __
 // The blocks past the slice's groups follow one at a time.
 // With ADD32 the product is taken of p + (p32 + p32lo) (an FP64 vector plus
 // a double-float increment not yet folded into it).
-template <int DIM, bool ADD32 = false>
+template <int DIM, bool ADD32 = false, bool COH = false>
 __device__ __forceinline__ double add_increment(const double* __restrict__ p, const float* __restrict__ p32,
                                                 const float* __restrict__ p32lo, int64_t i) {
-  if (ADD32) return __ldg(&p[i]) + ((double)__ldg(&p32[i]) + (double)__ldg(&p32lo[i]));
-  return __ldg(&p[i]);
+  if (ADD32) return ldv<COH>(&p[i]) + ((double)ldv<COH>(&p32[i]) + (double)ldv<COH>(&p32lo[i]));
+  return ldv<COH>(&p[i]);
 }
 
-template <int DIM, bool ADD32 = false>
+template <int DIM, bool ADD32 = false, bool COH = false>
 __device__ __forceinline__ void row_product(const SellView& v, const double* __restrict__ A,
                                             const double* __restrict__ p, int row, double (&y)[DIM],
                                             const float* __restrict__ p32 = nullptr,
@@ -220,7 +235,7 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
     for (int t = 0; t < kVec; ++t) {
       const int64_t c = (int64_t)comp(c4, t) * DIM;
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) pc[t][k] = add_increment<DIM, ADD32>(p, p32, p32lo, c + k);
+      for (int k = 0; k < DIM; ++k) pc[t][k] = add_increment<DIM, ADD32, COH>(p, p32, p32lo, c + k);
     }
 #pragma unroll
     for (int r = 0; r < DIM; ++r)
@@ -240,7 +255,7 @@ __device__ __forceinline__ void row_product(const SellView& v, const double* __r
     const int64_t c = (int64_t)__ldg(&v.scol[st]) * DIM;
     double pc[DIM];
 #pragma unroll
-    for (int q = 0; q < DIM; ++q) pc[q] = add_increment<DIM, ADD32>(p, p32, p32lo, c + q);
+    for (int q = 0; q < DIM; ++q) pc[q] = add_increment<DIM, ADD32, COH>(p, p32, p32lo, c + q);
 #pragma unroll
     for (int r = 0; r < DIM; ++r)
 #pragma unroll
@@ -374,6 +389,7 @@ __global__ void k_mx_init(int64_t ndof, const double* __restrict__ b, float* __r
     cg->it = 0;
     cg->maxit = maxit;
     cg->ru = 0;
+    cg->pfault = 0;
     cg->ru_count = 0;
     cg->graph_passes = 0;
     cg->zcoef = 1.0;
@@ -547,6 +563,319 @@ __global__ void __launch_bounds__(256) k_mx_pupdate(int64_t ndof, const float* _
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += (int64_t)gridDim.x * blockDim.x) {
     const float pi = p[i];
     p[i] = fmaf(bh, pi, fmaf(bl, pi, __fmul_rn(zc, __fmul_rn(invd[i], r[i]))));
+  }
+}
+
+// ---- the mixed solve as one persistent kernel ----------------------------
+// For systems that do not fill the GPU, the graph's three kernels per
+// iteration each cost a launch, a partly idle tail and a last-block fold,
+// together as much as the product itself on a 100k-particle plate.  Here the
+// blocks stay resident for the whole solve.  Every phase gives a thread the
+// same rows (the update and direction of a row's DOFs run on the thread that
+// took its product), so only p (read at the neighbours by the product) and
+// the solution (read at the neighbours by the FP64 residual) cross blocks,
+// and those reads go to L2.  Sums meet at grid barriers: each block
+// publishes its partial, waits, and folds all partials in block order, so
+// every block holds the same totals and takes the same branches.  The
+// recurrence, the reliable updates and the stopping rule are those of
+// k_mx_update, k_mx_residual, k_mx_replace and k_mx_pupdate.
+
+// Everything the persistent solve reads and writes.
+struct PcgMixed {
+  SellView v;
+  const float* A32;
+  const double* A64;
+  const double* b;     // right-hand side (unscaled)
+  const float* invd;
+  float *x, *xlo, *r, *rlo, *p, *q, *qlo;
+  double *x64, *r64;
+  CgScalars* cg;
+  double* partials;          // 6 x gridDim.x
+  unsigned long long* gbar;  // barrier arrivals, zero at launch
+  long long spin_limit;      // polls before a barrier wait gives up
+};
+
+// Polls before a grid-barrier wait gives up: at least 32 ns apart, so more
+// than half a second, against microseconds for a barrier that completes.
+constexpr long long kPcgSpinLimit = 1LL << 24;
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* a) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+  return v;
+}
+
+// Grid barrier on a monotone arrival count: the k-th barrier of a launch
+// waits until k * gridDim.x arrivals.  The fence before the arrival and the
+// acquire loads and fence after the wait order every block's writes before
+// the barrier ahead of every read after it.  The wait is bounded; returns
+// false in every thread of the block if it gave up.
+__device__ __forceinline__ bool grid_barrier(unsigned long long* gbar, unsigned long long target, long long limit) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(gbar, 1ULL);
+    int good = 1;
+    long long polls = 0;
+    while (ld_acquire_u64(gbar) < target) {
+      if (++polls > limit) {
+        good = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Grid totals of K values per block (valid in thread 0): published in slots
+// slot..slot+K-1 of the partials, then, after the barrier, folded by warp 0
+// of every block in block order and returned in every thread.
+template <int K>
+__device__ __forceinline__ bool grid_allreduce(const double (&v)[K], double* partials, int slot,
+                                               unsigned long long* gbar, unsigned long long& target, long long limit,
+                                               double (&tot)[K]) {
+  __shared__ double res[K];
+  const int G = gridDim.x;
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) partials[(int64_t)(slot + k) * G + blockIdx.x] = v[k];
+  target += (unsigned long long)G;
+  if (!grid_barrier(gbar, target, limit)) return false;
+  if (threadIdx.x < 32) {
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    for (int b = threadIdx.x; b < G; b += 32)
+#pragma unroll
+      for (int k = 0; k < K; ++k) acc[k] += __ldcg(&partials[(int64_t)(slot + k) * G + b]);
+    warp_sum<K>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < K; ++k) res[k] = acc[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) tot[k] = res[k];
+  return true;
+}
+
+// The block's copy of the solve's scalars: thread 0 updates it between
+// barriers, every thread reads it.
+struct PcgState {
+  double abs_new, rmax, threshold, bscale, rr;
+  long long it, maxit, ru_count, passes;
+  int done, ru;
+  float ah, al, bh, bl, zc;
+};
+
+// Register budget of the persistent kernel: that of the FP32 product.
+template <int DIM>
+constexpr int kPcgMinBlocks = DIM == 3 ? 2 : 3;
+
+template <int DIM, bool OFF16>
+__global__ void __launch_bounds__(256, kPcgMinBlocks<DIM>) k_mx_persistent(PcgMixed a) {
+  __shared__ PcgState s;
+  if (threadIdx.x == 0) {
+    const CgScalars* c = a.cg;
+    s.abs_new = c->abs_new;
+    s.rmax = c->rmax;
+    s.threshold = c->threshold;
+    s.bscale = c->bscale;
+    s.rr = c->rr;
+    s.it = c->it;
+    s.maxit = c->maxit;
+    s.ru_count = c->ru_count;
+    s.passes = 0;
+    s.done = c->done;
+    s.ru = 0;
+    s.ah = s.al = s.bh = s.bl = 0.f;
+    s.zc = 1.f;
+  }
+  __syncthreads();
+  const int n = a.v.n;
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long target = 0;
+  bool fault = false;
+  while (!s.done) {
+    // q = A p (FP32, double-float output) and p.q; alpha
+    {
+      float ps = 0.f, pc = 0.f;
+      for (int row = t0; row < n; row += stride) {
+        float y[DIM], yl[DIM];
+        row_product32<DIM, OFF16, true, true>(a.v, a.A32, a.p, row, y, yl);
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) {
+          const int64_t i = (int64_t)row * DIM + r;
+          const float pr = a.p[i];
+          a.q[i] = y[r];
+          a.qlo[i] = yl[r];
+          dot2_acc(ps, pc, pr, y[r]);
+          pc = fmaf(pr, yl[r], pc);
+        }
+      }
+      float s1[1] = {ps}, c1[1] = {pc};
+      double w[1] = {0.0}, tot[1];
+      block_df_sum<1>(s1, c1, w);
+      if (!grid_allreduce<1>(w, a.partials, 0, a.gbar, target, a.spin_limit, tot)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) df_split(s.abs_new / tot[0], s.ah, s.al);
+      __syncthreads();
+    }
+    // x += alpha p, r -= alpha q (double-float pairs), |r|^2 and r.z; then
+    // a reliable update is due, or beta
+    {
+      const float ah = s.ah, al = s.al;
+      float sb[2] = {0.f, 0.f}, cb[2] = {0.f, 0.f};
+      for (int row = t0; row < n; row += stride)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const int64_t i = (int64_t)row * DIM + c;
+          float rh = a.r[i], rl = a.rlo[i], xh = a.x[i], xl = a.xlo[i];
+          df_madd(rh, rl, -ah, -al, a.q[i], a.qlo[i]);
+          df_madd(xh, xl, ah, al, a.p[i], 0.f);
+          a.x[i] = xh;
+          a.xlo[i] = xl;
+          a.r[i] = rh;
+          a.rlo[i] = rl;
+          const float zi = a.invd[i] * rh;
+          dot2_acc(sb[0], cb[0], rh, rh);
+          cb[0] = fmaf(2.f * rh, rl, cb[0]);
+          dot2_acc(sb[1], cb[1], rh, zi);
+          cb[1] = fmaf(rl, zi, cb[1]);
+        }
+      double w[2] = {0.0, 0.0}, tot[2];
+      block_df_sum<2>(sb, cb, w);
+      if (!grid_allreduce<2>(w, a.partials, 1, a.gbar, target, a.spin_limit, tot)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) {
+        s.rr = tot[0];
+        s.it += 1;
+        if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+          s.done = 3;
+        } else {
+          const double rn = sqrt(tot[0]);
+          if (tot[0] < s.threshold || rn < kDelta * s.rmax) {
+            s.ru = 1;
+          } else {
+            s.rmax = fmax(s.rmax, rn);
+            const double beta = tot[1] / s.abs_new;
+            s.abs_new = tot[1];
+            df_split(beta, s.bh, s.bl);
+            s.zc = 1.f;
+          }
+          if (s.it >= s.maxit) s.done = 2;
+        }
+      }
+      __syncthreads();
+    }
+    if (s.done) break;
+    if (s.ru) {
+      // reliable update: r64 = s b - A64 (x64 + x) and |r64|^2
+      double acc[1] = {0.0}, tot[1];
+      const double sc = s.bscale;
+      for (int row = t0; row < n; row += stride) {
+        double y[DIM];
+        row_product<DIM, true, true>(a.v, a.A64, a.x64, row, y, a.x, a.xlo);
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const int64_t i = (int64_t)row * DIM + c;
+          const double ri = a.b[i] * sc - y[c];
+          a.r64[i] = ri;
+          acc[0] += ri * ri;
+        }
+      }
+      block_sum<1>(acc);
+      if (!grid_allreduce<1>(acc, a.partials, 3, a.gbar, target, a.spin_limit, tot)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) {
+        s.rr = tot[0];
+        s.ru_count += 1;
+        if (!isfinite(tot[0]))
+          s.done = 3;
+        else if (tot[0] < s.threshold)
+          s.done = 1;
+      }
+      __syncthreads();
+      if (s.done) break;
+      // x64 += x, x = 0, r = r64 as a pair; r.z and r.p give beta and the
+      // direction coefficient that restores r.p = 0 (as k_mx_replace)
+      double v[2] = {0.0, 0.0}, t2[2];
+      for (int row = t0; row < n; row += stride)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const int64_t i = (int64_t)row * DIM + c;
+          a.x64[i] += (double)a.x[i] + (double)a.xlo[i];
+          a.x[i] = 0.f;
+          a.xlo[i] = 0.f;
+          const double ri = a.r64[i];
+          float rh, rl;
+          df_split(ri, rh, rl);
+          a.r[i] = rh;
+          a.rlo[i] = rl;
+          v[0] += ri * (double)(a.invd[i] * rh);
+          v[1] += ri * (double)a.p[i];
+        }
+      block_sum<2>(v);
+      if (!grid_allreduce<2>(v, a.partials, 4, a.gbar, target, a.spin_limit, t2)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) {
+        const double old = s.abs_new;
+        s.abs_new = t2[0];
+        const double beta = t2[0] / old;
+        const double gamma = t2[0] != 0.0 ? t2[1] / t2[0] : 0.0;
+        df_split(beta, s.bh, s.bl);
+        s.zc = (float)(1.0 - beta * gamma);
+        s.rmax = sqrt(s.rr);
+        s.ru = 0;
+      }
+      __syncthreads();
+    }
+    // p = zc z + beta p with z = M^-1 r
+    {
+      const float bh = s.bh, bl = s.bl, zc = s.zc;
+      for (int row = t0; row < n; row += stride)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const int64_t i = (int64_t)row * DIM + c;
+          const float pi = a.p[i];
+          a.p[i] = fmaf(bh, pi, fmaf(bl, pi, __fmul_rn(zc, __fmul_rn(a.invd[i], a.r[i]))));
+        }
+      target += (unsigned long long)gridDim.x;
+      if (!grid_barrier(a.gbar, target, a.spin_limit)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) s.passes += 1;
+    }
+  }
+  if (fault) {
+    if (threadIdx.x == 0) atomicExch(&a.cg->pfault, 1);
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    CgScalars* c = a.cg;
+    c->done = s.done;
+    c->rr = s.rr;
+    c->it = s.it;
+    c->abs_new = s.abs_new;
+    c->rmax = s.rmax;
+    c->ru = s.ru;
+    c->ru_count = s.ru_count;
+    c->graph_passes = s.passes;
   }
 }
 
@@ -751,6 +1080,47 @@ int mixed_grids(lpm_handle* h, const SellView& sv, MixedGrids* mg) {
   mg->update = vector_grid(h, k_mx_update, ndof);
   mg->replace = vector_grid(h, k_mx_replace, ndof);
   mg->pupdate = vector_grid(h, k_mx_pupdate, ndof);
+  return LPM_OK;
+}
+
+// The persistent solve's kernel for the dimension and column format.
+using PcgFn = void (*)(PcgMixed);
+PcgFn pcg_fn(const SellView& sv, int dim) {
+  const bool o16 = sv.soff != nullptr;
+  if (dim == 3) return o16 ? k_mx_persistent<3, true> : k_mx_persistent<3, false>;
+  return o16 ? k_mx_persistent<2, true> : k_mx_persistent<2, false>;
+}
+
+// Blocks of the persistent solve, 0 where the graph runs instead: one
+// resident wave at most (a cooperative launch refuses more), no more blocks
+// than the rows fill, and no more than the partials hold.  LPM_CG_LOOP_AUTO
+// takes it when the FP32 operator stays in L2 and every row has a thread.
+int pcg_grid(lpm_handle* h, const SellView& sv) {
+  if (h->mf || h->cg_loop == LPM_CG_LOOP_GRAPH) return 0;
+  int coop = 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device) != cudaSuccess || !coop) return 0;
+  if (!h->sms && cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_fn(sv, h->dim), 256, 0) != cudaSuccess || per_sm < 1)
+    return 0;
+  const long long resident = (long long)h->sms * per_sm;
+  const long long need = ((long long)h->n + 255) / 256;
+  if (h->cg_loop == LPM_CG_LOOP_AUTO) {
+    const bool keep = (long long)h->nslots * h->dim * h->dim * 4 <= kKeepBytes;
+    if (!keep || need > resident) return 0;
+  }
+  const long long g = std::min<long long>(std::min(resident, need), (long long)kMaxRedBlocks * 4 / 6);
+  return (int)std::max<long long>(1, g);
+}
+
+int run_persistent_mixed(lpm_handle* h, const SellView& sv, int grid) {
+  Dev& d = h->d;
+  LPM_CUDA(h, cudaMemsetAsync(d.gbar, 0, sizeof(unsigned long long), h->stream));
+  PcgMixed a{sv,    d.A32,  d.A64, d.rhs, d.invd32, d.x32, d.x32lo,        d.r32,         d.r32lo,
+             d.p32, d.q32,  d.q32lo, d.x64, d.r64,  d.cg,  d.red.partials, d.gbar, kPcgSpinLimit};
+  void* args[] = {&a};
+  LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)pcg_fn(sv, h->dim), dim3(grid), dim3(256), args, 0, h->stream));
+  LPM_LAUNCHED(h, "k_mx_persistent");
   return LPM_OK;
 }
 
@@ -983,7 +1353,12 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   LPM_LAUNCHED(h, "k_mx_init");
   const bool timing = h->timing;
   const size_t ev0 = h->ev_used;
-  if (!timing) {
+  const int pgrid = timing ? 0 : pcg_grid(h, sv);
+  if (pgrid > 0) {
+    // the whole iteration loop as one persistent kernel
+    st = run_persistent_mixed(h, sv, pgrid);
+    if (st) return st;
+  } else if (!timing) {
     // the whole iteration loop as one graph launch
     if (!h->mx_exec || h->mx_graph_mf != h->mf || (!h->mf && h->mx_graph_spmv != (const void*)spmv32_fn(h, sv))) {
       st = build_mixed_graph(h, sv, mg);
@@ -1046,7 +1421,15 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   const CgScalars& c = *h->h_cg;
-  if (!timing) h->stats.kernel_launches += 3 * c.graph_passes + 2 * c.ru_count;
+  if (pgrid > 0) {
+    h->stats.persistent_solves += 1;
+    if (c.pfault) {
+      h->err = "persistent solve: a grid-barrier wait gave up";
+      return LPM_ERR_STATE;
+    }
+  } else if (!timing) {
+    h->stats.kernel_launches += 3 * c.graph_passes + 2 * c.ru_count;
+  }
   if (timing) {
     double ms_sum = 0.0;
     long long used = 0;

@@ -50,6 +50,7 @@ struct CgScalars {
   long long maxit;
   int done;           // 0 running, 1 converged, 2 iteration cap, 3 non-finite
   int ru;             // mixed solve: a reliable update is pending
+  int pfault;         // persistent solve: a grid-barrier wait gave up
   double rmax;        // mixed solve: largest |r| since the last reliable update
   long long ru_count; // mixed solve: reliable updates taken
   long long graph_passes;  // mixed solve: loop passes run by the solve graph
@@ -145,6 +146,7 @@ struct Dev {
   // reductions
   RedBuf red;
   CgScalars* cg;   // device scalars
+  unsigned long long* gbar;  // persistent solve: grid-barrier arrivals (zeroed before each launch)
   double* norms;   // device results of small reductions [8]
   // per-particle flags for the BC elimination
   unsigned char* fixed;
@@ -221,6 +223,7 @@ struct lpm_handle {
   double* h_norms = nullptr;       // pinned [8]
   lpm_stats stats{};
   bool timing = false;
+  int cg_loop = LPM_CG_LOOP_AUTO;  // how the solves run their iteration loop (lpm_set_cg_loop)
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   std::vector<void*> allocations;
