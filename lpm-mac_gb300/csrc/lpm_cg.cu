@@ -673,12 +673,16 @@ struct PcgState {
   float ah, al, bh, bl, zc;
 };
 
-// Register budget of the persistent kernel: that of the FP32 product.
+// Most threads per block of the persistent kernel: one block per SM with
+// the register budget of the FP32 product (2-D: 80 registers, 3-D: 128), as
+// many threads per SM as the product's 256-thread blocks.  Few large blocks
+// keep the barriers short: a barrier with its fold measured 2.6 us over 152
+// blocks against 4.4 us over 456.
 template <int DIM>
-constexpr int kPcgMinBlocks = DIM == 3 ? 2 : 3;
+constexpr int kPcgThreads = DIM == 3 ? 512 : 768;
 
 template <int DIM, bool OFF16>
-__global__ void __launch_bounds__(256, kPcgMinBlocks<DIM>) k_mx_persistent(PcgMixed a) {
+__global__ void __launch_bounds__(kPcgThreads<DIM>, 1) k_mx_persistent(PcgMixed a) {
   __shared__ PcgState s;
   if (threadIdx.x == 0) {
     const CgScalars* c = a.cg;
@@ -1091,20 +1095,28 @@ PcgFn pcg_fn(const SellView& sv, int dim) {
   return o16 ? k_mx_persistent<2, true> : k_mx_persistent<2, false>;
 }
 
-// Blocks of the persistent solve, 0 where the graph runs instead: one
-// resident wave at most (a cooperative launch refuses more), no more blocks
-// than the rows fill, and no more than the partials hold.  LPM_CG_LOOP_AUTO
-// takes it when the FP32 operator stays in L2 and every row has a thread.
-int pcg_grid(lpm_handle* h, const SellView& sv) {
+// Launch shape of the persistent solve; grid 0 where the graph runs
+// instead.  The rows are spread over every SM: about rows / SMs threads per
+// block (a multiple of 32, at least 128, at most kPcgThreads), so a lattice
+// of 80k rows takes 148 blocks of 544 threads rather than 105 full blocks.
+// At most one resident wave (a cooperative launch refuses more) and no more
+// blocks than the partials hold.  LPM_CG_LOOP_AUTO takes it when the FP32
+// operator stays in L2 and every row has a thread.
+int pcg_grid(lpm_handle* h, const SellView& sv, int* threads_out) {
   if (h->mf || h->cg_loop == LPM_CG_LOOP_GRAPH) return 0;
   int coop = 0;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device) != cudaSuccess || !coop) return 0;
   if (!h->sms && cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) return 0;
+  const long long cap = h->dim == 3 ? kPcgThreads<3> : kPcgThreads<2>;
+  const long long per_sm_rows = ((long long)h->n + h->sms - 1) / h->sms;
+  const int threads = (int)std::min(cap, std::max<long long>(128, (per_sm_rows + 31) / 32 * 32));
+  *threads_out = threads;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_fn(sv, h->dim), 256, 0) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_fn(sv, h->dim), threads, 0) != cudaSuccess ||
+      per_sm < 1)
     return 0;
   const long long resident = (long long)h->sms * per_sm;
-  const long long need = ((long long)h->n + 255) / 256;
+  const long long need = ((long long)h->n + threads - 1) / threads;
   if (h->cg_loop == LPM_CG_LOOP_AUTO) {
     const bool keep = (long long)h->nslots * h->dim * h->dim * 4 <= kKeepBytes;
     if (!keep || need > resident) return 0;
@@ -1113,13 +1125,14 @@ int pcg_grid(lpm_handle* h, const SellView& sv) {
   return (int)std::max<long long>(1, g);
 }
 
-int run_persistent_mixed(lpm_handle* h, const SellView& sv, int grid) {
+int run_persistent_mixed(lpm_handle* h, const SellView& sv, int grid, int threads) {
   Dev& d = h->d;
   LPM_CUDA(h, cudaMemsetAsync(d.gbar, 0, sizeof(unsigned long long), h->stream));
   PcgMixed a{sv,    d.A32,  d.A64, d.rhs, d.invd32, d.x32, d.x32lo,        d.r32,         d.r32lo,
              d.p32, d.q32,  d.q32lo, d.x64, d.r64,  d.cg,  d.red.partials, d.gbar, kPcgSpinLimit};
   void* args[] = {&a};
-  LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)pcg_fn(sv, h->dim), dim3(grid), dim3(256), args, 0, h->stream));
+  LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)pcg_fn(sv, h->dim), dim3(grid), dim3(threads), args, 0,
+                                          h->stream));
   LPM_LAUNCHED(h, "k_mx_persistent");
   return LPM_OK;
 }
@@ -1353,10 +1366,11 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   LPM_LAUNCHED(h, "k_mx_init");
   const bool timing = h->timing;
   const size_t ev0 = h->ev_used;
-  const int pgrid = timing ? 0 : pcg_grid(h, sv);
+  int pthreads = 0;
+  const int pgrid = timing ? 0 : pcg_grid(h, sv, &pthreads);
   if (pgrid > 0) {
     // the whole iteration loop as one persistent kernel
-    st = run_persistent_mixed(h, sv, pgrid);
+    st = run_persistent_mixed(h, sv, pgrid, pthreads);
     if (st) return st;
   } else if (!timing) {
     // the whole iteration loop as one graph launch

@@ -163,3 +163,69 @@ def test_plate_files_written_like_reference(tmp_path):
     mine = np.loadtxt(tmp_path / "plate.bond", dtype=np.int64)
     ref = np.loadtxt(os.path.join(IO_GOLDEN, "plate.bond"), dtype=np.int64)
     assert np.array_equal(mine[:, 1:], ref[:, 1:])
+
+
+BEAM = os.path.join(CPP, "examples", "cantilever_beam.cpp")
+
+
+def _beam_exact(xyz0, L, D, P, E, mu):
+    """Solution::computeSolBeam001 as the class code evaluates it (the
+    reference's 1/6/G/I term is an integer division there and so zero)."""
+    G, I = E / 2 / (1 + mu), D ** 3 / 12
+    x, y = xyz0[:, 0], xyz0[:, 1]
+    u1 = -P * x * x * y / 2 / E / I + P * y ** 3 * (0.0 - mu / 6 / E / I) + y * (P * L * L / 2 / E / I - P * D * D / 8 / G / I)
+    u2 = mu * P * x * y * y / 2 / E / I + P * x ** 3 / 6 / E / I - P * L * L * x / 2 / E / I + P * L ** 3 / 3 / E / I
+    return np.stack([u1, u2], axis=1)
+
+
+@pytest.mark.gpu
+def test_cantilever_beam_through_class_interface_matches_oracle(tmp_path):
+    """The reference's convergence-beam setup (ex7_convergence_beam: 30 x 10
+    hexagonal plate at radius 0.2, right end clamped, 2 N on the left end)
+    as a class-interface program (cpp/examples/cantilever_beam.cpp) on the
+    GPU with the symmetric tangent and the BC elimination of
+    SolverFatigue::solveProblemStatic: it converges, its final displacements
+    are within 1e-8 of the oracle's load step on the same particles and
+    bonds, and the relative L2 error against the closed-form beam solution
+    that it prints (Solution::computeL2Error) is the oracle's to 1e-6.
+    Built against the reference's own headers, the same program diverges
+    from the first Newton iteration (the tangent as written), as the
+    reference's own ex7 does."""
+    import re
+    from lpm_cases import lat, make_oracle, oracle, rel
+    exe = str(tmp_path / "beam")
+    compile_example(BEAM, exe, link=True)
+    out = str(tmp_path / "beam.txt")
+    env = dict(os.environ, LPM_CG_TOL="1e-12", LPM_TANGENT="symmetric")
+    r = subprocess.run([exe, out, "fatigue", "0.2"], capture_output=True, text=True, env=env, cwd=str(tmp_path),
+                       timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+    assert "Solving failed" not in r.stdout
+    l2_gpu = float(re.search(r"L2 error is: (\S+)", r.stdout).group(1))
+    d = np.loadtxt(out)
+    assert np.array_equal(d[:, 0].astype(np.int64), np.arange(len(d)))
+    xyz0, xyz = d[:, 4:7], d[:, 1:4]
+    E, mu, P = 69e3, 0.33, 2.0
+    cell = lat.UnitCell(lat.HEXAGON2D, 0.2)
+    p1, p2, layer = lat.find_bonds(xyz0, cell)
+    C11 = E * (1.0 - mu) / (1.0 + mu) / (1.0 - 2.0 * mu)
+    C12 = E * mu / (1.0 + mu) / (1.0 - 2.0 * mu)
+    Kn = np.full(len(p1), np.sqrt(3.0) / 12.0 * (C11 - C12))
+    Tv = np.full(len(p1), np.sqrt(3.0) / 48.0 * C12 - np.sqrt(3.0) / 144.0 * C11)
+    o = make_oracle(2, xyz0, p1, p2, layer, Kn, Tv, cell)
+    o.update()
+    n = len(xyz0)
+    left = np.where(xyz0[:, 0] < xyz0[:, 0].min() + 1e-6)[0]
+    right = np.where(xyz0[:, 0] > xyz0[:, 0].max() - 1e-6)[0]
+    apply = np.zeros((n, 3), np.int32)
+    apply[right, 0] = apply[right, 1] = 1
+    f = np.zeros((n, 3))
+    f[left, 1] = P / len(left)
+    assert 0 <= o.load_step(apply, np.zeros((n, 3)), f, sym=1, bc_elim=1, max_iter=30, tol=1e-5, cg_tol=1e-12) < 30
+    u_o = (o.get(oracle.XYZ) - xyz0)[:, :2]
+    u_g = (xyz - xyz0)[:, :2]
+    exact = _beam_exact(xyz0, 30.0, 10.0, P, E, mu)
+    l2_o = np.sqrt(((exact - u_o) ** 2).sum() / (exact ** 2).sum())
+    print("[beam] %d particles: GPU vs oracle %.2e; L2 error GPU %.6f, oracle %.6f" % (n, rel(u_g, u_o), l2_gpu, l2_o))
+    assert rel(u_g, u_o) <= 1e-8
+    assert np.isfinite(l2_gpu) and abs(l2_gpu - l2_o) <= 1e-6 * l2_o

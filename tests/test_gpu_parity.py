@@ -127,11 +127,14 @@ def test_mixed_solve_graph_matches_host_launched_loop():
     """The mixed solve's graph (device-set loop and reliable-update
     conditions) runs the same kernels in the same order as the host-launched
     loop that kernel timing selects: identical iterates, bit for bit, on a
-    relaunch too; the iteration cap and a zero right-hand side end it."""
+    relaunch too; the iteration cap and a zero right-hand side end it.  (The
+    persistent loop, which this small system would take by default, folds
+    its sums over other blocks: within the solve tolerance of the graph.)"""
     d = golden("kernels_sc_undamaged")
     g, dim, n = _gpu_at_golden_state(d)
     g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_ELIMINATE)
     g.residual()
+    g.set_cg_loop(capi.CG_LOOP_GRAPH)
     runs = []
     for timing in (False, True, False):
         g.set_kernel_timing(timing)
@@ -144,6 +147,11 @@ def test_mixed_solve_graph_matches_host_launched_loop():
     for it, x, _ in runs[1:]:
         assert it == runs[0][0]
         assert np.array_equal(x, runs[0][1])
+    g.set_cg_loop(capi.CG_LOOP_PERSISTENT)
+    it_p, rr_p, st_p = g.solve(capi.PREC_MIXED, 1e-10)
+    assert st_p == 0 and rr_p <= 1e-10 and abs(it_p - runs[0][0]) <= 2
+    assert rel(g.download(capi.F_DISP), runs[0][1]) <= 1e-8
+    g.set_cg_loop(capi.CG_LOOP_AUTO)
     assert runs[0][2]["refine_sweeps"] == runs[1][2]["refine_sweeps"] > 0
     # the graph launches the product, the update and the direction update per
     # iteration, and the two reliable-update kernels only when one is due
