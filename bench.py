@@ -29,9 +29,11 @@ Reported (one JSON line on rank 0):
   setup        the GPU bond search (checked identical to the CPU
                generator's bonds) and the creation of the device lattice
   fatigue      compact-tension fatigue cycles at full size (configuration 5)
-  softening    (--softening) load steps of the notched plate with the
-               softening bond law and damage rounds at full size
-               (configuration 3); minutes, so not in the default run
+  softening    load steps of the notched plate with the softening bond law
+               and damage rounds at full size (configuration 3): by default
+               the one step in which the first bonds soften (about 170
+               damage rounds); --softening-steps 4 times the crack's burst
+               too (minutes)
   j2_sensitivity  cost of carrying d/d(yield stress) and d/d(hardening)
                through J2 load steps of a BCC polycrystal (40^3 cells)
   polycrystal  configuration 4 at full size (BCC 60^3 cells, 20 grains):
@@ -75,8 +77,9 @@ def parse_args(argv=None):
     p.add_argument("--no-extras", action="store_true",
                    help="time the load steps only (no e2e, adjoint, force/assembly, set-up, fatigue, J2 legs): "
                         "for profiling runs")
-    p.add_argument("--softening", action="store_true",
-                   help="also time configuration 3 at full size (several minutes: its crack bursts in the timed steps)")
+    p.add_argument("--softening-steps", type=int, default=1,
+                   help="timed load steps of configuration 3 at full size from the first softened bond on (0: none; "
+                        "4 includes the crack's burst, several minutes)")
     return p.parse_args(argv)
 
 
@@ -904,8 +907,8 @@ def run_gb300(args):
                            "force_algorithmic_bytes": fb}
     run_leg(line, "setup", setup_cost, w, capi)
     run_leg(line, "fatigue", fatigue_cost, capi, local)
-    if args.softening:
-        run_leg(line, "softening", softening_cost, capi, local)
+    if args.softening_steps > 0:
+        run_leg(line, "softening", softening_cost, capi, local, steps=args.softening_steps)
     run_leg(line, "j2_sensitivity", j2_sensitivity_cost, capi, local)
     run_leg(line, "polycrystal", polycrystal_cost, capi, local)
     g.close()
