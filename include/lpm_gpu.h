@@ -291,7 +291,7 @@ typedef struct {
   int64_t mixed_fallbacks; /* mixed solves that broke down (non-finite FP32 recurrence,
                               e.g. an indefinite softened tangent) and were re-solved in FP64 */
   int64_t tangent_cg_iters; /* CG iterations of the tangent solves (lpm_tangent_begin) */
-  int64_t persistent_solves; /* mixed solves whose loop ran as one persistent kernel (lpm_set_cg_loop) */
+  int64_t persistent_solves; /* solves whose loop ran as one persistent kernel (lpm_set_cg_loop) */
 } lpm_stats;
 int lpm_get_stats(const lpm_handle* h, lpm_stats* st);
 int lpm_reset_stats(lpm_handle* h);
@@ -300,8 +300,8 @@ int lpm_reset_stats(lpm_handle* h);
  * is on, the solves launch their iterations one by one from the host instead
  * of as one CUDA graph (same kernels, same results). */
 int lpm_set_kernel_timing(lpm_handle* h, int on);
-/* How the mixed-precision solve runs its iteration loop.  No counterpart in
- * the reference (Eigen's loop runs on the host, solver.h:192-217).
+/* How lpm_solve runs its iteration loop.  No counterpart in the reference
+ * (Eigen's loop runs on the host, solver.h:192-217).
  *   LPM_CG_LOOP_GRAPH       one CUDA graph per solve: per iteration the
  *                           product, the update and the direction kernels,
  *                           with the loop and reliable-update conditions set
@@ -314,12 +314,13 @@ int lpm_set_kernel_timing(lpm_handle* h, int on);
  *                           recurrence, same stopping rule; the sums are
  *                           folded over another number of blocks, so the
  *                           last bits differ from the graph's.
- *   LPM_CG_LOOP_AUTO        (default) persistent when the assembled FP32
- *                           operator fits in half of L2 and the rows fit one
- *                           resident wave, else the graph.
- * The FP64 solve, the matrix-free operator and kernel timing always use the
- * graph or host loop.  A barrier wait that gives up (a bounded spin) ends the
- * solve with LPM_ERR_STATE. */
+ *   LPM_CG_LOOP_AUTO        (default) persistent when the rows fit one
+ *                           resident wave with a thread each and, for the
+ *                           mixed solve, the FP32 operator fits in half of
+ *                           L2; else the graph.
+ * Both precisions have both loops.  The matrix-free operator and kernel
+ * timing always use the graph or host loop.  A barrier wait that gives up (a
+ * bounded spin) ends the solve with LPM_ERR_STATE. */
 #define LPM_CG_LOOP_AUTO 0
 #define LPM_CG_LOOP_GRAPH 1
 #define LPM_CG_LOOP_PERSISTENT 2

@@ -883,6 +883,137 @@ __global__ void __launch_bounds__(kPcgThreads<DIM>, 1) k_mx_persistent(PcgMixed 
   }
 }
 
+// The FP64 solve as one persistent kernel: the recurrence of k_cg_spmv,
+// k_cg_update and k_cg_pupdate (Eigen's), with the same row ownership and
+// barriers as k_mx_persistent and no reliable updates.
+struct PcgFp64 {
+  SellView v;
+  const double* A;
+  const double* invd;
+  double *x, *r, *p, *q;
+  CgScalars* cg;
+  double* partials;          // 3 x gridDim.x
+  unsigned long long* gbar;  // barrier arrivals, zero at launch
+  long long spin_limit;
+};
+
+// Most threads per block: the FP64 product's 64 registers, one block per SM.
+constexpr int kPcg64Threads = 1024;
+
+template <int DIM>
+__global__ void __launch_bounds__(kPcg64Threads, 1) k_cg_persistent(PcgFp64 a) {
+  __shared__ double s_abs_new, s_threshold, s_alpha, s_beta, s_rr;
+  __shared__ long long s_it, s_maxit, s_passes;
+  __shared__ int s_done;
+  if (threadIdx.x == 0) {
+    const CgScalars* c = a.cg;
+    s_abs_new = c->abs_new;
+    s_threshold = c->threshold;
+    s_alpha = c->alpha;
+    s_beta = c->beta;
+    s_rr = c->rr;
+    s_it = c->it;
+    s_maxit = c->maxit;
+    s_passes = 0;
+    s_done = c->done;
+  }
+  __syncthreads();
+  const int n = a.v.n;
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long target = 0;
+  bool fault = false;
+  while (!s_done) {
+    // q = A p and p.q; alpha
+    {
+      double acc[1] = {0.0}, tot[1];
+      for (int row = t0; row < n; row += stride) {
+        double y[DIM];
+        row_product<DIM, false, true>(a.v, a.A, a.p, row, y);
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) {
+          const int64_t i = (int64_t)row * DIM + r;
+          a.q[i] = y[r];
+          acc[0] += a.p[i] * y[r];
+        }
+      }
+      block_sum<1>(acc);
+      if (!grid_allreduce<1>(acc, a.partials, 0, a.gbar, target, a.spin_limit, tot)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) s_alpha = s_abs_new / tot[0];
+      __syncthreads();
+    }
+    // x += alpha p, r -= alpha q, |r|^2 and r.z; convergence, beta
+    {
+      const double alpha = s_alpha;
+      double v[2] = {0.0, 0.0}, tot[2];
+      for (int row = t0; row < n; row += stride)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const int64_t i = (int64_t)row * DIM + c;
+          const double ri = a.r[i] - alpha * a.q[i];
+          a.x[i] = a.x[i] + alpha * a.p[i];
+          a.r[i] = ri;
+          const double zi = a.invd[i] * ri;
+          v[0] += ri * ri;
+          v[1] += ri * zi;
+        }
+      block_sum<2>(v);
+      if (!grid_allreduce<2>(v, a.partials, 1, a.gbar, target, a.spin_limit, tot)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) {
+        s_rr = tot[0];
+        if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+          s_done = 3;
+        } else if (tot[0] < s_threshold) {
+          s_done = 1;
+        } else {
+          s_beta = tot[1] / s_abs_new;
+          s_abs_new = tot[1];
+          s_it += 1;
+          if (s_it >= s_maxit) s_done = 2;
+        }
+      }
+      __syncthreads();
+    }
+    if (s_done) break;
+    // p = M^-1 r + beta p
+    {
+      const double beta = s_beta;
+      for (int row = t0; row < n; row += stride)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const int64_t i = (int64_t)row * DIM + c;
+          a.p[i] = a.invd[i] * a.r[i] + beta * a.p[i];
+        }
+      target += (unsigned long long)gridDim.x;
+      if (!grid_barrier(a.gbar, target, a.spin_limit)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) s_passes += 1;
+    }
+  }
+  if (fault) {
+    if (threadIdx.x == 0) atomicExch(&a.cg->pfault, 1);
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    CgScalars* c = a.cg;
+    c->done = s_done;
+    c->rr = s_rr;
+    c->it = s_it;
+    c->abs_new = s_abs_new;
+    c->alpha = s_alpha;
+    c->beta = s_beta;
+    c->graph_passes = s_passes;
+  }
+}
+
 // Grid of the FP64 row kernels (product, true residual): these are bound by
 // the FP64 pipe, and measured faster with several waves of blocks than with
 // one resident wave (0.99 against 1.06 ms per product at 101^3).
@@ -907,6 +1038,58 @@ int resident_grid(lpm_handle* h, K kernel, long long work) {
   const long long resident = h->sms > 0 ? (long long)h->sms * per_sm : kMaxRedBlocks;
   const long long g = std::min<long long>(resident, (work + 255) / 256);
   return (int)std::max<long long>(1, std::min<long long>(g, kMaxRedBlocks));
+}
+
+// Launch shape of a persistent solve, grid 0 where the graph runs instead.
+// The rows are spread over every SM: about rows / SMs threads per block (a
+// multiple of 32, at least 128, at most `cap`), so a lattice of 80k rows
+// takes 148 blocks of 544 threads rather than 105 full ones.  At most one
+// resident wave (a cooperative launch refuses more) and no more blocks than
+// `slots` partials per block fit in the reduction buffer.  LPM_CG_LOOP_AUTO
+// takes it when every row has a thread (and `auto_ok`).
+template <typename K>
+int persistent_shape(lpm_handle* h, K kernel, int cap, bool auto_ok, int slots, int* threads_out) {
+  if (h->mf || h->cg_loop == LPM_CG_LOOP_GRAPH) return 0;
+  int coop = 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device) != cudaSuccess || !coop) return 0;
+  if (!h->sms && cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) return 0;
+  const long long per_sm_rows = ((long long)h->n + h->sms - 1) / h->sms;
+  const int threads = (int)std::min<long long>(cap, std::max<long long>(128, (per_sm_rows + 31) / 32 * 32));
+  *threads_out = threads;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+    return 0;
+  const long long resident = (long long)h->sms * per_sm;
+  const long long need = ((long long)h->n + threads - 1) / threads;
+  if (h->cg_loop == LPM_CG_LOOP_AUTO && (!auto_ok || need > resident)) return 0;
+  const long long g = std::min<long long>(std::min(resident, need), (long long)kMaxRedBlocks * 4 / slots);
+  return (int)std::max<long long>(1, g);
+}
+
+// The FP64 solve's loop as one persistent kernel, when persistent_shape
+// allows.  Returns 1 if it ran (its scalars then in h->h_cg), 0 if the graph
+// should run, or an error.
+int run_persistent_fp64(lpm_handle* h, const SellView& sv, const double* A, double* x, double* r, double* p,
+                        double* q, const double* invd) {
+  using Fn = void (*)(PcgFp64);
+  const Fn fn = h->dim == 3 ? k_cg_persistent<3> : k_cg_persistent<2>;
+  int threads = 0;
+  const int grid = persistent_shape(h, fn, kPcg64Threads, true, 3, &threads);
+  if (grid <= 0) return 0;
+  Dev& d = h->d;
+  LPM_CUDA(h, cudaMemsetAsync(d.gbar, 0, sizeof(unsigned long long), h->stream));
+  PcgFp64 a{sv, A, invd, x, r, p, q, d.cg, d.red.partials, d.gbar, kPcgSpinLimit};
+  void* args[] = {&a};
+  LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(threads), args, 0, h->stream));
+  LPM_LAUNCHED(h, "k_cg_persistent");
+  LPM_CUDA(h, cudaMemcpyAsync(h->h_cg, d.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->stats.persistent_solves += 1;
+  if (h->h_cg->pfault) {
+    h->err = "persistent solve: a grid-barrier wait gave up";
+    return LPM_ERR_STATE;
+  }
+  return 1;
 }
 
 cudaEvent_t next_event(lpm_handle* h) {
@@ -935,7 +1118,10 @@ int run_cg(lpm_handle* h, const T* A, const T* b, T* x, T* r, T* p, T* q, const 
   LPM_LAUNCHED(h, "k_cg_init");
   const bool timing = h->timing;
   if constexpr (sizeof(T) == 8) {
-    if (!timing) {  // the whole iteration loop as one graph launch
+    if (!timing) {  // the whole iteration loop as one persistent kernel, or as one graph launch
+      const int pst = run_persistent_fp64(h, sv, A, x, r, p, q, invd);
+      if (pst < 0) return pst;
+      if (pst == 1) return LPM_OK;
       if (!h->fp_exec || h->fp_graph_x != (const void*)x || h->fp_graph_mf != h->mf) {
         const int st = build_fp64_graph(h, A, b, x, r, p, q, invd, GV, GR, sv);
         if (st) return st;
@@ -1095,34 +1281,12 @@ PcgFn pcg_fn(const SellView& sv, int dim) {
   return o16 ? k_mx_persistent<2, true> : k_mx_persistent<2, false>;
 }
 
-// Launch shape of the persistent solve; grid 0 where the graph runs
-// instead.  The rows are spread over every SM: about rows / SMs threads per
-// block (a multiple of 32, at least 128, at most kPcgThreads), so a lattice
-// of 80k rows takes 148 blocks of 544 threads rather than 105 full blocks.
-// At most one resident wave (a cooperative launch refuses more) and no more
-// blocks than the partials hold.  LPM_CG_LOOP_AUTO takes it when the FP32
-// operator stays in L2 and every row has a thread.
+// Launch shape of the persistent mixed solve (persistent_shape); AUTO takes
+// it only when the FP32 operator stays in L2.
 int pcg_grid(lpm_handle* h, const SellView& sv, int* threads_out) {
-  if (h->mf || h->cg_loop == LPM_CG_LOOP_GRAPH) return 0;
-  int coop = 0;
-  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device) != cudaSuccess || !coop) return 0;
-  if (!h->sms && cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) return 0;
-  const long long cap = h->dim == 3 ? kPcgThreads<3> : kPcgThreads<2>;
-  const long long per_sm_rows = ((long long)h->n + h->sms - 1) / h->sms;
-  const int threads = (int)std::min(cap, std::max<long long>(128, (per_sm_rows + 31) / 32 * 32));
-  *threads_out = threads;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg_fn(sv, h->dim), threads, 0) != cudaSuccess ||
-      per_sm < 1)
-    return 0;
-  const long long resident = (long long)h->sms * per_sm;
-  const long long need = ((long long)h->n + threads - 1) / threads;
-  if (h->cg_loop == LPM_CG_LOOP_AUTO) {
-    const bool keep = (long long)h->nslots * h->dim * h->dim * 4 <= kKeepBytes;
-    if (!keep || need > resident) return 0;
-  }
-  const long long g = std::min<long long>(std::min(resident, need), (long long)kMaxRedBlocks * 4 / 6);
-  return (int)std::max<long long>(1, g);
+  const bool keep = (long long)h->nslots * h->dim * h->dim * 4 <= kKeepBytes;
+  return persistent_shape(h, pcg_fn(sv, h->dim), h->dim == 3 ? kPcgThreads<3> : kPcgThreads<2>, keep, 6,
+                          threads_out);
 }
 
 int run_persistent_mixed(lpm_handle* h, const SellView& sv, int grid, int threads) {

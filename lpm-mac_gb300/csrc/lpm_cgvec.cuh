@@ -90,6 +90,7 @@ __global__ void k_cg_init(int64_t ndof, const T* __restrict__ b, T* __restrict__
     cg->it = 0;
     cg->maxit = maxit;
     cg->graph_passes = 0;
+    cg->pfault = 0;
     if (!isfinite(tot[0]) || !isfinite(tot[1]))
       cg->done = 3;
     else if (tot[0] == 0.0 || tot[0] < cg->threshold)

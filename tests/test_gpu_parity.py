@@ -171,11 +171,14 @@ def test_mixed_solve_graph_matches_host_launched_loop():
 
 def test_fp64_solve_graph_matches_host_launched_loop():
     """The FP64 solve's graph and its host-launched loop give the same
-    iterates, bit for bit; the iteration cap ends the graph too."""
+    iterates, bit for bit; the iteration cap ends the graph too.  The
+    persistent loop (this small system's default) agrees to the solve
+    tolerance, within two iterations, and stops at the cap too."""
     d = golden("kernels_sc_undamaged")
     g, dim, n = _gpu_at_golden_state(d)
     g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_ELIMINATE)
     g.residual()
+    g.set_cg_loop(capi.CG_LOOP_GRAPH)
     runs = []
     for timing in (False, True, False):
         g.set_kernel_timing(timing)
@@ -185,6 +188,14 @@ def test_fp64_solve_graph_matches_host_launched_loop():
     g.set_kernel_timing(False)
     for it, x in runs[1:]:
         assert it == runs[0][0] and np.array_equal(x, runs[0][1])
+    it, rr, st = g.solve(capi.PREC_FP64, 1e-10, maxit=7)
+    assert st == capi.NOT_CONVERGED and it == 7
+    g.set_cg_loop(capi.CG_LOOP_PERSISTENT)
+    g.reset_stats()
+    it, rr, st = g.solve(capi.PREC_FP64, 1e-10)
+    assert st == 0 and rr <= 1e-10 and abs(it - runs[0][0]) <= 2
+    assert rel(g.download(capi.F_DISP), runs[0][1]) <= 1e-9
+    assert g.stats()["persistent_solves"] == 1
     it, rr, st = g.solve(capi.PREC_FP64, 1e-10, maxit=7)
     assert st == capi.NOT_CONVERGED and it == 7
     g.close()

@@ -1,6 +1,6 @@
-"""The mixed solve's persistent loop (lpm_set_cg_loop) against its graph
-loop: the same recurrence, reliable updates and stopping rule run as one
-cooperative kernel whose blocks meet at grid barriers.  Load steps agree
+"""The persistent solve loops (lpm_set_cg_loop) against the graph loops: the
+same recurrences (and, mixed, the same reliable updates) and stopping rule
+run as one cooperative kernel whose blocks meet at grid barriers.  Load steps agree
 to the solve tolerance and iteration counts within a few percent (the sums
 are folded over another number of blocks, so the last bits differ), on 2-D
 and 3-D lattices, with one row per thread and, forced on a lattice larger
@@ -14,7 +14,7 @@ capi = pkg.capi
 pytestmark = pytest.mark.gpu
 
 
-def _steps(case, loop, nsteps=2):
+def _steps(case, loop, nsteps=2, precision=capi.PREC_MIXED):
     maker, args, du = case
     dim, xyz, p1, p2, layer, Kn, Tv, cell = maker(*args)
     groups, _, _ = tension_bcs(xyz, dim, du)
@@ -25,7 +25,7 @@ def _steps(case, loop, nsteps=2):
     g.reset_stats()
     its, newton = [], 0
     for _ in range(nsteps):
-        res = g.load_step(bcs, tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_MIXED, cg_tol=1e-10)
+        res = g.load_step(bcs, tangent=capi.TANGENT_SYMMETRIC, precision=precision, cg_tol=1e-10)
         assert res["status"] == capi.OK
         its.append(res["cg_iters"])
         newton += res["newton_iters"]
@@ -90,3 +90,26 @@ def test_persistent_loop_iteration_cap_and_repeatability():
         g.set_cg_loop(7)
     assert e.value.code == capi.ERR_ARG
     g.close()
+
+
+@pytest.mark.parametrize("name", ["plate41", "cube21"])
+def test_persistent_fp64_loop_matches_graph_and_oracle(name):
+    """FP64 load steps: the persistent loop within 1e-10 of the graph loop
+    and of the oracle (the plain FP64 form's bar), with the CG iteration
+    counts within two per solve of the graph's."""
+    from lpm_cases import make_oracle, oracle
+    ug, itg, sg, _ = _steps(CASES[name], capi.CG_LOOP_GRAPH, precision=capi.PREC_FP64)
+    up, itp, sp, newton = _steps(CASES[name], capi.CG_LOOP_PERSISTENT, precision=capi.PREC_FP64)
+    maker, args, du = CASES[name]
+    dim, xyz, p1, p2, layer, Kn, Tv, cell = maker(*args)
+    _, apply, dd = tension_bcs(xyz, dim, du)
+    o = make_oracle(dim, xyz, p1, p2, layer, Kn, Tv, cell)
+    o.update()
+    for _ in range(2):
+        o.load_step(apply, dd, sym=1, bc_elim=1, cg_tol=1e-10)
+    uo = o.get(oracle.XYZ) - xyz
+    print("[persistent fp64] %s: graph %s, persistent %s; persistent vs graph %.2e, vs oracle %.2e" % (
+        name, itg, itp, rel(up, ug), rel(up, uo)))
+    assert sg["persistent_solves"] == 0 and sp["persistent_solves"] >= newton > 0
+    assert rel(up, ug) <= 1e-10 and rel(up, uo) <= 1e-10
+    assert abs(sum(itp) - sum(itg)) <= 2 * newton
