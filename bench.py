@@ -77,6 +77,9 @@ def parse_args(argv=None):
     p.add_argument("--no-extras", action="store_true",
                    help="time the load steps only (no e2e, adjoint, force/assembly, set-up, fatigue, J2 legs): "
                         "for profiling runs")
+    p.add_argument("--profile-solve", choices=["sent", "ct"],
+                   help="profiling entry: one mixed solve (300 iterations) on the full-size SENT or CT plate's "
+                        "tangent, which runs as one persistent kernel; prints its time and exits")
     p.add_argument("--softening-steps", type=int, default=1,
                    help="timed load steps of configuration 3 at full size from the first softened bond on (0: none; "
                         "4 includes the crack's burst, several minutes)")
@@ -360,7 +363,7 @@ def fatigue_cost(capi, local, cycles=3):
     lattice, W = 40 mm from the load line, 0.15 mm spacing), HCF fatigue law
     with seeded per-particle A and B, nonlocal damage rate, pin loads
     cycled between 40 and 400 N (R = 0.1).  A static step to the minimum
-    load, then `cycles` calls of lpm_fatigue_cycle (one load increment up and
+    load, then `cycles` simulated cycles of lpm_fatigue_run (one load increment up and
     one down, a cycle jump of 1000), mixed precision.  Device time with CUDA
     events on the library's stream."""
     import torch
@@ -398,10 +401,12 @@ def fatigue_cost(capi, local, cycles=3):
     e1 = torch.cuda.Event(enable_timing=True)
     g.synchronize()
     e0.record(stream)
+    g.reset_stats()
     recs = fat.run_cycles(g, unit, spectrum, 1, 0.001, max_calls=cycles, **opts)
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
+    persistent = g.stats()["persistent_solves"]
     g.close()
     if any(rc["status"] != 0 for rc in recs):
         raise RuntimeError("CT fatigue cycle did not converge")
@@ -410,7 +415,8 @@ def fatigue_cost(capi, local, cycles=3):
             "cycles_per_s": len(recs) / (ms * 1e-3), "ms_per_cycle": ms / len(recs), "cycles": len(recs),
             "newton_iters_per_cycle": statistics.mean(rc["newton_iters"] for rc in recs),
             "cg_iters_per_cycle": statistics.mean(rc["cg_iters"] for rc in recs),
-            "cycle": "1 increment up, 1 down, cycle jump 1000 (lpm_fatigue_cycle)", "precision": "mixed"}
+            "cycle": "1 increment up, 1 down, cycle jump 1000 (lpm_fatigue_run)", "precision": "mixed",
+            "persistent_solves": persistent}
 
 
 def softening_cost(capi, local, steps=4, max_warm=15):
@@ -448,12 +454,14 @@ def softening_cost(capi, local, steps=4, max_warm=15):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     g.synchronize()
+    g.reset_stats()
     e0.record(stream)
     recs = [g.load_step(bcs, **opts) for _ in range(steps)]
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     d = g.download(capi.B_BDAMAGE)
+    persistent = g.stats()["persistent_solves"]
     g.close()
     if any(r["status"] != 0 for r in recs):
         raise RuntimeError("SENT step did not converge")
@@ -464,7 +472,8 @@ def softening_cost(capi, local, steps=4, max_warm=15):
             "damage_rounds_per_step": statistics.mean(r["damage_rounds"] for r in recs),
             "cg_iters_per_step": statistics.mean(r["cg_iters"] for r in recs),
             "softened_bonds": int((d > 0).sum()), "broken_bonds": int((d >= 1).sum()),
-            "precision": "mixed", "solver": "static with damage rounds, eliminated tangent"}
+            "precision": "mixed", "solver": "static with damage rounds, eliminated tangent",
+            "us_per_cg_iteration": 1e3 * ms / max(1, sum(r["cg_iters"] for r in recs)), "persistent_solves": persistent}
 
 
 def j2_sensitivity_cost(capi, local, ncell=40, steps=4):
@@ -927,9 +936,53 @@ def run_gb300(args):
 ARGS = None
 
 
+def profile_solve(case):
+    """One mixed solve of 300 iterations on the eliminated symmetric tangent
+    of a full-size plate after one FP64 load step (top edge up by 1e-3 mm),
+    with a seeded right-hand side: a small case for profiling the persistent
+    solve kernel (k_mx_persistent).  Device time with CUDA events."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    lat, capi = pkg.lattice, pkg.capi
+    if case == "sent":
+        xyz, p1, p2, layer, cell = lat.sent_plate(201, 401, 0.1)
+        E, nu = 69e3, 0.3
+    else:
+        xyz, p1, p2, layer, cell, _ = lat.ct_specimen(40.0, 0.4, 0.15)
+        E, nu = 110e3, 0.34
+    Kn, Tv = lat.bond_constants(cell, layer, cell.elastic_constants(E, nu, plane_stress=True, layout="row"))
+    g = capi.Lattice(2, xyz, p1, p2, layer, Kn, Tv, cell.particle_volume, cell.nneighbors)
+    y = xyz[:, 1]
+    bottom, top = np.where(y < y.min() + 1e-9)[0], np.where(y > y.max() - 1e-9)[0]
+    gb, gc, gt = g.add_group(bottom), g.add_group(bottom[:1]), g.add_group(top)
+    g.update()
+    r = g.load_step([("disp", gb, 1, 0.0), ("disp", gc, 0, 0.0), ("disp", gt, 1, 1e-3)],
+                    tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_FP64, cg_tol=1e-10)
+    g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_ELIMINATE)
+    g.upload(capi.F_RESIDUAL, np.random.default_rng(5).standard_normal(g.ndof))
+    stream = torch.cuda.ExternalStream(g.stream(), device="cuda:0")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g.reset_stats()
+    g.synchronize()
+    e0.record(stream)
+    it, rr, st = g.solve(capi.PREC_MIXED, 1e-8, maxit=300)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = {"profile_solve": case, "particles": len(xyz), "blocks": g.nblk, "iterations": it, "ms": ms,
+           "us_per_iteration": 1e3 * ms / max(it, 1), "persistent_solves": g.stats()["persistent_solves"],
+           "load_step": r}
+    g.close()
+    print(json.dumps(out))
+    return 0
+
+
 def main(argv=None):
     global ARGS
     ARGS = parse_args(argv)
+    if ARGS.profile_solve:
+        return profile_solve(ARGS.profile_solve)
     if ARGS.impl == "reference":
         return run_reference(ARGS)
     return run_gb300(ARGS)
