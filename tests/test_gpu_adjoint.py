@@ -1,7 +1,8 @@
 """Adjoint of the load step (lpm_backward_step, lpm_apply_jacobian, checkpoints).
 
 - the matrix-free Jacobian product against central differences of the
-  internal force computed by the oracle on the CPU;
+  internal force computed by the oracle on the CPU, beside the reference's
+  analytical stiffness derivative (both variants) on the same state;
 - gradients of a reaction force with respect to the bond constants and to
   (E, nu) against central differences of whole forward runs, within the
   1e-5 relative bound the adjoint is held to;
@@ -10,7 +11,7 @@
 import numpy as np
 import pytest
 
-from lpm_cases import cube, gpu_bcs, lat, make_gpu, make_oracle, oracle, pkg, plate, tension_bcs
+from lpm_cases import cube, dense_from_bsr, gpu_bcs, lat, make_gpu, make_oracle, oracle, pkg, plate, tension_bcs
 
 capi = pkg.capi
 STEP = dict(solver=capi.SOLVER_FATIGUE_STATIC, tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_FP64,
@@ -56,6 +57,20 @@ def test_jacobian_product_matches_central_differences(dim):
     assert np.abs(Hv - fd).max() <= 1e-6 * np.abs(fd).max()
     # the internal force is the gradient of the lattice energy: H is symmetric
     assert abs(u @ Hv - v @ Hu) <= 1e-12 * np.abs(u).sum() * np.abs(Hv).max()
+    # the reference's stiffness derivative (derivative.h, the same file as
+    # benchmark/Stiffness_derivative/derivative.h) is not this Jacobian: it
+    # leaves out the change of the bond directions, and as written its
+    # K_ii[1][0] entries are zero.  Its products differ from the central
+    # differences by orders of magnitude more than the exact Jacobian's.
+    cptr, cidx = g.pattern()
+    err = {"exact Jacobian": np.abs(Hv - fd).max() / np.abs(fd).max()}
+    for name, tangent in (("symmetric tangent", capi.TANGENT_SYMMETRIC), ("tangent as written", capi.TANGENT_AS_WRITTEN)):
+        g.assemble(tangent, capi.BC_NONE)
+        K = dense_from_bsr(cptr, cidx, g.K_bsr(), n, dim)
+        err[name] = np.abs(K @ v - fd).max() / np.abs(fd).max()
+    print("[jacobian] %d-D, random strain of 2e-3: max|product - central difference| / max|central difference|: %s" % (
+        dim, ", ".join("%s %.2e" % kv for kv in err.items())))
+    assert min(err["symmetric tangent"], err["tangent as written"]) >= 100 * err["exact Jacobian"]
     g.close()
 
 
