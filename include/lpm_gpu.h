@@ -325,6 +325,26 @@ int lpm_set_kernel_timing(lpm_handle* h, int on);
 #define LPM_CG_LOOP_GRAPH 1
 #define LPM_CG_LOOP_PERSISTENT 2
 int lpm_set_cg_loop(lpm_handle* h, int mode);
+/* Preconditioner of the mixed-precision solve.  The reference uses Jacobi
+ * (Eigen's DiagonalPreconditioner, solver.h:195-206), the default here.
+ *   LPM_PRECOND_COARSE  Jacobi plus a coarse correction, M^-1 = D^-1 +
+ *                       P (P^T A P)^-1 P^T, with P the rigid-body modes of
+ *                       boxes of particles of edge `box` (model length
+ *                       units, by initial position; 0: an edge that gives
+ *                       about 480 coarse DOFs), zero on eliminated DOFs.
+ *                       The iteration count then depends on the box and no
+ *                       longer grows with the lattice (the full-size notched
+ *                       plate: about 260 iterations against 1,900).  At most
+ *                       1,024 coarse DOFs (LPM_ERR_ARG beyond); the coarse
+ *                       operator and its dense inverse are rebuilt after
+ *                       each assembly.  Needs the assembled symmetric
+ *                       tangent (LPM_ERR_STATE otherwise) and runs the
+ *                       mixed solve as one persistent kernel whatever
+ *                       lpm_set_cg_loop says.  The FP64 solve keeps Jacobi.
+ * The same solution to the solve tolerance; other iterates and counts. */
+#define LPM_PRECOND_JACOBI 0
+#define LPM_PRECOND_COARSE 1
+int lpm_set_preconditioner(lpm_handle* h, int kind, double box);
 /* The handle's CUDA stream (cudaStream_t), for callers that time or order
  * work around the library. */
 int lpm_get_stream(const lpm_handle* h, void** stream);

@@ -13,8 +13,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liblpmgpu.so")
-SOURCES = ["lpm_capi.cu", "lpm_force.cu", "lpm_tangent.cu", "lpm_cg.cu", "lpm_laws.cu", "lpm_noalloc.cu", "lpm_adjoint.cu", "lpm_search.cu", "lpm_mfree.cu"]
-HEADERS = ["lpm_internal.cuh", "lpm_device.cuh", "lpm_cgvec.cuh", "lpm_df.cuh", "lpm_graph.cuh"]
+SOURCES = ["lpm_capi.cu", "lpm_force.cu", "lpm_tangent.cu", "lpm_cg.cu", "lpm_laws.cu", "lpm_noalloc.cu", "lpm_adjoint.cu", "lpm_search.cu", "lpm_mfree.cu", "lpm_coarse.cu"]
+HEADERS = ["lpm_internal.cuh", "lpm_device.cuh", "lpm_cgvec.cuh", "lpm_df.cuh", "lpm_graph.cuh", "lpm_grid.cuh", "lpm_coarse.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no fused multiply-add contraction, so host-side lengths (the
 # initial bond lengths) round like the reference's

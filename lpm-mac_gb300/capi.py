@@ -27,6 +27,7 @@ LAW_ELASTIC, LAW_DAMAGE, LAW_J2, LAW_FATIGUE_HCF, LAW_SOFTENING = 0, 1, 2, 3, 4
 T_PIN, T_XYZ, T_DAMAGE = 1, 2, 3  # tangent fields (lpm_tangent_get)
 OPERATOR_ASSEMBLED, OPERATOR_MATRIX_FREE = 0, 1
 CG_LOOP_AUTO, CG_LOOP_GRAPH, CG_LOOP_PERSISTENT = 0, 1, 2
+PRECOND_JACOBI, PRECOND_COARSE = 0, 1
 _NSTATE = {LAW_ELASTIC: 1, LAW_DAMAGE: 1, LAW_J2: 7, LAW_FATIGUE_HCF: 3, LAW_SOFTENING: 1}
 
 
@@ -139,6 +140,7 @@ def load(build_if_needed=True):
         "lpm_reset_stats": [H],
         "lpm_set_kernel_timing": [H, ctypes.c_int],
         "lpm_set_cg_loop": [H, ctypes.c_int],
+        "lpm_set_preconditioner": [H, ctypes.c_int, ctypes.c_double],
         "lpm_get_stream": [H, ctypes.POINTER(ctypes.c_void_p)],
         "lpm_synchronize": [H],
         "lpm_find_bonds": [ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, i64, ip, ip, ip, i64p],
@@ -177,7 +179,7 @@ def exported_symbols():
             "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_set_operator",
             "lpm_apply_operator", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
-            "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_set_cg_loop", "lpm_get_stream", "lpm_synchronize",
+            "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_set_cg_loop", "lpm_set_preconditioner", "lpm_get_stream", "lpm_synchronize",
             "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_fatigue_run", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
             "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_bond_constants", "lpm_tangent_bond_scrit",
             "lpm_tangent_get",
@@ -511,6 +513,11 @@ class Lattice:
         """CG_LOOP_AUTO (default), CG_LOOP_GRAPH or CG_LOOP_PERSISTENT: how the
         mixed solve runs its iteration loop."""
         self._check(self._L.lpm_set_cg_loop(self.h, int(mode)))
+
+    def set_preconditioner(self, kind, box=0.0):
+        """PRECOND_JACOBI (default) or PRECOND_COARSE (Jacobi plus the rigid-body
+        modes of boxes of edge `box`, 0: automatic) for the mixed solve."""
+        self._check(self._L.lpm_set_preconditioner(self.h, int(kind), float(box)))
 
     def set_kernel_timing(self, on):
         self._check(self._L.lpm_set_kernel_timing(self.h, int(bool(on))))

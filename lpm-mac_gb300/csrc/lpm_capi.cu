@@ -760,6 +760,19 @@ int lpm_set_cg_loop(lpm_handle* h, int mode) {
   return LPM_OK;
 }
 
+int lpm_set_preconditioner(lpm_handle* h, int kind, double box) {
+  if (!h) return LPM_ERR_ARG;
+  if (kind != LPM_PRECOND_JACOBI && kind != LPM_PRECOND_COARSE) return arg_error(h, "unknown preconditioner");
+  if (!(box >= 0.0)) return arg_error(h, "box edge must be zero or positive");
+  if (kind == LPM_PRECOND_COARSE && (box != h->cbox || !h->d.cagg)) {
+    h->cbox = box;
+    h->d.cagg = nullptr;  // aggregates rebuilt on the next solve (the old arrays stay with the handle)
+    h->coarse_valid = false;
+  }
+  h->precond = kind;
+  return LPM_OK;
+}
+
 int lpm_set_kernel_timing(lpm_handle* h, int on) {
   if (!h) return LPM_ERR_ARG;
   h->timing = on != 0;

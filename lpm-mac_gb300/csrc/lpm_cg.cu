@@ -48,9 +48,11 @@
 #include <vector>
 
 #include "lpm_cgvec.cuh"
+#include "lpm_coarse.cuh"
 #include "lpm_device.cuh"
 #include "lpm_df.cuh"
 #include "lpm_graph.cuh"
+#include "lpm_grid.cuh"
 
 namespace lpm {
 namespace {
@@ -590,77 +592,88 @@ struct PcgMixed {
   float *x, *xlo, *r, *rlo, *p, *q, *qlo;
   double *x64, *r64;
   CgScalars* cg;
-  double* partials;          // 6 x gridDim.x
+  double* partials;          // 7 x gridDim.x
   unsigned long long* gbar;  // barrier arrivals, zero at launch
   long long spin_limit;      // polls before a barrier wait gives up
+  // coarse correction (COARSE): z = D^-1 r + P A_c^-1 P^T r (lpm_coarse.cu)
+  const int *cagg, *cmem_ptr, *cmem;
+  const float* coff;
+  const unsigned char* cfixed;  // eliminated DOFs, or null
+  const double* cAinv;
+  double *cyc, *cec;
+  float* cz;
+  int cnagg;
 };
 
-// Polls before a grid-barrier wait gives up: at least 32 ns apart, so more
-// than half a second, against microseconds for a barrier that completes.
-constexpr long long kPcgSpinLimit = 1LL << 24;
-
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* a) {
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
-  return v;
-}
-
-// Grid barrier on a monotone arrival count: the k-th barrier of a launch
-// waits until k * gridDim.x arrivals.  The fence before the arrival and the
-// acquire loads and fence after the wait order every block's writes before
-// the barrier ahead of every read after it.  The wait is bounded; returns
-// false in every thread of the block if it gave up.
-__device__ __forceinline__ bool grid_barrier(unsigned long long* gbar, unsigned long long target, long long limit) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(gbar, 1ULL);
-    int good = 1;
-    long long polls = 0;
-    while (ld_acquire_u64(gbar) < target) {
-      if (++polls > limit) {
-        good = 0;
-        break;
+// z = D^-1 r + P A_c^-1 P^T r for this thread's rows, into a.cz, from r's
+// high words (written before the caller's last barrier).  The restriction
+// y = P^T r and the coarse solve e = A_c^-1 y each take one warp per
+// aggregate and end at a grid barrier; then each row adds P_i e to its
+// Jacobi term.  False if a barrier wait gave up.
+template <int DIM>
+__device__ bool coarse_z(const PcgMixed& a, unsigned long long& target) {
+  constexpr int NM = kModes<DIM>;
+  const int nc = a.cnagg * NM;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int ag = gwarp; ag < a.cnagg; ag += nwarps) {
+    double acc[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) acc[m] = 0.0;
+    for (int t = a.cmem_ptr[ag] + lane; t < a.cmem_ptr[ag + 1]; t += 32) {
+      const int i = a.cmem[t];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        const int64_t q = (int64_t)DIM * i + k;
+        if (a.cfixed && a.cfixed[q]) continue;
+        double w[NM];
+        mode_row<DIM>(k, a.coff[3 * i], a.coff[3 * i + 1], a.coff[3 * i + 2], w);
+        const double rk = (double)__ldcg(&a.r[q]);
+#pragma unroll
+        for (int m = 0; m < NM; ++m) acc[m] += w[m] * rk;
       }
-      __nanosleep(32);
     }
-    __threadfence();
-    ok = good;
+#pragma unroll
+    for (int m = 0; m < NM; ++m) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[m] += __shfl_down_sync(0xffffffffu, acc[m], o);
+      if (lane == 0) a.cyc[ag * NM + m] = acc[m];
+    }
   }
-  __syncthreads();
-  return ok != 0;
-}
-
-// Grid totals of K values per block (valid in thread 0): published in slots
-// slot..slot+K-1 of the partials, then, after the barrier, folded by warp 0
-// of every block in block order and returned in every thread.
-template <int K>
-__device__ __forceinline__ bool grid_allreduce(const double (&v)[K], double* partials, int slot,
-                                               unsigned long long* gbar, unsigned long long& target, long long limit,
-                                               double (&tot)[K]) {
-  __shared__ double res[K];
-  const int G = gridDim.x;
-  if (threadIdx.x == 0)
+  target += (unsigned long long)gridDim.x;
+  if (!grid_barrier(a.gbar, target, a.spin_limit)) return false;
+  for (int ag = gwarp; ag < a.cnagg; ag += nwarps)
+    for (int m = 0; m < NM; ++m) {
+      const double* row = a.cAinv + (int64_t)(ag * NM + m) * nc;
+      double acc = 0.0;
+      for (int c = lane; c < nc; c += 32) acc += __ldg(&row[c]) * __ldcg(&a.cyc[c]);
 #pragma unroll
-    for (int k = 0; k < K; ++k) partials[(int64_t)(slot + k) * G + blockIdx.x] = v[k];
-  target += (unsigned long long)G;
-  if (!grid_barrier(gbar, target, limit)) return false;
-  if (threadIdx.x < 32) {
-    double acc[K];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (lane == 0) a.cec[ag * NM + m] = acc;
+    }
+  target += (unsigned long long)gridDim.x;
+  if (!grid_barrier(a.gbar, target, a.spin_limit)) return false;
+  const int stride = gridDim.x * blockDim.x;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.v.n; row += stride) {
+    const int ag = a.cagg[row];
+    double e[NM];
 #pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.0;
-    for (int b = threadIdx.x; b < G; b += 32)
+    for (int m = 0; m < NM; ++m) e[m] = __ldcg(&a.cec[ag * NM + m]);
 #pragma unroll
-      for (int k = 0; k < K; ++k) acc[k] += __ldcg(&partials[(int64_t)(slot + k) * G + b]);
-    warp_sum<K>(acc);
-    if (threadIdx.x == 0)
+    for (int k = 0; k < DIM; ++k) {
+      const int64_t q = (int64_t)row * DIM + k;
+      float zi = a.invd[q] * a.r[q];
+      if (!(a.cfixed && a.cfixed[q])) {
+        double w[NM];
+        mode_row<DIM>(k, a.coff[3 * row], a.coff[3 * row + 1], a.coff[3 * row + 2], w);
+        double pe = 0.0;
 #pragma unroll
-      for (int k = 0; k < K; ++k) res[k] = acc[k];
+        for (int m = 0; m < NM; ++m) pe += w[m] * e[m];
+        zi += (float)pe;
+      }
+      a.cz[q] = zi;
+    }
   }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < K; ++k) tot[k] = res[k];
   return true;
 }
 
@@ -681,7 +694,7 @@ struct PcgState {
 template <int DIM>
 constexpr int kPcgThreads = DIM == 3 ? 512 : 768;
 
-template <int DIM, bool OFF16>
+template <int DIM, bool OFF16, bool COARSE>
 __global__ void __launch_bounds__(kPcgThreads<DIM>, 1) k_mx_persistent(PcgMixed a) {
   __shared__ PcgState s;
   if (threadIdx.x == 0) {
@@ -706,7 +719,28 @@ __global__ void __launch_bounds__(kPcgThreads<DIM>, 1) k_mx_persistent(PcgMixed 
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long target = 0;
   bool fault = false;
-  while (!s.done) {
+  if (COARSE && !s.done) {
+    // the first direction is the coarse-corrected z of the initial residual
+    if (!coarse_z<DIM>(a, target)) fault = true;
+    if (!fault) {
+      float sz[1] = {0.f}, cz[1] = {0.f};
+      for (int row = t0; row < n; row += stride)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const int64_t i = (int64_t)row * DIM + c;
+          const float zi = a.cz[i];
+          a.p[i] = zi;
+          dot2_acc(sz[0], cz[0], a.r[i], zi);
+          cz[0] = fmaf(a.rlo[i], zi, cz[0]);
+        }
+      double w[1] = {0.0}, tot[1];
+      block_df_sum<1>(sz, cz, w);
+      if (!grid_allreduce<1>(w, a.partials, 6, a.gbar, target, a.spin_limit, tot)) fault = true;
+      if (threadIdx.x == 0 && !fault) s.abs_new = tot[0];
+      __syncthreads();
+    }
+  }
+  while (!s.done && !fault) {
     // q = A p (FP32, double-float output) and p.q; alpha
     {
       float ps = 0.f, pc = 0.f;
@@ -772,10 +806,12 @@ __global__ void __launch_bounds__(kPcgThreads<DIM>, 1) k_mx_persistent(PcgMixed 
             s.ru = 1;
           } else {
             s.rmax = fmax(s.rmax, rn);
-            const double beta = tot[1] / s.abs_new;
-            s.abs_new = tot[1];
-            df_split(beta, s.bh, s.bl);
-            s.zc = 1.f;
+            if (!COARSE) {
+              const double beta = tot[1] / s.abs_new;
+              s.abs_new = tot[1];
+              df_split(beta, s.bh, s.bl);
+              s.zc = 1.f;
+            }
           }
           if (s.it >= s.maxit) s.done = 2;
         }
@@ -783,6 +819,40 @@ __global__ void __launch_bounds__(kPcgThreads<DIM>, 1) k_mx_persistent(PcgMixed 
       __syncthreads();
     }
     if (s.done) break;
+    if (COARSE && !s.ru) {
+      // z with the coarse correction, r.z and beta
+      if (!coarse_z<DIM>(a, target)) {
+        fault = true;
+        break;
+      }
+      float sz[1] = {0.f}, cz[1] = {0.f};
+      for (int row = t0; row < n; row += stride)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+          const int64_t i = (int64_t)row * DIM + c;
+          const float zi = a.cz[i];
+          dot2_acc(sz[0], cz[0], a.r[i], zi);
+          cz[0] = fmaf(a.rlo[i], zi, cz[0]);
+        }
+      double w[1] = {0.0}, tot[1];
+      block_df_sum<1>(sz, cz, w);
+      if (!grid_allreduce<1>(w, a.partials, 6, a.gbar, target, a.spin_limit, tot)) {
+        fault = true;
+        break;
+      }
+      if (threadIdx.x == 0) {
+        if (!isfinite(tot[0])) {
+          s.done = 3;
+        } else {
+          const double beta = tot[0] / s.abs_new;
+          s.abs_new = tot[0];
+          df_split(beta, s.bh, s.bl);
+          s.zc = 1.f;
+        }
+      }
+      __syncthreads();
+      if (s.done) break;
+    }
     if (s.ru) {
       // reliable update: r64 = s b - A64 (x64 + x) and |r64|^2
       double acc[1] = {0.0}, tot[1];
@@ -828,9 +898,24 @@ __global__ void __launch_bounds__(kPcgThreads<DIM>, 1) k_mx_persistent(PcgMixed 
           df_split(ri, rh, rl);
           a.r[i] = rh;
           a.rlo[i] = rl;
-          v[0] += ri * (double)(a.invd[i] * rh);
+          if (!COARSE) v[0] += ri * (double)(a.invd[i] * rh);
           v[1] += ri * (double)a.p[i];
         }
+      if (COARSE) {
+        // the replaced residual's coarse-corrected z (its restriction reads
+        // the other rows' new residual: a barrier first)
+        target += (unsigned long long)gridDim.x;
+        if (!grid_barrier(a.gbar, target, a.spin_limit) || !coarse_z<DIM>(a, target)) {
+          fault = true;
+          break;
+        }
+        for (int row = t0; row < n; row += stride)
+#pragma unroll
+          for (int c = 0; c < DIM; ++c) {
+            const int64_t i = (int64_t)row * DIM + c;
+            v[0] += a.r64[i] * (double)a.cz[i];
+          }
+      }
       block_sum<2>(v);
       if (!grid_allreduce<2>(v, a.partials, 4, a.gbar, target, a.spin_limit, t2)) {
         fault = true;
@@ -856,7 +941,8 @@ __global__ void __launch_bounds__(kPcgThreads<DIM>, 1) k_mx_persistent(PcgMixed 
         for (int c = 0; c < DIM; ++c) {
           const int64_t i = (int64_t)row * DIM + c;
           const float pi = a.p[i];
-          a.p[i] = fmaf(bh, pi, fmaf(bl, pi, __fmul_rn(zc, __fmul_rn(a.invd[i], a.r[i]))));
+          const float zi = COARSE ? a.cz[i] : __fmul_rn(a.invd[i], a.r[i]);
+          a.p[i] = fmaf(bh, pi, fmaf(bl, pi, __fmul_rn(zc, zi)));
         }
       target += (unsigned long long)gridDim.x;
       if (!grid_barrier(a.gbar, target, a.spin_limit)) {
@@ -1273,30 +1359,51 @@ int mixed_grids(lpm_handle* h, const SellView& sv, MixedGrids* mg) {
   return LPM_OK;
 }
 
-// The persistent solve's kernel for the dimension and column format.
+// The persistent solve's kernel for the dimension, column format and
+// preconditioner.
 using PcgFn = void (*)(PcgMixed);
-PcgFn pcg_fn(const SellView& sv, int dim) {
-  const bool o16 = sv.soff != nullptr;
-  if (dim == 3) return o16 ? k_mx_persistent<3, true> : k_mx_persistent<3, false>;
-  return o16 ? k_mx_persistent<2, true> : k_mx_persistent<2, false>;
+template <int DIM>
+PcgFn pcg_fn_dim(bool o16, bool coarse) {
+  if (coarse) return o16 ? k_mx_persistent<DIM, true, true> : k_mx_persistent<DIM, false, true>;
+  return o16 ? k_mx_persistent<DIM, true, false> : k_mx_persistent<DIM, false, false>;
+}
+PcgFn pcg_fn(const SellView& sv, int dim, bool coarse) {
+  return dim == 3 ? pcg_fn_dim<3>(sv.soff != nullptr, coarse) : pcg_fn_dim<2>(sv.soff != nullptr, coarse);
 }
 
 // Launch shape of the persistent mixed solve (persistent_shape); AUTO takes
-// it only when the FP32 operator stays in L2.
-int pcg_grid(lpm_handle* h, const SellView& sv, int* threads_out) {
+// it only when the FP32 operator stays in L2.  The coarse preconditioner
+// runs only here, whatever the loop mode.
+int pcg_grid(lpm_handle* h, const SellView& sv, int* threads_out, bool coarse) {
   const bool keep = (long long)h->nslots * h->dim * h->dim * 4 <= kKeepBytes;
-  return persistent_shape(h, pcg_fn(sv, h->dim), h->dim == 3 ? kPcgThreads<3> : kPcgThreads<2>, keep, 6,
-                          threads_out);
+  const int mode = h->cg_loop;
+  if (coarse) h->cg_loop = LPM_CG_LOOP_PERSISTENT;
+  const int g = persistent_shape(h, pcg_fn(sv, h->dim, coarse), h->dim == 3 ? kPcgThreads<3> : kPcgThreads<2>,
+                                 keep, 7, threads_out);
+  h->cg_loop = mode;
+  return g;
 }
 
-int run_persistent_mixed(lpm_handle* h, const SellView& sv, int grid, int threads) {
+int run_persistent_mixed(lpm_handle* h, const SellView& sv, int grid, int threads, bool coarse) {
   Dev& d = h->d;
   LPM_CUDA(h, cudaMemsetAsync(d.gbar, 0, sizeof(unsigned long long), h->stream));
   PcgMixed a{sv,    d.A32,  d.A64, d.rhs, d.invd32, d.x32, d.x32lo,        d.r32,         d.r32lo,
              d.p32, d.q32,  d.q32lo, d.x64, d.r64,  d.cg,  d.red.partials, d.gbar, kPcgSpinLimit};
+  if (coarse) {
+    a.cagg = d.cagg;
+    a.cmem_ptr = d.cmem_ptr;
+    a.cmem = d.cmem;
+    a.coff = d.coff;
+    a.cfixed = h->last_bc == LPM_BC_ELIMINATE ? d.fixed : nullptr;
+    a.cAinv = d.cAinv;
+    a.cyc = d.cyc;
+    a.cec = d.cec;
+    a.cz = d.cz;
+    a.cnagg = h->cnagg;
+  }
   void* args[] = {&a};
-  LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)pcg_fn(sv, h->dim), dim3(grid), dim3(threads), args, 0,
-                                          h->stream));
+  LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)pcg_fn(sv, h->dim, coarse), dim3(grid), dim3(threads), args,
+                                          0, h->stream));
   LPM_LAUNCHED(h, "k_mx_persistent");
   return LPM_OK;
 }
@@ -1530,11 +1637,26 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   LPM_LAUNCHED(h, "k_mx_init");
   const bool timing = h->timing;
   const size_t ev0 = h->ev_used;
+  const bool coarse = h->precond == LPM_PRECOND_COARSE;
+  if (coarse) {
+    if (h->mf || h->tangent != LPM_TANGENT_SYMMETRIC) {
+      h->err = "coarse preconditioner: needs the assembled symmetric tangent";
+      return LPM_ERR_STATE;
+    }
+    if (!h->coarse_valid) {
+      st = coarse_assemble(h);
+      if (st) return st;
+    }
+  }
   int pthreads = 0;
-  const int pgrid = timing ? 0 : pcg_grid(h, sv, &pthreads);
+  const int pgrid = timing && !coarse ? 0 : pcg_grid(h, sv, &pthreads, coarse);
+  if (coarse && pgrid <= 0) {
+    h->err = "coarse preconditioner: the persistent solve cannot be launched on this device";
+    return LPM_ERR_STATE;
+  }
   if (pgrid > 0) {
     // the whole iteration loop as one persistent kernel
-    st = run_persistent_mixed(h, sv, pgrid, pthreads);
+    st = run_persistent_mixed(h, sv, pgrid, pthreads, coarse);
     if (st) return st;
   } else if (!timing) {
     // the whole iteration loop as one graph launch
@@ -1549,7 +1671,7 @@ int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, do
   // flag once per batch of iterations
   const Spmv32Fn spmv32 = spmv32_fn(h, sv);
   long long batch = 8;
-  for (; timing;) {
+  for (; timing && pgrid <= 0;) {
     for (long long k = 0; k < batch; ++k) {
       cudaEvent_t e0 = nullptr, e1 = nullptr;
       if (timing) {

@@ -1,0 +1,337 @@
+// Coarse-space preconditioner of the mixed solve (lpm_set_preconditioner):
+//   M^-1 = D^-1 + P A_c^-1 P^T,   A_c = P^T A P,
+// additive two-level Schwarz with Jacobi as its one-level part.  The columns
+// of P are the rigid-body modes (2-D: two translations and the rotation;
+// 3-D: three translations and three rotations) of boxes of particles
+// (aggregates), zero on eliminated DOFs.  Jacobi leaves the smooth,
+// long-wavelength error of the lattice to the CG iterations; the coarse
+// correction takes it out, so the iteration count stops growing with the
+// lattice's size and depends on the box's instead.
+//
+// Set-up once per handle (host): the aggregates from the initial positions
+// (boxes of an edge `box`, numbered in the order of their first particle),
+// their members, each particle's offset from its aggregate's centroid, and
+// the aggregate pairs the operator's pattern couples.  Once per assembly
+// (device): A_c in FP64, one warp per aggregate pair summing over the pair's
+// blocks in a fixed order; modes without stiffness (an aggregate whose DOFs
+// are all eliminated, the rotation of a lone particle) set aside; then the
+// inverse by Gauss-Jordan elimination without pivoting (A_c is symmetric
+// positive definite on the remaining modes), one cooperative launch with a
+// grid barrier per column.  The solve applies it in k_mx_persistent.
+#include <algorithm>
+#include <cmath>
+#include <unordered_map>
+#include <vector>
+
+#include "lpm_device.cuh"
+#include "lpm_coarse.cuh"
+#include "lpm_grid.cuh"
+
+namespace lpm {
+
+// Most coarse DOFs: the dense inverse (8 MB in FP64 at 1,024) stays in L2,
+// and its Gauss-Jordan elimination takes one grid barrier per column.
+constexpr int kCoarseMax = 1024;
+// Coarse DOFs aimed at when the box edge is chosen automatically.
+constexpr int kCoarseTarget = 480;
+
+namespace {
+
+// A_c block (a, b) = sum over i in a, blocks (i, j) with j in b, of
+// P_i^T A_ij P_j.  One warp per pair: the lanes take the members of a in
+// turn and walk each member's slots in order; the lane sums are then folded
+// by a fixed shuffle tree.
+template <int DIM>
+__global__ void __launch_bounds__(128) k_coarse_pairs(int npair, const int* __restrict__ pairs,
+                                                      const int* __restrict__ mem_ptr, const int* __restrict__ mem,
+                                                      const int* __restrict__ agg, const float* __restrict__ off,
+                                                      const unsigned char* __restrict__ fixed,
+                                                      const int64_t* __restrict__ sell_ptr,
+                                                      const int* __restrict__ scol, const int* __restrict__ rowlen,
+                                                      const double* __restrict__ A, int64_t nslots, int nc,
+                                                      double* __restrict__ Ac) {
+  constexpr int NM = kModes<DIM>;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= npair) return;
+  const int a = pairs[2 * warp], b = pairs[2 * warp + 1];
+  double c[NM][NM];
+#pragma unroll
+  for (int m = 0; m < NM; ++m)
+#pragma unroll
+    for (int q = 0; q < NM; ++q) c[m][q] = 0.0;
+  for (int t = mem_ptr[a] + lane; t < mem_ptr[a + 1]; t += 32) {
+    const int i = mem[t];
+    double wi[DIM][NM];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) {
+      mode_row<DIM>(r, off[3 * i], off[3 * i + 1], off[3 * i + 2], wi[r]);
+      if (fixed && fixed[(int64_t)DIM * i + r])
+#pragma unroll
+        for (int m = 0; m < NM; ++m) wi[r][m] = 0.0;
+    }
+    const int len = rowlen[i];
+    const SellRow sr = sell_row(sell_ptr, i);
+    for (int k = 0; k < len; ++k) {
+      const int64_t s = k < sr.g4 ? sr.base + (int64_t)(k / kVec) * (kSlice * kVec) + (k % kVec)
+                                  : sr.tail + (int64_t)(k - sr.g4) * kSlice;
+      const int j = scol[s];
+      if (agg[j] != b) continue;
+      double wj[DIM][NM];
+#pragma unroll
+      for (int r = 0; r < DIM; ++r) {
+        mode_row<DIM>(r, off[3 * j], off[3 * j + 1], off[3 * j + 2], wj[r]);
+        if (fixed && fixed[(int64_t)DIM * j + r])
+#pragma unroll
+          for (int m = 0; m < NM; ++m) wj[r][m] = 0.0;
+      }
+      // (A_ij P_j)[r][q], then P_i^T times it
+#pragma unroll
+      for (int r = 0; r < DIM; ++r) {
+        double ap[NM];
+#pragma unroll
+        for (int q = 0; q < NM; ++q) ap[q] = 0.0;
+#pragma unroll
+        for (int s2 = 0; s2 < DIM; ++s2) {
+          const double v = A[(int64_t)(r * DIM + s2) * nslots + s];
+#pragma unroll
+          for (int q = 0; q < NM; ++q) ap[q] += v * wj[s2][q];
+        }
+#pragma unroll
+        for (int m = 0; m < NM; ++m)
+#pragma unroll
+          for (int q = 0; q < NM; ++q) c[m][q] += wi[r][m] * ap[q];
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < NM; ++m)
+#pragma unroll
+    for (int q = 0; q < NM; ++q) {
+      double v = c[m][q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) Ac[(int64_t)(a * NM + m) * nc + b * NM + q] = v;
+    }
+}
+
+// Modes without stiffness: a diagonal entry at most 1e-12 of the largest.
+// Their rows and columns become those of the identity for the elimination
+// (the inverse's are cleared afterwards); `active` records which are kept.
+__global__ void k_coarse_guard(int nc, double* __restrict__ Ac, int* __restrict__ active) {
+  __shared__ double smax[32];
+  double m = 0.0;
+  for (int q = threadIdx.x; q < nc; q += blockDim.x) m = fmax(m, fabs(Ac[(int64_t)q * nc + q]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = m;
+  __syncthreads();
+  m = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, smax[w]);
+  for (int q = threadIdx.x; q < nc; q += blockDim.x) active[q] = fabs(Ac[(int64_t)q * nc + q]) > 1e-12 * m ? 1 : 0;
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < (int64_t)nc * nc; e += blockDim.x) {
+    const int r = (int)(e / nc), c = (int)(e % nc);
+    if (!active[r] || !active[c]) Ac[e] = r == c ? 1.0 : 0.0;
+  }
+}
+
+// In-place Gauss-Jordan inversion without pivoting, ping-ponged between two
+// buffers (step k reads one and writes the other), one grid barrier per
+// step.  Afterwards the inverse is in X when nc is even, else in Y; the
+// rows and columns of inactive modes are cleared.
+__global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restrict__ active,
+                                unsigned long long* gbar, long long spin_limit, int* fault) {
+  const int64_t nn = (int64_t)nc * nc;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long target = 0;
+  for (int k = 0; k < nc; ++k) {
+    const double* src = (k & 1) ? Y : X;
+    double* dst = (k & 1) ? X : Y;
+    const double piv = __ldcg(&src[(int64_t)k * nc + k]);
+    for (int64_t e = t0; e < nn; e += stride) {
+      const int i = (int)(e / nc), j = (int)(e % nc);
+      double v;
+      if (i == k)
+        v = j == k ? 1.0 / piv : __ldcg(&src[e]) / piv;
+      else if (j == k)
+        v = -__ldcg(&src[e]) / piv;
+      else
+        v = __ldcg(&src[e]) - __ldcg(&src[(int64_t)i * nc + k]) * __ldcg(&src[(int64_t)k * nc + j]) / piv;
+      dst[e] = v;
+    }
+    target += gridDim.x;
+    if (!grid_barrier(gbar, target, spin_limit)) {
+      if (threadIdx.x == 0) atomicExch(fault, 1);
+      return;
+    }
+  }
+  double* res = (nc & 1) ? Y : X;
+  for (int64_t e = t0; e < nn; e += stride) {
+    const int i = (int)(e / nc), j = (int)(e % nc);
+    if (!active[i] || !active[j]) res[e] = 0.0;
+  }
+}
+
+}  // namespace
+
+int coarse_setup(lpm_handle* h) {
+  Dev& d = h->d;
+  const int n = h->n, dim = h->dim, nm = dim == 3 ? 6 : 3;
+  std::vector<double> x0((size_t)3 * n);
+  LPM_CUDA(h, cudaMemcpyAsync(x0.data(), d.x0, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
+  std::vector<int64_t> cptr((size_t)n + 1);
+  std::vector<int> cidx((size_t)h->nblk);
+  LPM_CUDA(h, cudaMemcpyAsync(cptr.data(), d.cptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(cidx.data(), d.cidx, sizeof(int) * h->nblk, cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  double lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = hi[k] = n ? x0[k] : 0.0;
+    for (int i = 0; i < n; ++i) {
+      lo[k] = std::min(lo[k], x0[3 * i + k]);
+      hi[k] = std::max(hi[k], x0[3 * i + k]);
+    }
+  }
+  double edge = h->cbox;
+  if (!(edge > 0.0)) {
+    double vol = 1.0;
+    for (int k = 0; k < dim; ++k) vol *= std::max(hi[k] - lo[k], 1e-300);
+    edge = std::pow(vol / std::max(1, kCoarseTarget / nm), 1.0 / dim);
+  }
+  std::unordered_map<int64_t, int> box_id;
+  std::vector<int> agg((size_t)n);
+  for (int i = 0; i < n; ++i) {
+    int64_t key = 0;
+    for (int k = 0; k < dim; ++k) key = key * 2000003 + (int64_t)std::floor((x0[3 * i + k] - lo[k]) / edge);
+    auto it = box_id.emplace(key, (int)box_id.size()).first;
+    agg[(size_t)i] = it->second;
+  }
+  const int nagg = (int)box_id.size();
+  if ((long long)nagg * nm > kCoarseMax) {
+    h->err = "coarse preconditioner: " + std::to_string(nagg) + " aggregates exceed " +
+             std::to_string(kCoarseMax / nm) + "; give a larger box";
+    return LPM_ERR_ARG;
+  }
+  std::vector<int> mem_ptr((size_t)nagg + 1, 0), mem((size_t)n);
+  for (int i = 0; i < n; ++i) mem_ptr[(size_t)agg[(size_t)i] + 1]++;
+  for (int a = 0; a < nagg; ++a) mem_ptr[(size_t)a + 1] += mem_ptr[(size_t)a];
+  std::vector<int> fill(mem_ptr.begin(), mem_ptr.end() - 1);
+  std::vector<double> cen((size_t)3 * nagg, 0.0);
+  for (int i = 0; i < n; ++i) {
+    const int a = agg[(size_t)i];
+    mem[(size_t)fill[(size_t)a]++] = i;
+    for (int k = 0; k < 3; ++k) cen[(size_t)3 * a + k] += x0[(size_t)3 * i + k];
+  }
+  std::vector<float> off((size_t)3 * n);
+  for (int a = 0; a < nagg; ++a)
+    for (int k = 0; k < 3; ++k) cen[(size_t)3 * a + k] /= std::max(1, mem_ptr[(size_t)a + 1] - mem_ptr[(size_t)a]);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k)
+      off[(size_t)3 * i + k] = (float)(x0[(size_t)3 * i + k] - cen[(size_t)3 * agg[(size_t)i] + k]);
+  // aggregate pairs coupled by the pattern, in order
+  std::vector<int> pairs;
+  std::vector<int> seen((size_t)nagg, -1), nbr;
+  for (int a = 0; a < nagg; ++a) {
+    nbr.clear();
+    for (int t = mem_ptr[(size_t)a]; t < mem_ptr[(size_t)a + 1]; ++t) {
+      const int i = mem[(size_t)t];
+      for (int64_t q = cptr[(size_t)i]; q < cptr[(size_t)i + 1]; ++q) {
+        const int b = agg[(size_t)cidx[(size_t)q]];
+        if (seen[(size_t)b] != a) {
+          seen[(size_t)b] = a;
+          nbr.push_back(b);
+        }
+      }
+    }
+    std::sort(nbr.begin(), nbr.end());
+    for (int b : nbr) {
+      pairs.push_back(a);
+      pairs.push_back(b);
+    }
+  }
+  const int nc = nagg * nm;
+  const int64_t ndof = (int64_t)n * dim;
+  d.cagg = (int*)dev_alloc(h, sizeof(int) * n);
+  d.cmem_ptr = (int*)dev_alloc(h, sizeof(int) * (nagg + 1));
+  d.cmem = (int*)dev_alloc(h, sizeof(int) * n);
+  d.cpair = (int*)dev_alloc(h, sizeof(int) * std::max<size_t>(pairs.size(), 1));
+  d.coff = (float*)dev_alloc(h, sizeof(float) * 3 * n);
+  d.cA = (double*)dev_alloc(h, sizeof(double) * (size_t)nc * nc);
+  d.cA2 = (double*)dev_alloc(h, sizeof(double) * (size_t)nc * nc);
+  d.cact = (int*)dev_alloc(h, sizeof(int) * nc);
+  d.cyc = (double*)dev_alloc(h, sizeof(double) * nc);
+  d.cec = (double*)dev_alloc(h, sizeof(double) * nc);
+  d.cz = (float*)dev_alloc(h, sizeof(float) * ndof);
+  d.cfault = (int*)dev_alloc(h, sizeof(int));
+  if (!d.cagg || !d.cmem_ptr || !d.cmem || !d.cpair || !d.coff || !d.cA || !d.cA2 || !d.cact || !d.cyc || !d.cec ||
+      !d.cz || !d.cfault)
+    return LPM_ERR_NOMEM;
+  LPM_CUDA(h, cudaMemcpyAsync(d.cagg, agg.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.cmem_ptr, mem_ptr.data(), sizeof(int) * (nagg + 1), cudaMemcpyHostToDevice,
+                              h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.cmem, mem.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  if (!pairs.empty())
+    LPM_CUDA(h, cudaMemcpyAsync(d.cpair, pairs.data(), sizeof(int) * pairs.size(), cudaMemcpyHostToDevice,
+                                h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.coff, off.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->cnagg = nagg;
+  h->cnc = nc;
+  h->cnpair = (int)(pairs.size() / 2);
+  h->cedge = edge;
+  h->coarse_valid = false;
+  return LPM_OK;
+}
+
+// A_c of the current operator and its inverse (in d.cAinv).
+int coarse_assemble(lpm_handle* h) {
+  Dev& d = h->d;
+  if (!d.cagg) {
+    const int st = coarse_setup(h);
+    if (st) return st;
+  }
+  const int nc = h->cnc;
+  const unsigned char* fixed = h->last_bc == LPM_BC_ELIMINATE ? d.fixed : nullptr;
+  LPM_CUDA(h, cudaMemsetAsync(d.cA, 0, sizeof(double) * (size_t)nc * nc, h->stream));
+  const int warps_per_block = 4;
+  const int G = (h->cnpair + warps_per_block - 1) / warps_per_block;
+  if (G > 0) {
+    if (h->dim == 3)
+      k_coarse_pairs<3><<<G, 32 * warps_per_block, 0, h->stream>>>(h->cnpair, d.cpair, d.cmem_ptr, d.cmem, d.cagg,
+                                                                  d.coff, fixed, d.sell_ptr, d.scol, d.rowlen,
+                                                                  d.A64, h->nslots, nc, d.cA);
+    else
+      k_coarse_pairs<2><<<G, 32 * warps_per_block, 0, h->stream>>>(h->cnpair, d.cpair, d.cmem_ptr, d.cmem, d.cagg,
+                                                                  d.coff, fixed, d.sell_ptr, d.scol, d.rowlen,
+                                                                  d.A64, h->nslots, nc, d.cA);
+    LPM_LAUNCHED(h, "k_coarse_pairs");
+  }
+  k_coarse_guard<<<1, 1024, 0, h->stream>>>(nc, d.cA, d.cact);
+  LPM_LAUNCHED(h, "k_coarse_guard");
+  if (!h->sms && cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess)
+    h->sms = 1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coarse_invert, 256, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const long long want = ((long long)nc * nc + 255) / 256;
+  const int grid = (int)std::max<long long>(1, std::min<long long>((long long)h->sms * per_sm, want));
+  LPM_CUDA(h, cudaMemsetAsync(d.gbar, 0, sizeof(unsigned long long), h->stream));
+  LPM_CUDA(h, cudaMemsetAsync(d.cfault, 0, sizeof(int), h->stream));
+  long long spin = kPcgSpinLimit;
+  int ncv = nc;
+  void* args[] = {&ncv, &d.cA, &d.cA2, &d.cact, &d.gbar, &spin, &d.cfault};
+  LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_coarse_invert, dim3(grid), dim3(256), args, 0, h->stream));
+  LPM_LAUNCHED(h, "k_coarse_invert");
+  int fault = 0;
+  LPM_CUDA(h, cudaMemcpyAsync(&fault, d.cfault, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  LPM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (fault) {
+    h->err = "coarse preconditioner: a grid-barrier wait gave up in the inversion";
+    return LPM_ERR_STATE;
+  }
+  d.cAinv = (nc & 1) ? d.cA2 : d.cA;
+  h->coarse_valid = true;
+  return LPM_OK;
+}
+
+}  // namespace lpm

@@ -147,6 +147,15 @@ struct Dev {
   RedBuf red;
   CgScalars* cg;   // device scalars
   unsigned long long* gbar;  // persistent solve: grid-barrier arrivals (zeroed before each launch)
+  // coarse-space preconditioner (lpm_coarse.cu): aggregate of each particle,
+  // members of each aggregate, coupled aggregate pairs, offsets from the
+  // aggregate centroids; the coarse operator and its inverse (dense, nc x nc),
+  // the modes kept, the restriction and coarse solution, the preconditioned
+  // residual
+  int *cagg, *cmem_ptr, *cmem, *cpair, *cact, *cfault;
+  float* coff;
+  double *cA, *cA2, *cAinv, *cyc, *cec;
+  float* cz;
   double* norms;   // device results of small reductions [8]
   // per-particle flags for the BC elimination
   unsigned char* fixed;
@@ -224,6 +233,12 @@ struct lpm_handle {
   lpm_stats stats{};
   bool timing = false;
   int cg_loop = LPM_CG_LOOP_AUTO;  // how the solves run their iteration loop (lpm_set_cg_loop)
+  int precond = LPM_PRECOND_JACOBI;  // preconditioner of the mixed solve (lpm_set_preconditioner)
+  double cbox = 0;                   // requested aggregate edge (0: chosen from the coarse target)
+  double cedge = 0;                  // edge in use
+  int cnagg = 0, cnc = 0, cnpair = 0;
+  bool coarse_valid = false;         // the coarse inverse matches the operator
+  int last_bc = -1;                  // BC mode of the last assembly
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   std::vector<void*> allocations;
@@ -280,6 +295,10 @@ int mf_launch_residual(lpm_handle* h);
 int mf_graph_product(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, bool fp32, const void* p, void* q,
                      float* qlo, cudaGraphNode_t* last);
 int mf_graph_residual(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, cudaGraphNode_t* last);
+// coarse-space preconditioner (lpm_coarse.cu): aggregates once per handle,
+// the coarse operator's inverse once per assembly
+int coarse_setup(lpm_handle* h);
+int coarse_assemble(lpm_handle* h);
 // solvers (lpm_cg.cu)
 int solve_fp64(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);
 int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);

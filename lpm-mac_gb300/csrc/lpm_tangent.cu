@@ -460,6 +460,8 @@ int launch_assemble(lpm_handle* h, int tangent, int bc) {
   }
   h->have_K = true;
   h->a32_valid = false;
+  h->coarse_valid = false;
+  h->last_bc = bc;
   h->tangent = tangent;
   return LPM_OK;
 }
