@@ -34,6 +34,8 @@ Reported (one JSON line on rank 0):
                the one step in which the first bonds soften (about 170
                damage rounds); --softening-steps 4 times the crack's burst
                too (minutes)
+  softening_coarse  the same steps with the coarse-space preconditioner
+               (Jacobi plus rigid-body modes of boxes of particles)
   j2_sensitivity  cost of carrying d/d(yield stress) and d/d(hardening)
                through J2 load steps of a BCC polycrystal (40^3 cells)
   polycrystal  configuration 4 at full size (BCC 60^3 cells, 20 grains):
@@ -419,7 +421,7 @@ def fatigue_cost(capi, local, cycles=3):
             "persistent_solves": persistent}
 
 
-def softening_cost(capi, local, steps=4, max_warm=15):
+def softening_cost(capi, local, steps=4, max_warm=15, precond=None):
     """Configuration 3 at full size: the single-edge-notched hexagonal plate
     (401 rows of 201/200 particles, 0.1 mm spacing, crack over 0.3 W),
     softening bond law (alpha 3) with Weibull(k = 10, lambda = 1.2e-3)
@@ -437,6 +439,8 @@ def softening_cost(capi, local, steps=4, max_warm=15):
     g = capi.Lattice(2, xyz, p1, p2, layer, Kn, Tv, cell.particle_volume, cell.nneighbors)
     g.set_law(capi.LAW_SOFTENING, [3.0, 1.0e-3])
     g.upload(capi.B_SCRIT, scrit)
+    if precond is not None:
+        g.set_preconditioner(precond, 0.0)
     g.update()
     c = xyz[:, 1]
     bottom, top = np.where(c < c.min() + 1e-9)[0], np.where(c > c.max() - 1e-9)[0]
@@ -473,7 +477,9 @@ def softening_cost(capi, local, steps=4, max_warm=15):
             "cg_iters_per_step": statistics.mean(r["cg_iters"] for r in recs),
             "softened_bonds": int((d > 0).sum()), "broken_bonds": int((d >= 1).sum()),
             "precision": "mixed", "solver": "static with damage rounds, eliminated tangent",
-            "us_per_cg_iteration": 1e3 * ms / max(1, sum(r["cg_iters"] for r in recs)), "persistent_solves": persistent}
+            "us_per_cg_iteration": 1e3 * ms / max(1, sum(r["cg_iters"] for r in recs)), "persistent_solves": persistent,
+            "preconditioner": "Jacobi (the reference's)" if precond is None else
+            "Jacobi plus rigid-body modes of particle boxes (lpm_set_preconditioner, automatic box)"}
 
 
 def j2_sensitivity_cost(capi, local, ncell=40, steps=4):
@@ -918,6 +924,8 @@ def run_gb300(args):
     run_leg(line, "fatigue", fatigue_cost, capi, local)
     if args.softening_steps > 0:
         run_leg(line, "softening", softening_cost, capi, local, steps=args.softening_steps)
+        run_leg(line, "softening_coarse", softening_cost, capi, local, steps=args.softening_steps,
+                precond=capi.PRECOND_COARSE)
     run_leg(line, "j2_sensitivity", j2_sensitivity_cost, capi, local)
     run_leg(line, "polycrystal", polycrystal_cost, capi, local)
     g.close()

@@ -599,7 +599,7 @@ struct PcgMixed {
   const int *cagg, *cmem_ptr, *cmem;
   const float* coff;
   const unsigned char* cfixed;  // eliminated DOFs, or null
-  const double* cAinv;
+  const float* cAinv;  // FP32 inverse of A_c
   double *cyc, *cec;
   float* cz;
   int cnagg;
@@ -607,69 +607,73 @@ struct PcgMixed {
 
 // z = D^-1 r + P A_c^-1 P^T r for this thread's rows, into a.cz, from r's
 // high words (written before the caller's last barrier).  The restriction
-// y = P^T r and the coarse solve e = A_c^-1 y each take one warp per
-// aggregate and end at a grid barrier; then each row adds P_i e to its
+// y = P^T r and the coarse solve e = A_c^-1 y each take one block per
+// aggregate (the members, or the columns of A_c^-1, spread over the block's
+// threads, in FP32 with compensated sums reduced over the block in a fixed
+// order: GB300's FP64 pipe would make these steps cost more than the
+// product) and end at a grid barrier; then each row adds P_i e to its
 // Jacobi term.  False if a barrier wait gave up.
 template <int DIM>
 __device__ bool coarse_z(const PcgMixed& a, unsigned long long& target) {
   constexpr int NM = kModes<DIM>;
   const int nc = a.cnagg * NM;
-  const int lane = threadIdx.x & 31;
-  const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int ag = gwarp; ag < a.cnagg; ag += nwarps) {
-    double acc[NM];
+  for (int ag = blockIdx.x; ag < a.cnagg; ag += gridDim.x) {
+    float sm[NM], cm[NM];
 #pragma unroll
-    for (int m = 0; m < NM; ++m) acc[m] = 0.0;
-    for (int t = a.cmem_ptr[ag] + lane; t < a.cmem_ptr[ag + 1]; t += 32) {
+    for (int m = 0; m < NM; ++m) sm[m] = cm[m] = 0.f;
+    for (int t = a.cmem_ptr[ag] + threadIdx.x; t < a.cmem_ptr[ag + 1]; t += blockDim.x) {
       const int i = a.cmem[t];
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
         const int64_t q = (int64_t)DIM * i + k;
         if (a.cfixed && a.cfixed[q]) continue;
-        double w[NM];
-        mode_row<DIM>(k, a.coff[3 * i], a.coff[3 * i + 1], a.coff[3 * i + 2], w);
-        const double rk = (double)__ldcg(&a.r[q]);
+        float w[NM];
+        mode_row<DIM, float>(k, a.coff[3 * i], a.coff[3 * i + 1], a.coff[3 * i + 2], w);
+        const float rk = __ldcg(&a.r[q]);
 #pragma unroll
-        for (int m = 0; m < NM; ++m) acc[m] += w[m] * rk;
+        for (int m = 0; m < NM; ++m) dot2_acc(sm[m], cm[m], w[m], rk);
       }
     }
+    double y[NM];
+    block_df_sum<NM>(sm, cm, y);
+    if (threadIdx.x == 0)
 #pragma unroll
-    for (int m = 0; m < NM; ++m) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc[m] += __shfl_down_sync(0xffffffffu, acc[m], o);
-      if (lane == 0) a.cyc[ag * NM + m] = acc[m];
-    }
+      for (int m = 0; m < NM; ++m) a.cyc[ag * NM + m] = y[m];
   }
   target += (unsigned long long)gridDim.x;
   if (!grid_barrier(a.gbar, target, a.spin_limit)) return false;
-  for (int ag = gwarp; ag < a.cnagg; ag += nwarps)
-    for (int m = 0; m < NM; ++m) {
-      const double* row = a.cAinv + (int64_t)(ag * NM + m) * nc;
-      double acc = 0.0;
-      for (int c = lane; c < nc; c += 32) acc += __ldg(&row[c]) * __ldcg(&a.cyc[c]);
+  for (int ag = blockIdx.x; ag < a.cnagg; ag += gridDim.x) {
+    float sm[NM], cm[NM];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-      if (lane == 0) a.cec[ag * NM + m] = acc;
+    for (int m = 0; m < NM; ++m) sm[m] = cm[m] = 0.f;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+      const float yc = (float)__ldcg(&a.cyc[c]);
+#pragma unroll
+      for (int m = 0; m < NM; ++m) dot2_acc(sm[m], cm[m], __ldg(&a.cAinv[(int64_t)(ag * NM + m) * nc + c]), yc);
     }
+    double e[NM];
+    block_df_sum<NM>(sm, cm, e);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int m = 0; m < NM; ++m) a.cec[ag * NM + m] = e[m];
+  }
   target += (unsigned long long)gridDim.x;
   if (!grid_barrier(a.gbar, target, a.spin_limit)) return false;
   const int stride = gridDim.x * blockDim.x;
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.v.n; row += stride) {
     const int ag = a.cagg[row];
-    double e[NM];
+    float e[NM];
 #pragma unroll
-    for (int m = 0; m < NM; ++m) e[m] = __ldcg(&a.cec[ag * NM + m]);
+    for (int m = 0; m < NM; ++m) e[m] = (float)__ldcg(&a.cec[ag * NM + m]);
 #pragma unroll
     for (int k = 0; k < DIM; ++k) {
       const int64_t q = (int64_t)row * DIM + k;
       float zi = a.invd[q] * a.r[q];
       if (!(a.cfixed && a.cfixed[q])) {
-        double w[NM];
-        mode_row<DIM>(k, a.coff[3 * row], a.coff[3 * row + 1], a.coff[3 * row + 2], w);
-        double pe = 0.0;
+        float w[NM];
+        mode_row<DIM, float>(k, a.coff[3 * row], a.coff[3 * row + 1], a.coff[3 * row + 2], w);
 #pragma unroll
-        for (int m = 0; m < NM; ++m) pe += w[m] * e[m];
-        zi += (float)pe;
+        for (int m = 0; m < NM; ++m) zi = fmaf(w[m], e[m], zi);
       }
       a.cz[q] = zi;
     }
@@ -1395,7 +1399,7 @@ int run_persistent_mixed(lpm_handle* h, const SellView& sv, int grid, int thread
     a.cmem = d.cmem;
     a.coff = d.coff;
     a.cfixed = h->last_bc == LPM_BC_ELIMINATE ? d.fixed : nullptr;
-    a.cAinv = d.cAinv;
+    a.cAinv = d.cAinv32;
     a.cyc = d.cyc;
     a.cec = d.cec;
     a.cz = d.cz;

@@ -38,12 +38,12 @@ constexpr int kCoarseTarget = 480;
 namespace {
 
 // A_c block (a, b) = sum over i in a, blocks (i, j) with j in b, of
-// P_i^T A_ij P_j.  One warp per pair: the lanes take the members of a in
-// turn and walk each member's slots in order; the lane sums are then folded
-// by a fixed shuffle tree.
+// P_i^T A_ij P_j.  One warp per pair: the lanes take the pair's rows (the
+// members of a with a block in b) in turn and walk each row's slots in
+// order; the lane sums are then folded by a fixed shuffle tree.
 template <int DIM>
 __global__ void __launch_bounds__(128) k_coarse_pairs(int npair, const int* __restrict__ pairs,
-                                                      const int* __restrict__ mem_ptr, const int* __restrict__ mem,
+                                                      const int* __restrict__ prow_ptr, const int* __restrict__ prow,
                                                       const int* __restrict__ agg, const float* __restrict__ off,
                                                       const unsigned char* __restrict__ fixed,
                                                       const int64_t* __restrict__ sell_ptr,
@@ -59,12 +59,12 @@ __global__ void __launch_bounds__(128) k_coarse_pairs(int npair, const int* __re
   for (int m = 0; m < NM; ++m)
 #pragma unroll
     for (int q = 0; q < NM; ++q) c[m][q] = 0.0;
-  for (int t = mem_ptr[a] + lane; t < mem_ptr[a + 1]; t += 32) {
-    const int i = mem[t];
+  for (int t = prow_ptr[warp] + lane; t < prow_ptr[warp + 1]; t += 32) {
+    const int i = prow[t];
     double wi[DIM][NM];
 #pragma unroll
     for (int r = 0; r < DIM; ++r) {
-      mode_row<DIM>(r, off[3 * i], off[3 * i + 1], off[3 * i + 2], wi[r]);
+      mode_row<DIM, double>(r, off[3 * i], off[3 * i + 1], off[3 * i + 2], wi[r]);
       if (fixed && fixed[(int64_t)DIM * i + r])
 #pragma unroll
         for (int m = 0; m < NM; ++m) wi[r][m] = 0.0;
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(128) k_coarse_pairs(int npair, const int* __re
       double wj[DIM][NM];
 #pragma unroll
       for (int r = 0; r < DIM; ++r) {
-        mode_row<DIM>(r, off[3 * j], off[3 * j + 1], off[3 * j + 2], wj[r]);
+        mode_row<DIM, double>(r, off[3 * j], off[3 * j + 1], off[3 * j + 2], wj[r]);
         if (fixed && fixed[(int64_t)DIM * j + r])
 #pragma unroll
           for (int m = 0; m < NM; ++m) wj[r][m] = 0.0;
@@ -137,9 +137,9 @@ __global__ void k_coarse_guard(int nc, double* __restrict__ Ac, int* __restrict_
 
 // In-place Gauss-Jordan inversion without pivoting, ping-ponged between two
 // buffers (step k reads one and writes the other), one grid barrier per
-// step.  Afterwards the inverse is in X when nc is even, else in Y; the
-// rows and columns of inactive modes are cleared.
-__global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restrict__ active,
+// step.  The inverse, with the rows and columns of inactive modes cleared,
+// is rounded to FP32 into inv32 (the preconditioner needs no more).
+__global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restrict__ active, float* inv32,
                                 unsigned long long* gbar, long long spin_limit, int* fault) {
   const int64_t nn = (int64_t)nc * nc;
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
@@ -147,16 +147,16 @@ __global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restr
   for (int k = 0; k < nc; ++k) {
     const double* src = (k & 1) ? Y : X;
     double* dst = (k & 1) ? X : Y;
-    const double piv = __ldcg(&src[(int64_t)k * nc + k]);
+    const double rp = 1.0 / __ldcg(&src[(int64_t)k * nc + k]);
     for (int64_t e = t0; e < nn; e += stride) {
       const int i = (int)(e / nc), j = (int)(e % nc);
       double v;
       if (i == k)
-        v = j == k ? 1.0 / piv : __ldcg(&src[e]) / piv;
+        v = j == k ? rp : __ldcg(&src[e]) * rp;
       else if (j == k)
-        v = -__ldcg(&src[e]) / piv;
+        v = -__ldcg(&src[e]) * rp;
       else
-        v = __ldcg(&src[e]) - __ldcg(&src[(int64_t)i * nc + k]) * __ldcg(&src[(int64_t)k * nc + j]) / piv;
+        v = __ldcg(&src[e]) - __ldcg(&src[(int64_t)i * nc + k]) * rp * __ldcg(&src[(int64_t)k * nc + j]);
       dst[e] = v;
     }
     target += gridDim.x;
@@ -165,10 +165,10 @@ __global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restr
       return;
     }
   }
-  double* res = (nc & 1) ? Y : X;
+  const double* res = (nc & 1) ? Y : X;
   for (int64_t e = t0; e < nn; e += stride) {
     const int i = (int)(e / nc), j = (int)(e % nc);
-    if (!active[i] || !active[j]) res[e] = 0.0;
+    inv32[e] = (!active[i] || !active[j]) ? 0.f : (float)__ldcg(&res[e]);
   }
 }
 
@@ -228,25 +228,31 @@ int coarse_setup(lpm_handle* h) {
   for (int i = 0; i < n; ++i)
     for (int k = 0; k < 3; ++k)
       off[(size_t)3 * i + k] = (float)(x0[(size_t)3 * i + k] - cen[(size_t)3 * agg[(size_t)i] + k]);
-  // aggregate pairs coupled by the pattern, in order
-  std::vector<int> pairs;
-  std::vector<int> seen((size_t)nagg, -1), nbr;
+  // aggregate pairs coupled by the pattern, in order, each with its rows
+  // (the members of a with a block in b, ascending)
+  std::vector<int> pairs, prow_ptr(1, 0), prow;
+  std::vector<int> seen_row((size_t)nagg, -1);
+  std::vector<std::vector<int>> rows_of((size_t)nagg);
+  std::vector<int> nbr;
   for (int a = 0; a < nagg; ++a) {
     nbr.clear();
     for (int t = mem_ptr[(size_t)a]; t < mem_ptr[(size_t)a + 1]; ++t) {
       const int i = mem[(size_t)t];
       for (int64_t q = cptr[(size_t)i]; q < cptr[(size_t)i + 1]; ++q) {
         const int b = agg[(size_t)cidx[(size_t)q]];
-        if (seen[(size_t)b] != a) {
-          seen[(size_t)b] = a;
-          nbr.push_back(b);
-        }
+        if (seen_row[(size_t)b] == i) continue;
+        if (rows_of[(size_t)b].empty()) nbr.push_back(b);
+        seen_row[(size_t)b] = i;
+        rows_of[(size_t)b].push_back(i);
       }
     }
     std::sort(nbr.begin(), nbr.end());
     for (int b : nbr) {
       pairs.push_back(a);
       pairs.push_back(b);
+      prow.insert(prow.end(), rows_of[(size_t)b].begin(), rows_of[(size_t)b].end());
+      prow_ptr.push_back((int)prow.size());
+      rows_of[(size_t)b].clear();
     }
   }
   const int nc = nagg * nm;
@@ -255,16 +261,19 @@ int coarse_setup(lpm_handle* h) {
   d.cmem_ptr = (int*)dev_alloc(h, sizeof(int) * (nagg + 1));
   d.cmem = (int*)dev_alloc(h, sizeof(int) * n);
   d.cpair = (int*)dev_alloc(h, sizeof(int) * std::max<size_t>(pairs.size(), 1));
+  d.cprow_ptr = (int*)dev_alloc(h, sizeof(int) * prow_ptr.size());
+  d.cprow = (int*)dev_alloc(h, sizeof(int) * std::max<size_t>(prow.size(), 1));
   d.coff = (float*)dev_alloc(h, sizeof(float) * 3 * n);
   d.cA = (double*)dev_alloc(h, sizeof(double) * (size_t)nc * nc);
   d.cA2 = (double*)dev_alloc(h, sizeof(double) * (size_t)nc * nc);
   d.cact = (int*)dev_alloc(h, sizeof(int) * nc);
+  d.cAinv32 = (float*)dev_alloc(h, sizeof(float) * (size_t)nc * nc);
   d.cyc = (double*)dev_alloc(h, sizeof(double) * nc);
   d.cec = (double*)dev_alloc(h, sizeof(double) * nc);
   d.cz = (float*)dev_alloc(h, sizeof(float) * ndof);
   d.cfault = (int*)dev_alloc(h, sizeof(int));
-  if (!d.cagg || !d.cmem_ptr || !d.cmem || !d.cpair || !d.coff || !d.cA || !d.cA2 || !d.cact || !d.cyc || !d.cec ||
-      !d.cz || !d.cfault)
+  if (!d.cagg || !d.cmem_ptr || !d.cmem || !d.cpair || !d.cprow_ptr || !d.cprow || !d.coff || !d.cA || !d.cA2 ||
+      !d.cact || !d.cAinv32 || !d.cyc || !d.cec || !d.cz || !d.cfault)
     return LPM_ERR_NOMEM;
   LPM_CUDA(h, cudaMemcpyAsync(d.cagg, agg.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.cmem_ptr, mem_ptr.data(), sizeof(int) * (nagg + 1), cudaMemcpyHostToDevice,
@@ -274,6 +283,10 @@ int coarse_setup(lpm_handle* h) {
     LPM_CUDA(h, cudaMemcpyAsync(d.cpair, pairs.data(), sizeof(int) * pairs.size(), cudaMemcpyHostToDevice,
                                 h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.coff, off.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+  LPM_CUDA(h, cudaMemcpyAsync(d.cprow_ptr, prow_ptr.data(), sizeof(int) * prow_ptr.size(), cudaMemcpyHostToDevice,
+                              h->stream));
+  if (!prow.empty())
+    LPM_CUDA(h, cudaMemcpyAsync(d.cprow, prow.data(), sizeof(int) * prow.size(), cudaMemcpyHostToDevice, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
   h->cnagg = nagg;
   h->cnc = nc;
@@ -283,7 +296,7 @@ int coarse_setup(lpm_handle* h) {
   return LPM_OK;
 }
 
-// A_c of the current operator and its inverse (in d.cAinv).
+// A_c of the current operator and its inverse (FP32, in d.cAinv32).
 int coarse_assemble(lpm_handle* h) {
   Dev& d = h->d;
   if (!d.cagg) {
@@ -297,11 +310,11 @@ int coarse_assemble(lpm_handle* h) {
   const int G = (h->cnpair + warps_per_block - 1) / warps_per_block;
   if (G > 0) {
     if (h->dim == 3)
-      k_coarse_pairs<3><<<G, 32 * warps_per_block, 0, h->stream>>>(h->cnpair, d.cpair, d.cmem_ptr, d.cmem, d.cagg,
+      k_coarse_pairs<3><<<G, 32 * warps_per_block, 0, h->stream>>>(h->cnpair, d.cpair, d.cprow_ptr, d.cprow, d.cagg,
                                                                   d.coff, fixed, d.sell_ptr, d.scol, d.rowlen,
                                                                   d.A64, h->nslots, nc, d.cA);
     else
-      k_coarse_pairs<2><<<G, 32 * warps_per_block, 0, h->stream>>>(h->cnpair, d.cpair, d.cmem_ptr, d.cmem, d.cagg,
+      k_coarse_pairs<2><<<G, 32 * warps_per_block, 0, h->stream>>>(h->cnpair, d.cpair, d.cprow_ptr, d.cprow, d.cagg,
                                                                   d.coff, fixed, d.sell_ptr, d.scol, d.rowlen,
                                                                   d.A64, h->nslots, nc, d.cA);
     LPM_LAUNCHED(h, "k_coarse_pairs");
@@ -319,7 +332,7 @@ int coarse_assemble(lpm_handle* h) {
   LPM_CUDA(h, cudaMemsetAsync(d.cfault, 0, sizeof(int), h->stream));
   long long spin = kPcgSpinLimit;
   int ncv = nc;
-  void* args[] = {&ncv, &d.cA, &d.cA2, &d.cact, &d.gbar, &spin, &d.cfault};
+  void* args[] = {&ncv, &d.cA, &d.cA2, &d.cact, &d.cAinv32, &d.gbar, &spin, &d.cfault};
   LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_coarse_invert, dim3(grid), dim3(256), args, 0, h->stream));
   LPM_LAUNCHED(h, "k_coarse_invert");
   int fault = 0;
@@ -329,7 +342,6 @@ int coarse_assemble(lpm_handle* h) {
     h->err = "coarse preconditioner: a grid-barrier wait gave up in the inversion";
     return LPM_ERR_STATE;
   }
-  d.cAinv = (nc & 1) ? d.cA2 : d.cA;
   h->coarse_valid = true;
   return LPM_OK;
 }

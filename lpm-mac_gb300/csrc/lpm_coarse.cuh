@@ -11,11 +11,11 @@ constexpr int kModes = DIM == 3 ? 6 : 3;
 // Row k (DOF direction) of P for a particle at offset d from its aggregate's
 // centroid: translations, then rotations (about z in 2-D; about x, y, z in
 // 3-D, omega x d).
-template <int DIM>
-__device__ __forceinline__ void mode_row(int k, double dx, double dy, double dz, double (&w)[kModes<DIM>]) {
+template <int DIM, typename T>
+__device__ __forceinline__ void mode_row(int k, T dx, T dy, T dz, T (&w)[kModes<DIM>]) {
 #pragma unroll
-  for (int m = 0; m < kModes<DIM>; ++m) w[m] = 0.0;
-  w[k] = 1.0;
+  for (int m = 0; m < kModes<DIM>; ++m) w[m] = T(0);
+  w[k] = T(1);
   if (DIM == 2) {
     w[2] = k == 0 ? -dy : dx;
   } else {

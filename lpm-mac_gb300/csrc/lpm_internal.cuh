@@ -152,10 +152,10 @@ struct Dev {
   // aggregate centroids; the coarse operator and its inverse (dense, nc x nc),
   // the modes kept, the restriction and coarse solution, the preconditioned
   // residual
-  int *cagg, *cmem_ptr, *cmem, *cpair, *cact, *cfault;
+  int *cagg, *cmem_ptr, *cmem, *cpair, *cprow_ptr, *cprow, *cact, *cfault;
   float* coff;
-  double *cA, *cA2, *cAinv, *cyc, *cec;
-  float* cz;
+  double *cA, *cA2, *cyc, *cec;
+  float *cAinv32, *cz;
   double* norms;   // device results of small reductions [8]
   // per-particle flags for the BC elimination
   unsigned char* fixed;
