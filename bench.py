@@ -79,9 +79,10 @@ def parse_args(argv=None):
     p.add_argument("--no-extras", action="store_true",
                    help="time the load steps only (no e2e, adjoint, force/assembly, set-up, fatigue, J2 legs): "
                         "for profiling runs")
-    p.add_argument("--profile-solve", choices=["sent", "ct"],
+    p.add_argument("--profile-solve", choices=["sent", "ct", "sent-coarse", "ct-coarse"],
                    help="profiling entry: one mixed solve (300 iterations) on the full-size SENT or CT plate's "
-                        "tangent, which runs as one persistent kernel; prints its time and exits")
+                        "tangent, which runs as one persistent kernel (with the coarse-space preconditioner for "
+                        "the -coarse cases); prints its time and exits")
     p.add_argument("--softening-steps", type=int, default=1,
                    help="timed load steps of configuration 3 at full size from the first softened bond on (0: none; "
                         "4 includes the crack's burst, several minutes)")
@@ -953,6 +954,8 @@ def profile_solve(case):
     import __graft_entry__ as ge
     pkg = ge.load_package()
     lat, capi = pkg.lattice, pkg.capi
+    coarse = case.endswith("-coarse")
+    case = case.split("-")[0]
     if case == "sent":
         xyz, p1, p2, layer, cell = lat.sent_plate(201, 401, 0.1)
         E, nu = 69e3, 0.3
@@ -968,6 +971,8 @@ def profile_solve(case):
     r = g.load_step([("disp", gb, 1, 0.0), ("disp", gc, 0, 0.0), ("disp", gt, 1, 1e-3)],
                     tangent=capi.TANGENT_SYMMETRIC, precision=capi.PREC_FP64, cg_tol=1e-10)
     g.assemble(capi.TANGENT_SYMMETRIC, capi.BC_ELIMINATE)
+    if coarse:
+        g.set_preconditioner(capi.PRECOND_COARSE, 0.0)
     g.upload(capi.F_RESIDUAL, np.random.default_rng(5).standard_normal(g.ndof))
     stream = torch.cuda.ExternalStream(g.stream(), device="cuda:0")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -978,7 +983,7 @@ def profile_solve(case):
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
-    out = {"profile_solve": case, "particles": len(xyz), "blocks": g.nblk, "iterations": it, "ms": ms,
+    out = {"profile_solve": case + ("-coarse" if coarse else ""), "particles": len(xyz), "blocks": g.nblk, "iterations": it, "ms": ms,
            "us_per_iteration": 1e3 * ms / max(it, 1), "persistent_solves": g.stats()["persistent_solves"],
            "load_step": r}
     g.close()
