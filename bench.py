@@ -29,6 +29,7 @@ Reported (one JSON line on rank 0):
   setup        the GPU bond search (checked identical to the CPU
                generator's bonds) and the creation of the device lattice
   fatigue      compact-tension fatigue cycles at full size (configuration 5)
+  fatigue_coarse  the same cycles with the coarse-space preconditioner
   softening    load steps of the notched plate with the softening bond law
                and damage rounds at full size (configuration 3): by default
                the one step in which the first bonds soften (about 170
@@ -361,7 +362,7 @@ def setup_cost(w, capi):
             "lattice_create_ms": (t3 - t2) * 1e3, "timing": "host wall clock, host arrays in and out"}
 
 
-def fatigue_cost(capi, local, cycles=3):
+def fatigue_cost(capi, local, cycles=3, precond=None):
     """Configuration 5 at full size: the compact-tension plate (hexagonal
     lattice, W = 40 mm from the load line, 0.15 mm spacing), HCF fatigue law
     with seeded per-particle A and B, nonlocal damage rate, pin loads
@@ -388,6 +389,8 @@ def fatigue_cost(capi, local, cycles=3):
     near_pins = (np.abs(xyz[:, 0] - cx) <= info["radius"]) & ((xyz[:, 1] >= cy_t) | (xyz[:, 1] <= cy_b))
     g.set_types(np.where(near_pins, 4, 0).astype(np.int32), 4)  # the pin regions do not damage
     g.set_nonlocal(nl_ptr, nl_idx, L)
+    if precond is not None:
+        g.set_preconditioner(precond, 0.0)
     g.update()
     gm, gt, gb = g.add_group(groups["mid"]), g.add_group(groups["top"]), g.add_group(groups["bottom"])
     f_max, R = 400.0, 0.1
@@ -419,7 +422,9 @@ def fatigue_cost(capi, local, cycles=3):
             "newton_iters_per_cycle": statistics.mean(rc["newton_iters"] for rc in recs),
             "cg_iters_per_cycle": statistics.mean(rc["cg_iters"] for rc in recs),
             "cycle": "1 increment up, 1 down, cycle jump 1000 (lpm_fatigue_run)", "precision": "mixed",
-            "persistent_solves": persistent}
+            "persistent_solves": persistent,
+            "preconditioner": "Jacobi (the reference's)" if precond is None else
+            "Jacobi plus rigid-body modes of particle boxes (lpm_set_preconditioner, automatic box)"}
 
 
 def softening_cost(capi, local, steps=4, max_warm=15, precond=None):
@@ -923,6 +928,7 @@ def run_gb300(args):
                            "force_algorithmic_bytes": fb}
     run_leg(line, "setup", setup_cost, w, capi)
     run_leg(line, "fatigue", fatigue_cost, capi, local)
+    run_leg(line, "fatigue_coarse", fatigue_cost, capi, local, precond=capi.PRECOND_COARSE)
     if args.softening_steps > 0:
         run_leg(line, "softening", softening_cost, capi, local, steps=args.softening_steps)
         run_leg(line, "softening_coarse", softening_cost, capi, local, steps=args.softening_steps,

@@ -370,6 +370,9 @@ class Assembly {
                          Tv.data(), c.particle_volume, c.nneighbors, &g_->h),
               "lpm_create");
     g_->nb = (int64_t)p1.size();
+    if (lpm_gpu_options().precond != LPM_PRECOND_JACOBI)
+      lpm_check(lpm_set_preconditioner(g_->h, lpm_gpu_options().precond, lpm_gpu_options().precond_box),
+                "lpm_set_preconditioner");
     // material law and per-particle parameters
     std::vector<double> prm, all;
     pt_sys[0]->gpuParams(prm);

@@ -59,13 +59,16 @@ enum class LatticeType : char { Square2D, Hexagon2D, SimpleCubic3D, FCC3D, BCC3D
 // Run-time choices of the GPU path that have no counterpart in the
 // reference's interface.  Defaults reproduce the reference; environment
 // variables override them (LPM_TANGENT=symmetric, LPM_PRECISION=mixed,
-// LPM_CG_TOL=1e-10, LPM_STATIC_BC=eliminate).
+// LPM_CG_TOL=1e-10, LPM_STATIC_BC=eliminate; LPM_PRECOND=coarse or
+// coarse:<box edge> for the coarse-space preconditioner of the mixed solve).
 struct LpmGpuOptions {
   int tangent = LPM_TANGENT_AS_WRITTEN;
   int precision = LPM_PREC_FP64;
   double cg_tol = 2.220446049250313e-16;  // Eigen's default: machine epsilon
   int static_bc = LPM_BC_NONE;            // SolverStatic leaves the BC elimination out
   bool verbose = true;                    // the reference's printf lines
+  int precond = LPM_PRECOND_JACOBI;       // Eigen's DiagonalPreconditioner
+  double precond_box = 0.0;               // coarse box edge (0: automatic)
 };
 inline LpmGpuOptions& lpm_gpu_options() {
   static LpmGpuOptions o = [] {
@@ -77,6 +80,12 @@ inline LpmGpuOptions& lpm_gpu_options() {
     if (const char* s = getenv("LPM_STATIC_BC")) v.static_bc = strcmp(s, "eliminate") == 0 ? LPM_BC_ELIMINATE
                                                                                           : LPM_BC_NONE;
     if (const char* s = getenv("LPM_QUIET")) v.verbose = atoi(s) == 0;
+    if (const char* s = getenv("LPM_PRECOND")) {
+      if (strncmp(s, "coarse", 6) == 0) {
+        v.precond = LPM_PRECOND_COARSE;
+        if (s[6] == ':') v.precond_box = atof(s + 7);
+      }
+    }
     return v;
   }();
   return o;

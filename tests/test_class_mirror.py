@@ -229,3 +229,14 @@ def test_cantilever_beam_through_class_interface_matches_oracle(tmp_path):
     print("[beam] %d particles: GPU vs oracle %.2e; L2 error GPU %.6f, oracle %.6f" % (n, rel(u_g, u_o), l2_gpu, l2_o))
     assert rel(u_g, u_o) <= 1e-8
     assert np.isfinite(l2_gpu) and abs(l2_gpu - l2_o) <= 1e-6 * l2_o
+    # the same program in mixed precision with the coarse-space
+    # preconditioner, chosen by environment alone
+    env2 = dict(env, LPM_PRECISION="mixed", LPM_PRECOND="coarse")
+    out2 = str(tmp_path / "beam_coarse.txt")
+    r2 = subprocess.run([exe, out2, "fatigue", "0.2"], capture_output=True, text=True, env=env2, cwd=str(tmp_path),
+                        timeout=600)
+    assert r2.returncode == 0, r2.stdout[-3000:] + r2.stderr[-3000:]
+    assert "Solving failed" not in r2.stdout
+    u_c = (np.loadtxt(out2)[:, 1:4] - xyz0)[:, :2]
+    print("[beam] mixed precision, coarse preconditioner: GPU vs oracle %.2e" % rel(u_c, u_o))
+    assert rel(u_c, u_o) <= 1e-8
