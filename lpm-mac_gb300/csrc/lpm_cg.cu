@@ -599,7 +599,7 @@ struct PcgMixed {
   const int *cagg, *cmem_ptr, *cmem;
   const float* coff;
   const unsigned char* cfixed;  // eliminated DOFs, or null
-  const float* cAinv;  // FP32 inverse of A_c
+  const double* cAinv;  // inverse of A_c (symmetric)
   double *cyc, *cec;
   float* cz;
   int cnagg;
@@ -609,10 +609,12 @@ struct PcgMixed {
 // high words (written before the caller's last barrier).  The restriction
 // y = P^T r and the coarse solve e = A_c^-1 y each take one block per
 // aggregate (the members, or the columns of A_c^-1, spread over the block's
-// threads, in FP32 with compensated sums reduced over the block in a fixed
-// order: GB300's FP64 pipe would make these steps cost more than the
-// product) and end at a grid barrier; then each row adds P_i e to its
-// Jacobi term.  False if a barrier wait gave up.
+// threads, summed in FP32 pairs reduced over the block in a fixed order:
+// GB300's FP64 pipe would make FP64 sums cost more than the product; the
+// coarse product keeps one FP64 product per term, since A_c^-1 of small
+// boxes can be too ill-conditioned for FP32 entries) and end at a grid
+// barrier; then each row adds P_i e to its Jacobi term.  False if a barrier
+// wait gave up.
 template <int DIM>
 __device__ bool coarse_z(const PcgMixed& a, unsigned long long& target) {
   constexpr int NM = kModes<DIM>;
@@ -647,9 +649,14 @@ __device__ bool coarse_z(const PcgMixed& a, unsigned long long& target) {
 #pragma unroll
     for (int m = 0; m < NM; ++m) sm[m] = cm[m] = 0.f;
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-      const float yc = (float)__ldcg(&a.cyc[c]);
+      const double yc = __ldcg(&a.cyc[c]);
 #pragma unroll
-      for (int m = 0; m < NM; ++m) dot2_acc(sm[m], cm[m], __ldg(&a.cAinv[(int64_t)(ag * NM + m) * nc + c]), yc);
+      for (int m = 0; m < NM; ++m) {
+        // one FP64 product per term, summed as a compensated FP32 pair
+        float ph, pl;
+        df_split(__ldg(&a.cAinv[(int64_t)(ag * NM + m) * nc + c]) * yc, ph, pl);
+        df_add(sm[m], cm[m], ph, pl);
+      }
     }
     double e[NM];
     block_df_sum<NM>(sm, cm, e);
@@ -1399,7 +1406,7 @@ int run_persistent_mixed(lpm_handle* h, const SellView& sv, int grid, int thread
     a.cmem = d.cmem;
     a.coff = d.coff;
     a.cfixed = h->last_bc == LPM_BC_ELIMINATE ? d.fixed : nullptr;
-    a.cAinv = d.cAinv32;
+    a.cAinv = d.cAinv;
     a.cyc = d.cyc;
     a.cec = d.cec;
     a.cz = d.cz;

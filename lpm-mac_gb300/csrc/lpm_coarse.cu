@@ -137,9 +137,12 @@ __global__ void k_coarse_guard(int nc, double* __restrict__ Ac, int* __restrict_
 
 // In-place Gauss-Jordan inversion without pivoting, ping-ponged between two
 // buffers (step k reads one and writes the other), one grid barrier per
-// step.  The inverse, with the rows and columns of inactive modes cleared,
-// is rounded to FP32 into inv32 (the preconditioner needs no more).
-__global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restrict__ active, float* inv32,
+// step.  The result is then symmetrized, (B + B^T)/2, with the rows and
+// columns of inactive modes cleared, into the other buffer (X when nc is
+// odd, else Y): elimination leaves the computed inverse of an
+// ill-conditioned A_c slightly unsymmetric, and CG needs a symmetric
+// preconditioner.
+__global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restrict__ active,
                                 unsigned long long* gbar, long long spin_limit, int* fault) {
   const int64_t nn = (int64_t)nc * nc;
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
@@ -166,9 +169,10 @@ __global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restr
     }
   }
   const double* res = (nc & 1) ? Y : X;
+  double* out = (nc & 1) ? X : Y;
   for (int64_t e = t0; e < nn; e += stride) {
     const int i = (int)(e / nc), j = (int)(e % nc);
-    inv32[e] = (!active[i] || !active[j]) ? 0.f : (float)__ldcg(&res[e]);
+    out[e] = (!active[i] || !active[j]) ? 0.0 : 0.5 * (__ldcg(&res[e]) + __ldcg(&res[(int64_t)j * nc + i]));
   }
 }
 
@@ -267,13 +271,12 @@ int coarse_setup(lpm_handle* h) {
   d.cA = (double*)dev_alloc(h, sizeof(double) * (size_t)nc * nc);
   d.cA2 = (double*)dev_alloc(h, sizeof(double) * (size_t)nc * nc);
   d.cact = (int*)dev_alloc(h, sizeof(int) * nc);
-  d.cAinv32 = (float*)dev_alloc(h, sizeof(float) * (size_t)nc * nc);
   d.cyc = (double*)dev_alloc(h, sizeof(double) * nc);
   d.cec = (double*)dev_alloc(h, sizeof(double) * nc);
   d.cz = (float*)dev_alloc(h, sizeof(float) * ndof);
   d.cfault = (int*)dev_alloc(h, sizeof(int));
   if (!d.cagg || !d.cmem_ptr || !d.cmem || !d.cpair || !d.cprow_ptr || !d.cprow || !d.coff || !d.cA || !d.cA2 ||
-      !d.cact || !d.cAinv32 || !d.cyc || !d.cec || !d.cz || !d.cfault)
+      !d.cact || !d.cyc || !d.cec || !d.cz || !d.cfault)
     return LPM_ERR_NOMEM;
   LPM_CUDA(h, cudaMemcpyAsync(d.cagg, agg.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(d.cmem_ptr, mem_ptr.data(), sizeof(int) * (nagg + 1), cudaMemcpyHostToDevice,
@@ -296,7 +299,7 @@ int coarse_setup(lpm_handle* h) {
   return LPM_OK;
 }
 
-// A_c of the current operator and its inverse (FP32, in d.cAinv32).
+// A_c of the current operator and its symmetrized inverse (in d.cAinv).
 int coarse_assemble(lpm_handle* h) {
   Dev& d = h->d;
   if (!d.cagg) {
@@ -332,7 +335,7 @@ int coarse_assemble(lpm_handle* h) {
   LPM_CUDA(h, cudaMemsetAsync(d.cfault, 0, sizeof(int), h->stream));
   long long spin = kPcgSpinLimit;
   int ncv = nc;
-  void* args[] = {&ncv, &d.cA, &d.cA2, &d.cact, &d.cAinv32, &d.gbar, &spin, &d.cfault};
+  void* args[] = {&ncv, &d.cA, &d.cA2, &d.cact, &d.gbar, &spin, &d.cfault};
   LPM_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_coarse_invert, dim3(grid), dim3(256), args, 0, h->stream));
   LPM_LAUNCHED(h, "k_coarse_invert");
   int fault = 0;
@@ -342,6 +345,7 @@ int coarse_assemble(lpm_handle* h) {
     h->err = "coarse preconditioner: a grid-barrier wait gave up in the inversion";
     return LPM_ERR_STATE;
   }
+  d.cAinv = (nc & 1) ? d.cA : d.cA2;
   h->coarse_valid = true;
   return LPM_OK;
 }

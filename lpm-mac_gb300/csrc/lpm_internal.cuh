@@ -154,8 +154,8 @@ struct Dev {
   // residual
   int *cagg, *cmem_ptr, *cmem, *cpair, *cprow_ptr, *cprow, *cact, *cfault;
   float* coff;
-  double *cA, *cA2, *cyc, *cec;
-  float *cAinv32, *cz;
+  double *cA, *cA2, *cAinv, *cyc, *cec;  // cAinv: cA or cA2, wherever the inversion ended
+  float* cz;
   double* norms;   // device results of small reductions [8]
   // per-particle flags for the BC elimination
   unsigned char* fixed;
