@@ -37,6 +37,9 @@ Reported (one JSON line on rank 0):
                too (minutes)
   softening_coarse  the same steps with the coarse-space preconditioner
                (Jacobi plus rigid-body modes of boxes of particles)
+  softening_sensitivity  the coarse-preconditioned steps carrying the
+               reaction's tangents along E and the Weibull scale through every
+               damage round, relative to softening_coarse
   j2_sensitivity  cost of carrying d/d(yield stress) and d/d(hardening)
                through J2 load steps of a BCC polycrystal (40^3 cells)
   polycrystal  configuration 4 at full size (BCC 60^3 cells, 20 grains):
@@ -427,7 +430,7 @@ def fatigue_cost(capi, local, cycles=3, precond=None):
             "Jacobi plus rigid-body modes of particle boxes (lpm_set_preconditioner, automatic box)"}
 
 
-def softening_cost(capi, local, steps=4, max_warm=15, precond=None):
+def softening_cost(capi, local, steps=4, max_warm=15, precond=None, tangents=False):
     """Configuration 3 at full size: the single-edge-notched hexagonal plate
     (401 rows of 201/200 particles, 0.1 mm spacing, crack over 0.3 W),
     softening bond law (alpha 3) with Weibull(k = 10, lambda = 1.2e-3)
@@ -460,6 +463,11 @@ def softening_cost(capi, local, steps=4, max_warm=15, precond=None):
         if g.load_step(bcs, **opts)["status"] != 0:
             raise RuntimeError("SENT step did not converge")
         warm += 1
+    if tangents:
+        # d/d(log E) and d/d(log lambda) of the Weibull scale, carried
+        # through every damage round of the timed steps
+        g.tangent_begin_softening([{"dKn": g.download(capi.B_KN), "dTv": g.download(capi.B_TV)},
+                                   {"dscrit": g.download(capi.B_SCRIT)}], tol=1e-10)
     stream = torch.cuda.ExternalStream(g.stream(), device="cuda:%d" % local)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -471,7 +479,13 @@ def softening_cost(capi, local, steps=4, max_warm=15, precond=None):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     d = g.download(capi.B_BDAMAGE)
-    persistent = g.stats()["persistent_solves"]
+    stats = g.stats()
+    persistent = stats["persistent_solves"]
+    if tangents:
+        c = xyz[:, 1]
+        top_ids = np.where(c > c.max() - 1e-9)[0]
+        dR = [float(g.tangent_get(k, capi.T_PIN)[top_ids, 1].sum()) for k in range(2)]
+        g.tangent_end()
     g.close()
     if any(r["status"] != 0 for r in recs):
         raise RuntimeError("SENT step did not converge")
@@ -485,7 +499,9 @@ def softening_cost(capi, local, steps=4, max_warm=15, precond=None):
             "precision": "mixed", "solver": "static with damage rounds, eliminated tangent",
             "us_per_cg_iteration": 1e3 * ms / max(1, sum(r["cg_iters"] for r in recs)), "persistent_solves": persistent,
             "preconditioner": "Jacobi (the reference's)" if precond is None else
-            "Jacobi plus rigid-body modes of particle boxes (lpm_set_preconditioner, automatic box)"}
+            "Jacobi plus rigid-body modes of particle boxes (lpm_set_preconditioner, automatic box)",
+            **({"tangent_directions": "d/d(log E), d/d(log Weibull scale)", "dR_top": dR,
+                "tangent_cg_iters": stats["tangent_cg_iters"]} if tangents else {})}
 
 
 def j2_sensitivity_cost(capi, local, ncell=40, steps=4):
@@ -933,6 +949,11 @@ def run_gb300(args):
         run_leg(line, "softening", softening_cost, capi, local, steps=args.softening_steps)
         run_leg(line, "softening_coarse", softening_cost, capi, local, steps=args.softening_steps,
                 precond=capi.PRECOND_COARSE)
+        run_leg(line, "softening_sensitivity", softening_cost, capi, local, steps=args.softening_steps,
+                precond=capi.PRECOND_COARSE, tangents=True)
+        sf, ss = line.get("softening_coarse", {}), line.get("softening_sensitivity", {})
+        if "ms_per_step" in sf and "ms_per_step" in ss:
+            ss["relative_to_forward_step"] = ss["ms_per_step"] / sf["ms_per_step"]
     run_leg(line, "j2_sensitivity", j2_sensitivity_cost, capi, local)
     run_leg(line, "polycrystal", polycrystal_cost, capi, local)
     g.close()

@@ -694,6 +694,11 @@ static int jacobian_bicgstab(lpm_handle* h, const double* g, double* x, double t
                                                             d.bdamage, d.bforce, d.Kn, d.Tv, d.mask, d.adj_invd);
   LPM_LAUNCHED(h, "k_jac_invdiag");
   if (maxit < 0) maxit = 2LL * m;
+  // right preconditioner: the exact diagonal, plus the coarse correction of
+  // the assembled symmetric tangent when the user chose it
+  // (lpm_set_preconditioner): the exact Jacobian differs from that tangent
+  // by the bond directions' change, so its coarse space serves here too
+  const bool coarse = coarse_usable(h);
   const int GV = grid_for(m, 256, kMaxRedBlocks), T = 256, GE = grid_for(m, T);
   LPM_CUDA(h, cudaMemsetAsync(x, 0, sizeof(double) * m, h->stream));
   LPM_CUDA(h, cudaMemsetAsync(p, 0, sizeof(double) * m, h->stream));
@@ -724,6 +729,10 @@ static int jacobian_bicgstab(lpm_handle* h, const double* g, double* x, double t
     const double beta = (rho_new / rho) * (alpha / omega);
     k_bicg_p<<<GE, T, 0, h->stream>>>(m, r, v, d.adj_invd, it == 0 ? 0.0 : beta, omega, p, ph);
     LPM_LAUNCHED(h, "k_bicg_p");
+    if (coarse) {
+      st = coarse_apply64(h, p, d.adj_invd, ph);
+      if (st) return st;
+    }
     st = apply_jacobian(h, ph, v, true, nullptr);
     if (st) return st;
     st = dot2(rh, v, rh, v, q);
@@ -731,6 +740,10 @@ static int jacobian_bicgstab(lpm_handle* h, const double* g, double* x, double t
     alpha = rho_new / q[0];
     k_bicg_s<<<GE, T, 0, h->stream>>>(m, r, v, d.adj_invd, alpha, sv, sh);
     LPM_LAUNCHED(h, "k_bicg_s");
+    if (coarse) {
+      st = coarse_apply64(h, sv, d.adj_invd, sh);
+      if (st) return st;
+    }
     st = apply_jacobian(h, sh, tv, true, nullptr);
     if (st) return st;
     st = dot2(tv, sv, tv, tv, q);

@@ -176,6 +176,81 @@ __global__ void k_coarse_invert(int nc, double* X, double* Y, const int* __restr
   }
 }
 
+// The same coarse correction for FP64 vectors, as three launches (the
+// tangent solves' BiCGSTAB, whose loop runs from the host): y = P^T r with a
+// block per aggregate, e = A_c^-1 y with a block per aggregate, then
+// z = invd r + P e per row.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_coarse_restrict64(int nagg, const int* __restrict__ mem_ptr,
+                                                           const int* __restrict__ mem, const float* __restrict__ off,
+                                                           const unsigned char* __restrict__ fixed,
+                                                           const double* __restrict__ r, double* __restrict__ y) {
+  constexpr int NM = kModes<DIM>;
+  for (int ag = blockIdx.x; ag < nagg; ag += gridDim.x) {
+    double acc[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) acc[m] = 0.0;
+    for (int t = mem_ptr[ag] + threadIdx.x; t < mem_ptr[ag + 1]; t += blockDim.x) {
+      const int i = mem[t];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        const int64_t q = (int64_t)DIM * i + k;
+        if (fixed[q]) continue;
+        double w[NM];
+        mode_row<DIM, double>(k, off[3 * i], off[3 * i + 1], off[3 * i + 2], w);
+#pragma unroll
+        for (int m = 0; m < NM; ++m) acc[m] += w[m] * r[q];
+      }
+    }
+    block_sum<NM>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int m = 0; m < NM; ++m) y[ag * NM + m] = acc[m];
+  }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_coarse_solve64(int nagg, const double* __restrict__ Ainv,
+                                                        const double* __restrict__ y, double* __restrict__ e) {
+  constexpr int NM = kModes<DIM>;
+  const int nc = nagg * NM;
+  for (int ag = blockIdx.x; ag < nagg; ag += gridDim.x) {
+    double acc[NM];
+#pragma unroll
+    for (int m = 0; m < NM; ++m) acc[m] = 0.0;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x)
+#pragma unroll
+      for (int m = 0; m < NM; ++m) acc[m] += Ainv[(int64_t)(ag * NM + m) * nc + c] * y[c];
+    block_sum<NM>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int m = 0; m < NM; ++m) e[ag * NM + m] = acc[m];
+  }
+}
+
+template <int DIM>
+__global__ void k_coarse_prolong64(int n, const int* __restrict__ agg, const float* __restrict__ off,
+                                   const unsigned char* __restrict__ fixed, const double* __restrict__ invd,
+                                   const double* __restrict__ r, const double* __restrict__ e,
+                                   double* __restrict__ z) {
+  constexpr int NM = kModes<DIM>;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int ag = agg[i];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    const int64_t q = (int64_t)DIM * i + k;
+    double zi = invd[q] * r[q];
+    if (!fixed[q]) {
+      double w[NM];
+      mode_row<DIM, double>(k, off[3 * i], off[3 * i + 1], off[3 * i + 2], w);
+#pragma unroll
+      for (int m = 0; m < NM; ++m) zi += w[m] * e[ag * NM + m];
+    }
+    z[q] = zi;
+  }
+}
+
 }  // namespace
 
 int coarse_setup(lpm_handle* h) {
@@ -347,6 +422,40 @@ int coarse_assemble(lpm_handle* h) {
   }
   d.cAinv = (nc & 1) ? d.cA : d.cA2;
   h->coarse_valid = true;
+  return LPM_OK;
+}
+
+}  // namespace lpm
+
+namespace lpm {
+
+// The coarse correction applies to the tangent solves when the user chose it
+// and the last assembly is the symmetric tangent with the displacement BCs
+// eliminated (its eliminated DOFs contain the constrained ones, on which the
+// correction is zero).
+bool coarse_usable(const lpm_handle* h) {
+  return h->precond == LPM_PRECOND_COARSE && h->have_K && !h->mf && h->tangent == LPM_TANGENT_SYMMETRIC &&
+         h->last_bc == LPM_BC_ELIMINATE;
+}
+
+int coarse_apply64(lpm_handle* h, const double* r, const double* invd, double* z) {
+  Dev& d = h->d;
+  if (!h->coarse_valid) {
+    const int st = coarse_assemble(h);
+    if (st) return st;
+  }
+  const int nagg = h->cnagg;
+  if (h->dim == 3) {
+    k_coarse_restrict64<3><<<nagg, 256, 0, h->stream>>>(nagg, d.cmem_ptr, d.cmem, d.coff, d.fixed, r, d.cyc);
+    k_coarse_solve64<3><<<nagg, 256, 0, h->stream>>>(nagg, d.cAinv, d.cyc, d.cec);
+    k_coarse_prolong64<3><<<grid_for(h->n, 256), 256, 0, h->stream>>>(h->n, d.cagg, d.coff, d.fixed, invd, r, d.cec, z);
+  } else {
+    k_coarse_restrict64<2><<<nagg, 256, 0, h->stream>>>(nagg, d.cmem_ptr, d.cmem, d.coff, d.fixed, r, d.cyc);
+    k_coarse_solve64<2><<<nagg, 256, 0, h->stream>>>(nagg, d.cAinv, d.cyc, d.cec);
+    k_coarse_prolong64<2><<<grid_for(h->n, 256), 256, 0, h->stream>>>(h->n, d.cagg, d.coff, d.fixed, invd, r, d.cec, z);
+  }
+  LPM_LAUNCHED(h, "k_coarse_apply64");
+  h->stats.kernel_launches += 2;
   return LPM_OK;
 }
 

@@ -299,6 +299,10 @@ int mf_graph_residual(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, 
 // the coarse operator's inverse once per assembly
 int coarse_setup(lpm_handle* h);
 int coarse_assemble(lpm_handle* h);
+// z = invd r + P A_c^-1 P^T r for FP64 device vectors (the tangent solves),
+// when coarse_usable
+bool coarse_usable(const lpm_handle* h);
+int coarse_apply64(lpm_handle* h, const double* r, const double* invd, double* z);
 // solvers (lpm_cg.cu)
 int solve_fp64(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);
 int solve_mixed(lpm_handle* h, double tol, long long maxit, long long* iters, double* relres);

@@ -75,7 +75,7 @@ def test_sent_softening_steps_match_oracle(precision, operator):
     g.close()
 
 
-def _sent_run(args, sc, scale_k, scale_sc, steps, tangents=False):
+def _sent_run(args, sc, scale_k, scale_sc, steps, tangents=False, precond=None):
     """The notched plate pulled `steps` times with the constants and the
     critical stretches scaled; per step the top reaction, the damage rounds
     and the damaged-bond pattern, and with `tangents` the reaction's
@@ -84,6 +84,8 @@ def _sent_run(args, sc, scale_k, scale_sc, steps, tangents=False):
     g = make_gpu(dim, xyz, p1, p2, layer, Kn * scale_k, Tv * scale_k, cell)
     g.set_law(capi.LAW_SOFTENING, [3.0, 1.0e-3])
     g.upload(capi.B_SCRIT, sc * scale_sc)
+    if precond is not None:
+        g.set_preconditioner(precond, 0.0)
     g.update()
     c = xyz[:, 1]
     bottom, top = np.where(c < c.min() + 1e-9)[0], np.where(c > c.max() - 1e-9)[0]
@@ -110,7 +112,8 @@ def _sent_run(args, sc, scale_k, scale_sc, steps, tangents=False):
 
 
 @pytest.mark.gpu
-def test_softening_reaction_tangents_match_central_differences():
+@pytest.mark.parametrize("precond", ["jacobi", "coarse"])
+def test_softening_reaction_tangents_match_central_differences(precond):
     """Configuration-3 sensitivities: the top reaction of each load step of
     the notched plate, differentiated along log E (all bond constants) and
     along log lambda (the scale of the Weibull critical stretches), by the
@@ -119,10 +122,13 @@ def test_softening_reaction_tangents_match_central_differences():
     the steps before any change of the discrete path (the damage rounds and
     the set of damaged bonds are the same in the base and both perturbed
     runs); at least one compared step must have softened bonds.  The peak
-    reaction's derivative is that of the step where it peaks."""
+    reaction's derivative is that of the step where it peaks.  With the
+    coarse-space preconditioner chosen, the tangents' BiCGSTAB solves use it
+    too (the FP64 forward solves keep Jacobi), to the same bar."""
     args, sc = setup()
     steps, h = 6, 1e-4
-    base = _sent_run(args, sc, 1.0, 1.0, steps, tangents=True)
+    pre = capi.PRECOND_COARSE if precond == "coarse" else None
+    base = _sent_run(args, sc, 1.0, 1.0, steps, tangents=True, precond=pre)
     runs = {(k, sgn): _sent_run(args, sc, *((1 + sgn * h, 1.0) if k == 0 else (1.0, 1 + sgn * h)), steps)
             for k in range(2) for sgn in (1, -1)}
     compared, softened = 0, 0
@@ -135,8 +141,8 @@ def test_softening_reaction_tangents_match_central_differences():
             fd = (runs[k, 1][t]["R"] - runs[k, -1][t]["R"]) / (2 * h)
             tg = base[t]["dR"][k]
             err = abs(tg - fd) / max(abs(fd), 1e-12 * abs(base[t]["R"]))
-            print("[softening tangent] step %d dir %d: tangent %.9e FD %.9e rel %.2e rounds %d damaged %d" % (
-                t, k, tg, fd, err, base[t]["rounds"], int(base[t]["damaged"].sum())))
+            print("[softening tangent, %s] step %d dir %d: tangent %.9e FD %.9e rel %.2e rounds %d damaged %d" % (
+                precond, t, k, tg, fd, err, base[t]["rounds"], int(base[t]["damaged"].sum())))
             assert err <= 1e-5, (t, k)
         compared += 1
         softened += bool(base[t]["damaged"].any())
