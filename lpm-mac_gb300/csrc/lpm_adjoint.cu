@@ -629,66 +629,112 @@ static int jacobian_cg(lpm_handle* h, const double* g, double* x, double tol, lo
 // BiCGSTAB (van der Vorst, SIAM J. Sci. Stat. Comput. 13 (1992)) for the
 // non-symmetric H_ff of a partially damaged state, right-preconditioned by
 // H's exact diagonal; the vector work of one iteration in three kernels.
-__global__ void k_dot2(int64_t m, const double* __restrict__ a, const double* __restrict__ b,
-                       const double* __restrict__ c, const double* __restrict__ e, double* partials,
-                       unsigned int* ticket, double* out) {
+// Its scalars stay on the device: the dot kernels' last blocks update them
+// and the vector kernels read them, so an iteration needs no host round
+// trip; the host reads them once per batch of iterations.
+struct BicgScalars {
+  double bnorm, tol2b;  // |b| and tol^2 |b|^2
+  double rho, rho_new, alpha, omega, rr;
+  long long it, maxit;
+  int done;  // 0 running, 1 converged, 2 iteration cap or breakdown, 3 non-finite
+};
+
+enum BicgStage { kBicgInit, kBicgAlpha, kBicgOmega, kBicgRes };
+
+// Two dot products (a.b, c.e) folded over the grid; the last block updates
+// the scalars for the stage.  Nothing once the solve has ended.
+template <int STAGE>
+__global__ void k_bicg_dot(int64_t m, const double* __restrict__ a, const double* __restrict__ b,
+                           const double* __restrict__ c, const double* __restrict__ e, double* partials,
+                           unsigned int* ticket, BicgScalars* S, double tol, long long maxit) {
+  if (STAGE != kBicgInit && S->done) return;
   double v[2] = {0.0, 0.0};
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
     v[0] += a[t] * b[t];
     v[1] += c[t] * e[t];
   }
   double tot[2];
-  if (grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0) {
-    out[0] = tot[0];
-    out[1] = tot[1];
+  if (!(grid_sum<2>(v, partials, ticket, tot) && threadIdx.x == 0)) return;
+  if (STAGE == kBicgInit) {  // (g.g, rh.r) with r = rh = g
+    S->bnorm = sqrt(tot[0]);
+    S->tol2b = tol * tol * tot[0];
+    S->rho = S->alpha = S->omega = 1.0;
+    S->rho_new = tot[1];
+    S->rr = tot[0];
+    S->it = 0;
+    S->maxit = maxit;
+    S->done = !isfinite(tot[0]) ? 3 : (tot[0] == 0.0 || maxit <= 0) ? (tot[0] == 0.0 ? 1 : 2) : 0;
+  } else if (STAGE == kBicgAlpha) {  // rh.v
+    S->alpha = S->rho_new / tot[0];
+  } else if (STAGE == kBicgOmega) {  // (t.s, t.t)
+    S->omega = tot[1] > 0.0 ? tot[0] / tot[1] : 0.0;
+  } else {  // (r.r, rh.r)
+    S->rho = S->rho_new;
+    S->rho_new = tot[1];
+    S->rr = tot[0];
+    S->it += 1;
+    if (!isfinite(tot[0]))
+      S->done = 3;
+    else if (tot[0] <= S->tol2b)
+      S->done = 1;
+    else if (S->it >= S->maxit || S->rho_new == 0.0 || S->omega == 0.0)
+      S->done = 2;
   }
 }
 
-// p = r + beta (p - omega v), phat = M p
+// p = r + beta (p - omega v), phat = M p, with beta from the scalars (0 in
+// the first iteration)
 __global__ void k_bicg_p(int64_t m, const double* __restrict__ r, const double* __restrict__ v,
-                         const double* __restrict__ invd, double beta, double omega, double* __restrict__ p,
+                         const double* __restrict__ invd, const BicgScalars* S, double* __restrict__ p,
                          double* __restrict__ phat) {
+  if (S->done) return;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  const double pt = r[t] + beta * (p[t] - omega * v[t]);
+  const double beta = S->it == 0 ? 0.0 : (S->rho_new / S->rho) * (S->alpha / S->omega);
+  const double pt = r[t] + beta * (p[t] - S->omega * v[t]);
   p[t] = pt;
   phat[t] = invd[t] * pt;
 }
 
 // s = r - alpha v, shat = M s
 __global__ void k_bicg_s(int64_t m, const double* __restrict__ r, const double* __restrict__ v,
-                         const double* __restrict__ invd, double alpha, double* __restrict__ sv,
+                         const double* __restrict__ invd, const BicgScalars* S, double* __restrict__ sv,
                          double* __restrict__ shat) {
+  if (S->done) return;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  const double st = r[t] - alpha * v[t];
+  const double st = r[t] - S->alpha * v[t];
   sv[t] = st;
   shat[t] = invd[t] * st;
 }
 
 // x += alpha phat + omega shat, r = s - omega t
 __global__ void k_bicg_xr(int64_t m, const double* __restrict__ phat, const double* __restrict__ shat,
-                          const double* __restrict__ sv, const double* __restrict__ tv, double alpha, double omega,
+                          const double* __restrict__ sv, const double* __restrict__ tv, const BicgScalars* S,
                           double* __restrict__ x, double* __restrict__ r) {
+  if (S->done) return;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  x[t] += alpha * phat[t] + omega * shat[t];
-  r[t] = sv[t] - omega * tv[t];
+  x[t] += S->alpha * phat[t] + S->omega * shat[t];
+  r[t] = sv[t] - S->omega * tv[t];
 }
 
 // H_ff x = g (g zero on the constrained DOFs) by right-preconditioned
-// BiCGSTAB on the exact Jacobian at the prepared state.
+// BiCGSTAB on the exact Jacobian at the prepared state.  The iterations are
+// enqueued in batches; the scalars stop the vector updates on the device as
+// soon as the solve has ended, so the few products left in a batch change
+// nothing.
 static int jacobian_bicgstab(lpm_handle* h, const double* g, double* x, double tol, long long maxit,
                              long long* iters, double* relres) {
   Dev& d = h->d;
   const int dim = h->dim;
   const int64_t m = (int64_t)h->n * dim;
   if (!d.tg_bicg) {
-    d.tg_bicg = (double*)dev_alloc(h, sizeof(double) * (size_t)(7 * m + 2));
+    d.tg_bicg = (double*)dev_alloc(h, sizeof(double) * (size_t)(7 * m) + sizeof(BicgScalars));
     if (!d.tg_bicg) return LPM_ERR_NOMEM;
   }
-  double *r = d.tg_bicg, *rh = r + m, *p = rh + m, *ph = p + m, *v = ph + m, *sv = v + m, *sh = sv + m,
-         *dots = sh + m;
+  double *r = d.tg_bicg, *rh = r + m, *p = rh + m, *ph = p + m, *v = ph + m, *sv = v + m, *sh = sv + m;
+  BicgScalars* S = reinterpret_cast<BicgScalars*>(sh + m);
   double* tv = d.adj_q;  // t = H shat
   k_jac_invdiag<<<grid_for(h->n, 128), 128, 0, h->stream>>>(h->n, dim, d.bptr, d.blayer, d.opp, d.cs, d.dis,
                                                             d.bdamage, d.bforce, d.Kn, d.Tv, d.mask, d.adj_invd);
@@ -705,65 +751,49 @@ static int jacobian_bicgstab(lpm_handle* h, const double* g, double* x, double t
   LPM_CUDA(h, cudaMemsetAsync(v, 0, sizeof(double) * m, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(r, g, sizeof(double) * m, cudaMemcpyDeviceToDevice, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(rh, g, sizeof(double) * m, cudaMemcpyDeviceToDevice, h->stream));
-  auto dot2 = [&](const double* a, const double* b, const double* c, const double* e, double out[2]) -> int {
-    k_dot2<<<GV, 256, 0, h->stream>>>(m, a, b, c, e, d.red.partials, d.red.ticket + 9, dots);
-    LPM_LAUNCHED(h, "k_dot2");
-    LPM_CUDA(h, cudaMemcpyAsync(h->h_norms, dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  unsigned int* ticket = d.red.ticket + 9;
+  k_bicg_dot<kBicgInit><<<GV, 256, 0, h->stream>>>(m, g, g, rh, r, d.red.partials, ticket, S, tol, maxit);
+  LPM_LAUNCHED(h, "k_bicg_dot");
+  BicgScalars hs{};
+  long long batch = 4;
+  for (;;) {
+    for (long long k = 0; k < batch; ++k) {
+      k_bicg_p<<<GE, T, 0, h->stream>>>(m, r, v, d.adj_invd, S, p, ph);
+      LPM_LAUNCHED(h, "k_bicg_p");
+      if (coarse) {
+        const int st = coarse_apply64(h, p, d.adj_invd, ph);
+        if (st) return st;
+      }
+      int st = apply_jacobian(h, ph, v, true, nullptr);
+      if (st) return st;
+      k_bicg_dot<kBicgAlpha><<<GV, 256, 0, h->stream>>>(m, rh, v, rh, v, d.red.partials, ticket, S, tol, maxit);
+      LPM_LAUNCHED(h, "k_bicg_dot");
+      k_bicg_s<<<GE, T, 0, h->stream>>>(m, r, v, d.adj_invd, S, sv, sh);
+      LPM_LAUNCHED(h, "k_bicg_s");
+      if (coarse) {
+        st = coarse_apply64(h, sv, d.adj_invd, sh);
+        if (st) return st;
+      }
+      st = apply_jacobian(h, sh, tv, true, nullptr);
+      if (st) return st;
+      k_bicg_dot<kBicgOmega><<<GV, 256, 0, h->stream>>>(m, tv, sv, tv, tv, d.red.partials, ticket, S, tol, maxit);
+      LPM_LAUNCHED(h, "k_bicg_dot");
+      k_bicg_xr<<<GE, T, 0, h->stream>>>(m, ph, sh, sv, tv, S, x, r);
+      LPM_LAUNCHED(h, "k_bicg_xr");
+      k_bicg_dot<kBicgRes><<<GV, 256, 0, h->stream>>>(m, r, r, rh, r, d.red.partials, ticket, S, tol, maxit);
+      LPM_LAUNCHED(h, "k_bicg_dot");
+    }
+    LPM_CUDA(h, cudaMemcpyAsync(&hs, S, sizeof(BicgScalars), cudaMemcpyDeviceToHost, h->stream));
     LPM_CUDA(h, cudaStreamSynchronize(h->stream));
-    out[0] = h->h_norms[0];
-    out[1] = h->h_norms[1];
-    return LPM_OK;
-  };
-  double q[2];
-  int st = dot2(g, g, rh, r, q);
-  if (st) return st;
-  const double bnorm = sqrt(q[0]);
-  double rho = 1.0, alpha = 1.0, omega = 1.0, rho_new = q[1], rn = bnorm;
-  long long it = 0;
-  if (!std::isfinite(bnorm)) {
-    h->err = "tangent: non-finite right-hand side";
+    if (hs.done) break;
+    if (batch < 32) batch *= 2;
+  }
+  if (hs.done == 3) {
+    h->err = hs.it == 0 ? "tangent: non-finite right-hand side" : "tangent: non-finite value in BiCGSTAB";
     return LPM_ERR_NONFINITE;
   }
-  while (bnorm > 0.0 && rn > tol * bnorm && it < maxit) {
-    if (rho_new == 0.0 || omega == 0.0) break;  // breakdown: reported as not converged
-    const double beta = (rho_new / rho) * (alpha / omega);
-    k_bicg_p<<<GE, T, 0, h->stream>>>(m, r, v, d.adj_invd, it == 0 ? 0.0 : beta, omega, p, ph);
-    LPM_LAUNCHED(h, "k_bicg_p");
-    if (coarse) {
-      st = coarse_apply64(h, p, d.adj_invd, ph);
-      if (st) return st;
-    }
-    st = apply_jacobian(h, ph, v, true, nullptr);
-    if (st) return st;
-    st = dot2(rh, v, rh, v, q);
-    if (st) return st;
-    alpha = rho_new / q[0];
-    k_bicg_s<<<GE, T, 0, h->stream>>>(m, r, v, d.adj_invd, alpha, sv, sh);
-    LPM_LAUNCHED(h, "k_bicg_s");
-    if (coarse) {
-      st = coarse_apply64(h, sv, d.adj_invd, sh);
-      if (st) return st;
-    }
-    st = apply_jacobian(h, sh, tv, true, nullptr);
-    if (st) return st;
-    st = dot2(tv, sv, tv, tv, q);
-    if (st) return st;
-    omega = q[1] > 0.0 ? q[0] / q[1] : 0.0;
-    k_bicg_xr<<<GE, T, 0, h->stream>>>(m, ph, sh, sv, tv, alpha, omega, x, r);
-    LPM_LAUNCHED(h, "k_bicg_xr");
-    rho = rho_new;
-    st = dot2(r, r, rh, r, q);
-    if (st) return st;
-    rn = sqrt(q[0]);
-    rho_new = q[1];
-    ++it;
-    if (!std::isfinite(rn)) {
-      h->err = "tangent: non-finite value in BiCGSTAB";
-      return LPM_ERR_NONFINITE;
-    }
-  }
-  if (iters) *iters = it;
-  *relres = bnorm > 0.0 ? rn / bnorm : 0.0;
+  if (iters) *iters = hs.it;
+  *relres = hs.bnorm > 0.0 ? sqrt(hs.rr) / hs.bnorm : 0.0;
   return LPM_OK;
 }
 
