@@ -345,6 +345,13 @@ int lpm_set_cg_loop(lpm_handle* h, int mode);
 #define LPM_PRECOND_JACOBI 0
 #define LPM_PRECOND_COARSE 1
 int lpm_set_preconditioner(lpm_handle* h, int kind, double box);
+/* The aggregates LPM_PRECOND_COARSE forms, without a device: boxes of edge
+ * `box` (0: automatic) from the lowest corner of the particles' bounding
+ * box, numbered in the order of their first particle.  xyz0: n*3 initial
+ * positions; agg[n] receives each particle's aggregate, *nagg their count
+ * (times 3 in 2-D, 6 in 3-D: the coarse DOFs), *edge (may be NULL) the edge
+ * used. */
+int lpm_coarse_boxes(int dim, int n, const double* xyz0, double box, int* agg, int* nagg, double* edge);
 /* The handle's CUDA stream (cudaStream_t), for callers that time or order
  * work around the library. */
 int lpm_get_stream(const lpm_handle* h, void** stream);

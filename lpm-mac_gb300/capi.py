@@ -141,6 +141,7 @@ def load(build_if_needed=True):
         "lpm_set_kernel_timing": [H, ctypes.c_int],
         "lpm_set_cg_loop": [H, ctypes.c_int],
         "lpm_set_preconditioner": [H, ctypes.c_int, ctypes.c_double],
+        "lpm_coarse_boxes": [ctypes.c_int, ctypes.c_int, dp, ctypes.c_double, ip, ip, dp],
         "lpm_get_stream": [H, ctypes.POINTER(ctypes.c_void_p)],
         "lpm_synchronize": [H],
         "lpm_find_bonds": [ctypes.c_int, dp, ctypes.c_double, ctypes.c_double, i64, ip, ip, ip, i64p],
@@ -179,7 +180,7 @@ def exported_symbols():
             "lpm_update_geometry_force", "lpm_residual", "lpm_assemble", "lpm_get_K", "lpm_set_operator",
             "lpm_apply_operator", "lpm_solve",
             "lpm_move_by_disp", "lpm_newton", "lpm_load_step", "lpm_store_state", "lpm_reset_state",
-            "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_set_cg_loop", "lpm_set_preconditioner", "lpm_get_stream", "lpm_synchronize",
+            "lpm_get_stats", "lpm_reset_stats", "lpm_set_kernel_timing", "lpm_set_cg_loop", "lpm_set_preconditioner", "lpm_coarse_boxes", "lpm_get_stream", "lpm_synchronize",
             "lpm_find_bonds", "lpm_find_neighbors", "lpm_fatigue_cycle", "lpm_fatigue_run", "lpm_backward_step", "lpm_apply_jacobian", "lpm_checkpoint_save", "lpm_checkpoint_restore",
             "lpm_checkpoint_drop", "lpm_tangent_begin", "lpm_tangent_bond_constants", "lpm_tangent_bond_scrit",
             "lpm_tangent_get",
@@ -234,6 +235,20 @@ def find_neighbors(xyz, radius):
     if st != OK:
         raise LpmError(st, L.lpm_last_error(None).decode())
     return ptr, idx
+
+
+def coarse_boxes(dim, xyz0, box=0.0):
+    """The aggregates of the coarse-space preconditioner (lpm_coarse_boxes,
+    host only): (aggregate id per particle, count, box edge used)."""
+    L = load()
+    x = np.ascontiguousarray(xyz0, dtype=np.float64).reshape(-1, 3)
+    agg = np.zeros(len(x), np.int32)
+    nagg = ctypes.c_int()
+    edge = ctypes.c_double()
+    st = L.lpm_coarse_boxes(int(dim), len(x), _d(x), float(box), _i(agg), ctypes.byref(nagg), ctypes.byref(edge))
+    if st != OK:
+        raise LpmError(st, L.lpm_last_error(None).decode())
+    return agg, nagg.value, edge.value
 
 
 def _d(a):

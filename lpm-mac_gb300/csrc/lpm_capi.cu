@@ -773,6 +773,15 @@ int lpm_set_preconditioner(lpm_handle* h, int kind, double box) {
   return LPM_OK;
 }
 
+int lpm_coarse_boxes(int dim, int n, const double* xyz0, double box, int* agg, int* nagg, double* edge) {
+  if ((dim != 2 && dim != 3) || n < 0 || (n > 0 && (!xyz0 || !agg)) || !nagg || !(box >= 0.0)) {
+    lpm::set_global_error("lpm_coarse_boxes: bad arguments");
+    return LPM_ERR_ARG;
+  }
+  *nagg = lpm::coarse_boxes(dim, n, xyz0, box, agg, edge);
+  return LPM_OK;
+}
+
 int lpm_set_kernel_timing(lpm_handle* h, int on) {
   if (!h) return LPM_ERR_ARG;
   h->timing = on != 0;

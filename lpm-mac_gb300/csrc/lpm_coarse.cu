@@ -253,6 +253,37 @@ __global__ void k_coarse_prolong64(int n, const int* __restrict__ agg, const flo
 
 }  // namespace
 
+// The aggregates: boxes of edge `box` from the lowest corner of the
+// particles' bounding box (box <= 0: the edge that gives about
+// kCoarseTarget coarse DOFs for the box volume), numbered in the order of
+// their first particle.  Writes agg[n] and the edge used; returns the count.
+int coarse_boxes(int dim, int n, const double* x0, double box, int* agg, double* edge_out) {
+  const int nm = dim == 3 ? 6 : 3;
+  double lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = hi[k] = n ? x0[k] : 0.0;
+    for (int i = 0; i < n; ++i) {
+      lo[k] = std::min(lo[k], x0[3 * i + k]);
+      hi[k] = std::max(hi[k], x0[3 * i + k]);
+    }
+  }
+  double edge = box;
+  if (!(edge > 0.0)) {
+    double vol = 1.0;
+    for (int k = 0; k < dim; ++k) vol *= std::max(hi[k] - lo[k], 1e-300);
+    edge = std::pow(vol / std::max(1, kCoarseTarget / nm), 1.0 / dim);
+  }
+  std::unordered_map<int64_t, int> box_id;
+  for (int i = 0; i < n; ++i) {
+    int64_t key = 0;
+    for (int k = 0; k < dim; ++k) key = key * 2000003 + (int64_t)std::floor((x0[3 * i + k] - lo[k]) / edge);
+    auto it = box_id.emplace(key, (int)box_id.size()).first;
+    agg[i] = it->second;
+  }
+  if (edge_out) *edge_out = edge;
+  return (int)box_id.size();
+}
+
 int coarse_setup(lpm_handle* h) {
   Dev& d = h->d;
   const int n = h->n, dim = h->dim, nm = dim == 3 ? 6 : 3;
@@ -263,29 +294,9 @@ int coarse_setup(lpm_handle* h) {
   LPM_CUDA(h, cudaMemcpyAsync(cptr.data(), d.cptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, h->stream));
   LPM_CUDA(h, cudaMemcpyAsync(cidx.data(), d.cidx, sizeof(int) * h->nblk, cudaMemcpyDeviceToHost, h->stream));
   LPM_CUDA(h, cudaStreamSynchronize(h->stream));
-  double lo[3], hi[3];
-  for (int k = 0; k < 3; ++k) {
-    lo[k] = hi[k] = n ? x0[k] : 0.0;
-    for (int i = 0; i < n; ++i) {
-      lo[k] = std::min(lo[k], x0[3 * i + k]);
-      hi[k] = std::max(hi[k], x0[3 * i + k]);
-    }
-  }
-  double edge = h->cbox;
-  if (!(edge > 0.0)) {
-    double vol = 1.0;
-    for (int k = 0; k < dim; ++k) vol *= std::max(hi[k] - lo[k], 1e-300);
-    edge = std::pow(vol / std::max(1, kCoarseTarget / nm), 1.0 / dim);
-  }
-  std::unordered_map<int64_t, int> box_id;
   std::vector<int> agg((size_t)n);
-  for (int i = 0; i < n; ++i) {
-    int64_t key = 0;
-    for (int k = 0; k < dim; ++k) key = key * 2000003 + (int64_t)std::floor((x0[3 * i + k] - lo[k]) / edge);
-    auto it = box_id.emplace(key, (int)box_id.size()).first;
-    agg[(size_t)i] = it->second;
-  }
-  const int nagg = (int)box_id.size();
+  double edge = 0.0;
+  const int nagg = coarse_boxes(dim, n, x0.data(), h->cbox, agg.data(), &edge);
   if ((long long)nagg * nm > kCoarseMax) {
     h->err = "coarse preconditioner: " + std::to_string(nagg) + " aggregates exceed " +
              std::to_string(kCoarseMax / nm) + "; give a larger box";

@@ -297,6 +297,7 @@ int mf_graph_product(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, b
 int mf_graph_residual(lpm_handle* h, cudaGraph_t g, const cudaGraphNode_t* dep, cudaGraphNode_t* last);
 // coarse-space preconditioner (lpm_coarse.cu): aggregates once per handle,
 // the coarse operator's inverse once per assembly
+int coarse_boxes(int dim, int n, const double* x0, double box, int* agg, double* edge_out);
 int coarse_setup(lpm_handle* h);
 int coarse_assemble(lpm_handle* h);
 // z = invd r + P A_c^-1 P^T r for FP64 device vectors (the tangent solves),
