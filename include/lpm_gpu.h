@@ -340,7 +340,11 @@ int lpm_set_cg_loop(lpm_handle* h, int mode);
  *                       each assembly.  Needs the assembled symmetric
  *                       tangent (LPM_ERR_STATE otherwise) and runs the
  *                       mixed solve as one persistent kernel whatever
- *                       lpm_set_cg_loop says.  The FP64 solve keeps Jacobi.
+ *                       lpm_set_cg_loop says.  The FP64 solve keeps Jacobi;
+ *                       the tangent solves (lpm_tangent_begin) use it as
+ *                       BiCGSTAB's right preconditioner.  A new box edge
+ *                       rebuilds the aggregates on the next solve (the
+ *                       previous arrays stay allocated until lpm_destroy).
  * The same solution to the solve tolerance; other iterates and counts. */
 #define LPM_PRECOND_JACOBI 0
 #define LPM_PRECOND_COARSE 1
