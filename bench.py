@@ -30,6 +30,8 @@ Reported (one JSON line on rank 0):
                generator's bonds) and the creation of the device lattice
   fatigue      compact-tension fatigue cycles at full size (configuration 5)
   fatigue_coarse  the same cycles with the coarse-space preconditioner
+  fatigue_sensitivity  those cycles carrying the damage's tangents along the
+               HCF A and B, relative to fatigue_coarse
   softening    load steps of the notched plate with the softening bond law
                and damage rounds at full size (configuration 3): by default
                the one step in which the first bonds soften (about 170
@@ -365,7 +367,7 @@ def setup_cost(w, capi):
             "lattice_create_ms": (t3 - t2) * 1e3, "timing": "host wall clock, host arrays in and out"}
 
 
-def fatigue_cost(capi, local, cycles=3, precond=None):
+def fatigue_cost(capi, local, cycles=3, precond=None, tangents=False):
     """Configuration 5 at full size: the compact-tension plate (hexagonal
     lattice, W = 40 mm from the load line, 0.15 mm spacing), HCF fatigue law
     with seeded per-particle A and B, nonlocal damage rate, pin loads
@@ -402,6 +404,14 @@ def fatigue_cost(capi, local, cycles=3, precond=None):
     r = g.load_step(fixed + [("force", gt, 0.0, R * f_max, 0.0), ("force", gb, 0.0, -R * f_max, 0.0)], **opts)
     if r["status"] != 0:
         raise RuntimeError("CT static step did not converge: %s" % r)
+    if tangents:
+        # d/d(log A) and d/dB of every particle's HCF parameters, carried
+        # through the cycles
+        da = np.zeros_like(params)
+        da[:, 0] = params[:, 0]
+        db = np.zeros_like(params)
+        db[:, 1] = 1.0
+        g.tangent_begin([da, db], tol=1e-10)
     unit = fixed + [("force", gt, 0.0, 1.0, 0.0), ("force", gb, 0.0, -1.0, 0.0)]
     spectrum = fat.ca_spectrum(f_max, R, 1000 * (cycles + 1))
     fat.run_cycles(g, unit, spectrum, 1, 0.001, max_calls=1, **opts)  # warm-up cycle
@@ -415,7 +425,8 @@ def fatigue_cost(capi, local, cycles=3, precond=None):
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
-    persistent = g.stats()["persistent_solves"]
+    stats = g.stats()
+    persistent = stats["persistent_solves"]
     g.close()
     if any(rc["status"] != 0 for rc in recs):
         raise RuntimeError("CT fatigue cycle did not converge")
@@ -427,7 +438,9 @@ def fatigue_cost(capi, local, cycles=3, precond=None):
             "cycle": "1 increment up, 1 down, cycle jump 1000 (lpm_fatigue_run)", "precision": "mixed",
             "persistent_solves": persistent,
             "preconditioner": "Jacobi (the reference's)" if precond is None else
-            "Jacobi plus rigid-body modes of particle boxes (lpm_set_preconditioner, automatic box)"}
+            "Jacobi plus rigid-body modes of particle boxes (lpm_set_preconditioner, automatic box)",
+            **({"tangent_directions": "d/d(log A), d/dB of the HCF law", "tangent_cg_iters": stats["tangent_cg_iters"]}
+               if tangents else {})}
 
 
 def softening_cost(capi, local, steps=4, max_warm=15, precond=None, tangents=False):
@@ -945,6 +958,10 @@ def run_gb300(args):
     run_leg(line, "setup", setup_cost, w, capi)
     run_leg(line, "fatigue", fatigue_cost, capi, local)
     run_leg(line, "fatigue_coarse", fatigue_cost, capi, local, precond=capi.PRECOND_COARSE)
+    run_leg(line, "fatigue_sensitivity", fatigue_cost, capi, local, precond=capi.PRECOND_COARSE, tangents=True)
+    fc, fs = line.get("fatigue_coarse", {}), line.get("fatigue_sensitivity", {})
+    if "ms_per_cycle" in fc and "ms_per_cycle" in fs:
+        fs["relative_to_forward_cycle"] = fs["ms_per_cycle"] / fc["ms_per_cycle"]
     if args.softening_steps > 0:
         run_leg(line, "softening", softening_cost, capi, local, steps=args.softening_steps)
         run_leg(line, "softening_coarse", softening_cost, capi, local, steps=args.softening_steps,
