@@ -51,3 +51,10 @@ def test_bad_arguments_refused():
         with pytest.raises(capi.LpmError) as e:
             capi.coarse_boxes(dim, x, box)
         assert e.value.code == capi.ERR_ARG
+
+
+def test_empty_and_single_particle_inputs():
+    agg, nagg, edge = capi.coarse_boxes(2, np.zeros((0, 3)), 1.0)
+    assert nagg == 0 and len(agg) == 0 and edge == 1.0
+    agg, nagg, edge = capi.coarse_boxes(3, np.array([[0.5, -1.0, 2.0]]), 0.0)
+    assert nagg == 1 and agg.tolist() == [0] and edge > 0.0
