@@ -272,6 +272,7 @@ int coarse_boxes(int dim, int n, const double* x0, double box, int* agg, double*
     double vol = 1.0;
     for (int k = 0; k < dim; ++k) vol *= std::max(hi[k] - lo[k], 1e-300);
     edge = std::pow(vol / std::max(1, kCoarseTarget / nm), 1.0 / dim);
+    if (!(edge > 0.0) || !std::isfinite(edge)) edge = 1.0;  // no extent (one particle): one box
   }
   std::unordered_map<int64_t, int> box_id;
   for (int i = 0; i < n; ++i) {
